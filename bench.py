@@ -1,0 +1,381 @@
+"""Benchmark: OSTR subset-iterations/s on the clinical DBT workload.
+
+Workload (``clinical``): volume 1024x512x60 @ 0.14x0.14x1.0 mm, detector
+1664x832 @ 0.14 mm, 25 views over +-25 deg, 25 subsets (one view each), Huber
+penalty delta 0.003/mm, beta 100, seeded synthetic breast phantom with 200
+glandular ellipsoids and 40 calcifications, counts Poisson(5e3 exp(-Ax)).
+
+Our arm: one step = one full OSTR iteration (25 sub-iterations, each a fused
+forward-projection+gradient kernel and a fused back-projection+penalty+update
+kernel) on device-resident data.  ``value`` = subset-iterations/s.  ``e2e`` =
+the same metric through ``ostr.reconstruct`` (the public call) from pinned host
+buffers: scan upload, gamma/d precompute, 50 iterations, volume download.
+
+``--impl reference``: the reference's algorithm on the host cores (the FP32
+CPU restatement of Tomo_OSTR_gold.cpp + Tomo_OSTR.cu, OpenMP over all
+cores), one step = one sub-iteration of the same workload.
+
+Multi-GPU (torchrun, N>1): independent replicas, one reconstruction per rank,
+no data-path collective; timing is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "OSTR subset-iterations/s"
+UNIT = "subset-iters/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="clinical")
+    ap.add_argument("--e2e-iters", type=int, default=None)
+    ap.add_argument("--e2e-runs", type=int, default=2)
+    ap.add_argument("--cpu-subiters", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_scan_gpu(cfg, seed):
+    """Phantom + counts; the counts' forward projection runs on the GPU."""
+    import torch
+
+    from newrecon_gb300 import ostr
+    from newrecon_gb300.phantom import breast_phantom, poisson_counts
+
+    g = cfg.geom
+    x = breast_phantom(g, seed, cfg.n_glandular, cfg.n_calc, thickness_mm=cfg.thickness_mm)
+    ostr.set_geometry(g)
+    idx = np.arange(g.n_angles, dtype=np.int32)
+    line = torch.zeros(g.n_angles * g.n_bins, device="cuda")
+    ostr.fprojectCB_1R_GPU_OSTR_cos(torch.from_numpy(x.ravel()).cuda(), line,
+                                    torch.from_numpy(cfg.angles).cuda(),
+                                    torch.from_numpy(idx).cuda(), 0, g.n_angles)
+    y = poisson_counts(line.cpu().numpy(), cfg.I0, seed)
+    b = np.full_like(y, cfg.I0)
+    return x.ravel(), y, b
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.p = None
+        self.path = os.path.join("/tmp", f"nr_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.p is None:
+            return None
+        time.sleep(0.2)
+        self.p.terminate()
+        self.p.wait()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in open(self.path):
+            parts = [s.strip() for s in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.isfile(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_info():
+    model = ""
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith(("model name", "cpu part")):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except OSError:
+        pass
+    return os.cpu_count(), model
+
+
+def cpu_port_subiters(cfg, x_true, y, b, d, n_sub: int, threads: int):
+    """FP32 CPU restatement, n_sub sub-iterations on the host cores (s per sub-iter)."""
+    from oracle.oracle import Oracle
+
+    g = cfg.geom
+    O = Oracle(np.float32)
+    O.set_threads(threads)
+    M = cfg.subset_num
+    A = g.n_angles
+    ridx = O.reorder_index(A, M)
+    yr = O.regroup(y, A, M)
+    br = O.regroup(b, A, M)
+    Vs = A // M
+    x = np.zeros(g.n_voxels, np.float32)
+    d = np.ascontiguousarray(d, np.float32)
+    times = []
+    for k in range(n_sub):
+        a = k % M
+        t0 = time.perf_counter()
+        O.subiter(g, cfg.angles, ridx, a * Vs, (a + 1) * Vs, yr[a * Vs * g.n_bins:(a + 1) * Vs * g.n_bins],
+                  br[a * Vs * g.n_bins:(a + 1) * Vs * g.n_bins], d, x, subset_num=M, beta=cfg.beta,
+                  delta=cfg.delta, potential=cfg.potential)
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from newrecon_gb300 import native, ostr
+    from newrecon_gb300.geometry import config
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    native.load()
+    cfg = config(args.config, seed=rank)
+    g = cfg.geom
+    x_true, y, b = make_scan_gpu(cfg, seed=rank)
+    plan = ostr.OSTR(g, subset_num=cfg.subset_num, beta=cfg.beta, delta=cfg.delta,
+                     potential=cfg.potential)
+    plan.setup(cfg.angles, y, b)
+    M = cfg.subset_num
+    xa = torch.zeros(g.n_voxels, device="cuda")
+    xb = torch.zeros(g.n_voxels, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step(evs=None):
+        nonlocal xa, xb
+        for a in range(M):
+            if evs is not None:
+                evs[0].record(stream)
+            plan.project(xa, a)
+            if evs is not None:
+                evs[1].record(stream)
+            plan.update(xa, xb, a)
+            if evs is not None:
+                evs[2].record(stream)
+                evs = evs[3:]
+            xa, xb = xb, xa
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    plan.check()
+    events = [torch.cuda.Event(enable_timing=True) for _ in range(3 * M * args.steps)]
+    clocks = Clocks(local)
+    clocks.start()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for s in range(args.steps):
+        step(events[3 * M * s:3 * M * (s + 1)])
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    elapsed = t_start.elapsed_time(t_end) / 1e3
+    if ws > 1:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    plan.check()
+    fp_ms = np.array([events[3 * k].elapsed_time(events[3 * k + 1]) for k in range(M * args.steps)])
+    up_ms = np.array([events[3 * k + 1].elapsed_time(events[3 * k + 2])
+                      for k in range(M * args.steps)])
+    n_sub = M * args.steps * ws
+    value = n_sub / elapsed
+    N = g.n_voxels
+    B = g.n_bins
+    Vs = g.n_angles // M
+    fp_bytes = 4 * N * Vs + 12 * B * Vs       # x read per view + y, b read + h written
+    up_bytes = 12 * N + 4 * B * Vs            # x, d read + x' written + h read
+    peak, peak_kind = measured_peaks()
+    kern = {
+        "ostr_fp_h": {"avg_ms": float(fp_ms.mean()), "bytes": fp_bytes,
+                      "gbs": fp_bytes / (fp_ms.mean() / 1e3) / 1e9},
+        "ostr_update": {"avg_ms": float(up_ms.mean()), "bytes": up_bytes,
+                        "gbs": up_bytes / (up_ms.mean() / 1e3) / 1e9},
+    }
+    dom = max(kern, key=lambda k: kern[k]["avg_ms"])
+    ach = kern[dom]["gbs"]
+    traffic = None
+    prof_traffic = os.path.join(HERE, "profiles", "dram_traffic.txt")
+    if os.path.isfile(prof_traffic):
+        for ln in open(prof_traffic):
+            parts = ln.split()
+            if len(parts) >= 2 and parts[0] == dom and not ln.startswith("#"):
+                traffic = float(parts[1])
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded breast phantom, Poisson counts)",
+        "config": {"workload": "clinical: 1024x512x60 vox @0.14x0.14x1mm, 1664x832 det @0.14mm, "
+                               "25 views +-25deg, 25 subsets, Huber d=0.003 b=100, I0=5e3",
+                   "step": "1 OSTR iteration = 25 sub-iterations", "parallelism": f"replicas x{ws}",
+                   "l2": "inputs larger than L2 (x, x', d: 3 x 126 MB; y, b: 2 x 138 MB)"},
+        "gpu_launches": 2 * M * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / peak,
+                     "traffic": traffic, "kernels": kern},
+    }
+    if clk is not None:
+        out["clocks"] = clk
+    if not args.no_e2e:
+        out["e2e"] = e2e_ours(args, cfg, y, b)
+    if rank == 0 and not args.no_cpu_baseline:
+        d = plan.section("d").cpu().numpy()
+        threads = os.cpu_count() or 1
+        times = cpu_port_subiters(cfg, x_true, y, b, d, args.cpu_subiters, threads)
+        ncpu, model = cpu_info()
+        out["cpu_baseline"] = {"value": len(times) / sum(times), "unit": UNIT, "cores": threads,
+                               "kind": "port",
+                               "sample": f"{len(times)} sub-iterations of the clinical workload "
+                                         f"(FP32 restatement, OpenMP), {model}"}
+    if ws > 1:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def e2e_ours(args, cfg, y, b):
+    import torch
+
+    from newrecon_gb300 import ostr
+
+    iters = args.e2e_iters or cfg.iter_num
+    g = cfg.geom
+    y_h = torch.from_numpy(y).pin_memory()
+    b_h = torch.from_numpy(b).pin_memory()
+    a_h = torch.from_numpy(cfg.angles).pin_memory()
+    kw = dict(angles=a_h, subset_num=cfg.subset_num, iter_num=iters, beta=cfg.beta,
+              delta=cfg.delta, potential=cfg.potential)
+    ostr.reconstruct(g, y_h, b_h, **kw)  # warm-up
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(args.e2e_runs):
+        t0 = time.perf_counter()
+        vol = ostr.reconstruct(g, y_h, b_h, **kw)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    assert vol.device.type == "cpu"
+    sub = iters * cfg.subset_num
+    return {"value": sub / float(np.mean(ts)), "unit": UNIT,
+            "h2d_bytes_per_step": int(y.nbytes + b.nbytes + cfg.angles.nbytes),
+            "d2h_bytes_per_step": int(g.n_voxels * 4),
+            "step": f"ostr.reconstruct from pinned host buffers: upload, gamma/d setup, "
+                    f"{iters} iterations x {cfg.subset_num} subsets, volume download",
+            "seconds_per_call": float(np.mean(ts))}
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    from newrecon_gb300.geometry import config
+    from newrecon_gb300.phantom import breast_phantom, poisson_counts
+    from oracle import build as obuild
+    from oracle.oracle import Oracle
+
+    if not os.path.isfile(obuild.ORACLE_SO):
+        obuild.build_oracle().wait()
+    cfg = config(args.config, seed=0)
+    g = cfg.geom
+    threads = os.cpu_count() or 1
+    O = Oracle(np.float32)
+    O.set_threads(threads)
+    x = breast_phantom(g, 0, cfg.n_glandular, cfg.n_calc, thickness_mm=cfg.thickness_mm).ravel()
+    idx = np.arange(g.n_angles, dtype=np.int32)
+    y = poisson_counts(O.fp_ostr(g, x, cfg.angles, idx, 0, g.n_angles), cfg.I0, 0)
+    b = np.full_like(y, cfg.I0)
+    # d = SBP(gamma * yry) over all views, as the reference precomputes it
+    gam = O.fp_gamma(g, cfg.angles, idx, 0, g.n_angles, "length")
+    d = O.bp_sbp(g, O.compute_yry(y) * gam, idx, cfg.angles, 0, g.n_angles)
+    times = cpu_port_subiters(cfg, x, y, b, d, args.warmup + args.steps, threads)[args.warmup:]
+    elapsed = float(sum(times))
+    value = len(times) / elapsed
+    ncpu, model = cpu_info()
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded breast phantom, Poisson counts)",
+        "config": {"workload": "clinical: 1024x512x60 vox @0.14x0.14x1mm, 1664x832 det @0.14mm, "
+                               "25 views +-25deg, 25 subsets, Huber d=0.003 b=100, I0=5e3",
+                   "step": "1 OSTR sub-iteration on the host cores", "parallelism": "host"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{len(times)} sub-iterations (FP32 restatement of the "
+                                   f"reference's gold path, OpenMP), {model}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

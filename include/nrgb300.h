@@ -1,0 +1,219 @@
+/*
+ * nrgb300.h -- C ABI of the GB300 OSTR reconstruction library (libnrgb300.so).
+ *
+ * Ordered-subsets transmission (OSTR) penalized-likelihood reconstruction for
+ * digital breast tomosynthesis.  Every entry point takes plain device pointers,
+ * element counts and a CUDA stream handle (passed as void*), returns an
+ * nr_status and never allocates: buffers (including scratch workspace) belong
+ * to the caller.  Geometry travels by value into the kernels, so the library
+ * holds no global state and calls on different streams may overlap.
+ *
+ * Layouts (the reference's, PranjalSahu/newrecon):
+ *   volume       [z][y][x], x fastest            (Tomo_OSTR.cu:538, :1604)
+ *   projections  [view][i<BINSx][j<BINSy], j fastest, after x_y_flip
+ *                                                 (Tomo_OSTR.cu:1365,
+ *                                                  Tomo_OSTR_gold.cpp:93-105)
+ *   index        int32 view order; [a0, a1) is half-open and indexes the
+ *                reordered index (Tomo_OSTR_gold.cpp:451)
+ *
+ * Every projector / back projector / prior ACCUMULATES or leaves untouched
+ * exactly what the reference does, so existing callers keep their
+ * zero-the-buffer-first discipline (Tomo_OSTR_gold.cpp:843-846).
+ */
+#ifndef NRGB300_H
+#define NRGB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  Replaces the reference's printf + exit(1) error paths
+ * (Tomo_OSTR_gold.cpp:121-125, Tomo_OSTR.cu:2232-2236, :2627-2630). */
+typedef enum nr_status {
+    NR_OK = 0,
+    NR_ERR_BAD_GEOMETRY = 1,   /* sizes <= 0, Vx != Vy, subset count not dividing views ... */
+    NR_ERR_BAD_ARGUMENT = 2,   /* null pointer, bad view range, delta <= 0, unknown enum */
+    NR_ERR_LAUNCH = 3,         /* a kernel launch failed */
+    NR_ERR_NONFINITE = 4,      /* NaN/Inf detected by a device status word */
+    NR_ERR_TIMEOUT = 5,        /* a bounded device wait gave up */
+    NR_ERR_WORKSPACE = 6,      /* workspace missing, too small or misaligned */
+    NR_ERR_CUDA = 7            /* any other CUDA runtime error */
+} nr_status;
+
+/* Scanner + grid geometry.  Field-for-field the reference's host globals
+ * h_IMGSIZx ... h_sourceY (Tomo_OSTR.cu:21-36, :47-50) and ostr.py:21-52. */
+typedef struct nr_geom {
+    int32_t nx, ny, nz;        /* IMGSIZx, IMGSIZy, IMGSIZz (voxels)            */
+    float vx, vy, vz;          /* Vsize_x, Vsize_y, Vsize_z (mm)                 */
+    float x_p0, y_p0, z_p0;    /* volume corner (mm)                             */
+    int32_t nbx, nby;          /* BINSx, BINSy (detector bins)                   */
+    float bx, by;              /* Bsize_x, Bsize_y (mm)                          */
+    float x_d0, y_d0;          /* detector corner (mm)                           */
+    float detectorR;           /* detector plane at z = -detectorR (mm)          */
+    float sourceR;             /* source at (R sin t, sourceY, R cos t) (mm)     */
+    float sourceY;
+    int32_t n_angles;          /* ANGLES                                         */
+} nr_geom;
+
+/* Penalty potentials (RDD += w*omega(t), RD += w*omega(t)*t, t = x_j - x_k). */
+enum {
+    NR_POT_Q2 = 0,         /* omega = 1                       G_Q2_prior      Tomo_OSTR.cu:118-184 */
+    NR_POT_LANGE = 1,      /* omega = 1/(1+|t|/delta)         G_Fessler_prior Tomo_OSTR.cu:187-255 */
+    NR_POT_HYPERBOLA = 2,  /* omega = 1/sqrt(1+(t/delta)^2)   formula of      Tomo_OSTR.cu:314     */
+    NR_POT_HUBER = 3       /* omega = min(1, delta/|t|)       (no reference counterpart)           */
+};
+
+/* Normalisation projection gamma. */
+enum {
+    NR_GAMMA_LENGTH = 0,   /* full source-to-bin length |src - bin| (Tomo_OSTR.cu:1172) */
+    NR_GAMMA_CHORD = 1     /* in-volume chord length (ostr.py:641, ostr.ipynb:815)      */
+};
+
+/* ---------------------------------------------------------------------------
+ * Geometry check.  Replaces the reference's scattered exit(1) checks:
+ * Vx == Vy (Tomo_OSTR_gold.cpp:380-386), subset_num | ANGLES
+ * (Tomo_OSTR.cu:2627-2630).  subset_num <= 0 skips the subset check.
+ * ------------------------------------------------------------------------- */
+nr_status nr_validate_geometry(const nr_geom* g, int32_t subset_num);
+
+/* ---------------------------------------------------------------------------
+ * Reference-shaped operators (drop-in for the launch wrappers).
+ * ------------------------------------------------------------------------- */
+
+/* line[(a-a0)][i][j] = cos(theta) * Siddon line integral of x for views
+ * index[a], a in [a0,a1).  Rays that miss the volume leave line untouched.
+ * Replaces fprojectCB_1R_GPU_OSTR_cos (Tomo_OSTR.cu:2334-2359; kernel :1313). */
+nr_status nr_fp_ostr(const nr_geom* g, const float* x, float* line,
+                     const float* angles, const int32_t* index,
+                     int32_t a0, int32_t a1, void* stream);
+
+/* gamma[(a-a0)][i][j] for rays that hit the volume (others untouched).
+ * mode = NR_GAMMA_LENGTH | NR_GAMMA_CHORD.
+ * Replaces fprojectCB_1R_GPU_OSTR_normprj (Tomo_OSTR.cu:2361-2393; :1378). */
+nr_status nr_fp_gamma(const nr_geom* g, float* gamma,
+                      const float* angles, const int32_t* index,
+                      int32_t a0, int32_t a1, int32_t mode, void* stream);
+
+/* vol[j] += sum over views of the voxel-driven bilinear back projection of
+ * prj (SBP, depth weighted).  Deterministic gather, no atomics.
+ * Replaces bprojectCB_GPU_SBP (Tomo_OSTR.cu:2435-2457; kernel :1553). */
+nr_status nr_bp_sbp(const nr_geom* g, float* vol, const float* prj,
+                    const int32_t* index, const float* angles,
+                    int32_t a0, int32_t a1, void* stream);
+
+/* RDD += sum_k w_k omega(t), RD += sum_k w_k omega(t) t over the 26-neighbourhood.
+ * Replaces prior_GPU_OSTR (Lange, Tomo_OSTR.cu:2216-2245) and
+ * prior_GPU_OSTR_Q2 (Tomo_OSTR.cu:2189-2213).  delta must be > 0 unless Q2. */
+nr_status nr_prior(const nr_geom* g, float* RDD, float* RD, const float* x,
+                   int32_t potential, float delta, float z_xy_ratio, void* stream);
+
+/* Element-wise host helpers of the reference, on the device. */
+/* compute_yry (Tomo_OSTR_gold.cpp:183-205); scat may be NULL (r = 0). */
+nr_status nr_compute_yry(float* yry, const float* prj, const float* scat,
+                         int64_t n, void* stream);
+/* compute_gamma_yry (Tomo_OSTR_gold.cpp:208-218). */
+nr_status nr_compute_gamma_yry(float* out, const float* yry, const float* gamma,
+                               int64_t n, void* stream);
+/* compute_h (Tomo_OSTR_gold.cpp:245-260); scat may be NULL. */
+nr_status nr_compute_h(float* h, const float* prj, const float* blank,
+                       const float* line, const float* scat, int64_t n, void* stream);
+/* update_est (Tomo_OSTR_gold.cpp:265-295), in place on est. */
+nr_status nr_update_est(float* est, const float* capL, const float* RD,
+                        const float* d, const float* RDD, float beta,
+                        int64_t n, void* stream);
+/* buf *= s (the x subset_num scaling of capL, Tomo_OSTR_gold.cpp:767-771). */
+nr_status nr_scale(float* buf, float s, int64_t n, void* stream);
+/* regroup_prj (Tomo_OSTR_gold.cpp:220-242): out view (i*Vs + j) = in view (j*M + i). */
+nr_status nr_regroup(float* out, const float* in, int32_t n_angles,
+                     int32_t subset_num, int64_t b_size, void* stream);
+/* x_y_flip (Tomo_OSTR_gold.cpp:93-105) for n_views views: out[v][i][j] = in[v][j][i]. */
+nr_status nr_x_y_flip(float* out, const float* in, int32_t nbx, int32_t nby,
+                      int32_t n_views, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Fused device-resident OSTR (no reference counterpart as one call: it is the
+ * whole loop of ConebeamCT_OSTR_{LangePrior,Q2Prior}_GPU,
+ * Tomo_OSTR_gold.cpp:301-918 / :920-1469, kept on the GPU).
+ * ------------------------------------------------------------------------- */
+typedef struct nr_ostr_params {
+    int32_t subset_num;        /* M; must divide n_angles                        */
+    int32_t potential;         /* NR_POT_*                                       */
+    int32_t gamma_mode;        /* NR_GAMMA_*                                     */
+    int32_t has_scatter;       /* 0: r = 0 everywhere                            */
+    float beta;                /* penalty weight                                 */
+    float delta;               /* potential scale (1/mm), > 0 unless Q2          */
+} nr_ostr_params;
+
+/* Bytes of workspace the fused path needs for this geometry and parameters. */
+nr_status nr_ostr_workspace_size(const nr_geom* g, const nr_ostr_params* p,
+                                 size_t* bytes);
+
+/* Load the scan into the workspace and precompute the curvature d.
+ * prj, blank, scat: [view][i][j] in ORIGINAL view order (scat may be NULL).
+ * angles: n_angles float32 radians (device).  Equivalent to lines
+ * Tomo_OSTR_gold.cpp:409-642 (yry, gamma, gamma*yry, d, regroup, reorder). */
+nr_status nr_ostr_setup(const nr_geom* g, const nr_ostr_params* p,
+                        const float* angles, const float* prj, const float* blank,
+                        const float* scat, void* workspace, size_t ws_bytes,
+                        void* stream);
+
+/* First half of sub-iteration `subset`: the fused forward projection of x
+ * over the subset's views and the OSTR detector gradient
+ * h = (y/(b e^-l + r) - 1) b e^-l into the workspace (Tomo_OSTR_gold.cpp:732-756). */
+nr_status nr_ostr_project(const nr_geom* g, const nr_ostr_params* p, const float* x,
+                          int32_t subset, void* workspace, size_t ws_bytes, void* stream);
+
+/* Second half: x_out = max(0, x - (M SBP(h) + beta RD)/(d + 2 beta RDD)) with
+ * the penalty of x, fused (Tomo_OSTR_gold.cpp:759-814).  x_out != x. */
+nr_status nr_ostr_update(const nr_geom* g, const nr_ostr_params* p, const float* x,
+                         float* x_out, int32_t subset, void* workspace, size_t ws_bytes,
+                         void* stream);
+
+/* Workspace sections a caller may read (device pointer + byte size). */
+enum {
+    NR_WS_D = 0,          /* float[N]: curvature d                                   */
+    NR_WS_H = 1,          /* float[Vs][BINSy][BINSx]: last subset gradient h         */
+    NR_WS_Y = 2,          /* float[A][BINSy][BINSx]: counts, subset order            */
+    NR_WS_GAMMA_YRY = 3,  /* float[A][BINSy][BINSx]: gamma*yry, original order       */
+    NR_WS_INDEX = 4       /* int32[A]: subset-major view order                       */
+};
+nr_status nr_ostr_workspace_section(const nr_geom* g, const nr_ostr_params* p,
+                                    int32_t section, void* workspace, size_t ws_bytes,
+                                    void** ptr, size_t* bytes);
+
+/* Run n_iters full iterations (M sub-iterations each) on x in place
+ * ([z][y][x], non-negative).  Equivalent to Tomo_OSTR_gold.cpp:724-887. */
+nr_status nr_ostr_iterate(const nr_geom* g, const nr_ostr_params* p, float* x,
+                          int32_t n_iters, void* workspace, size_t ws_bytes,
+                          void* stream);
+
+/* One sub-iteration for subset a (0 <= a < M), x in place. */
+nr_status nr_ostr_subiter(const nr_geom* g, const nr_ostr_params* p, float* x,
+                          int32_t subset, void* workspace, size_t ws_bytes,
+                          void* stream);
+
+/* Penalized-likelihood objective in FP64 (no reference counterpart; the
+ * reference has no objective):
+ *   out[0] = sum_i (ybar_i + r_i - y_i log(ybar_i + r_i)),  ybar = b exp(-FP_cos(x))
+ *   out[1] = 1/2 sum_j sum_k w_jk psi(x_j - x_k)
+ * out is a device pointer to 2 doubles; total = out[0] + beta * out[1]. */
+nr_status nr_ostr_objective(const nr_geom* g, const nr_ostr_params* p,
+                            const float* x, double* out, void* workspace,
+                            size_t ws_bytes, void* stream);
+
+/* Reads and clears the workspace's device status word (NaN/Inf detection)
+ * after synchronising the stream.  *flags = 0 when clean. */
+nr_status nr_ostr_check(void* workspace, size_t ws_bytes, int32_t* flags,
+                        void* stream);
+
+/* Library version string. */
+const char* nr_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NRGB300_H */

@@ -1,0 +1,86 @@
+// common.cuh -- shared device helpers of libnrgb300 (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/nrgb300.h"
+
+#define NR_API extern "C" __attribute__((visibility("default")))
+
+// Status bits of the device status word kept in the workspace.
+#define NR_FLAG_NONFINITE 1
+#define NR_FLAG_TIMEOUT 2
+
+namespace nr {
+
+// Geometry as the kernels use it: the caller's nr_geom passed by value
+// (__grid_constant__) plus per-launch derived constants.
+struct Geo {
+    nr_geom g;
+    float xmax, ymax, zmax;  // far corner of the volume
+};
+
+__host__ inline Geo make_geo(const nr_geom& g) {
+    Geo d;
+    d.g = g;
+    d.xmax = g.x_p0 + (float)g.nx * g.vx;
+    d.ymax = g.y_p0 + (float)g.ny * g.vy;
+    d.zmax = g.z_p0 + (float)g.nz * g.vz;
+    return d;
+}
+
+// Source position for view angle theta: rotation about the y axis at the
+// origin, Tomo_OSTR.cu:1340-1345 (sinf/cosf of a float32 angle).
+__device__ __forceinline__ void source_pos(const nr_geom& g, float theta, float* x0, float* y0,
+                                           float* z0, float* ct) {
+    float s, c;
+    sincosf(theta, &s, &c);
+    *x0 = g.sourceR * s;
+    *z0 = g.sourceR * c;
+    *y0 = g.sourceY;
+    *ct = c;
+}
+
+// Bin centre on the stationary detector, Tomo_OSTR.cu:1349-1356.  The
+// reference forms x_d0 + (i+0.5)*Bsize in double and rounds once to float;
+// (i+0.5)*Bsize is exact in double, so one fused multiply-add (single
+// rounding of the exact value) reproduces it.
+__device__ __forceinline__ float bin_x(const nr_geom& g, int i) {
+    return __fmaf_rn((float)i + 0.5f, g.bx, g.x_d0);
+}
+__device__ __forceinline__ float bin_y(const nr_geom& g, int j) {
+    return __fmaf_rn((float)j + 0.5f, g.by, g.y_d0);
+}
+// Voxel centre, Tomo_OSTR.cu:1624-1626 (same double-then-round form).
+__device__ __forceinline__ float vox_x(const nr_geom& g, int i) {
+    return __fmaf_rn((float)i + 0.5f, g.vx, g.x_p0);
+}
+__device__ __forceinline__ float vox_y(const nr_geom& g, int i) {
+    return __fmaf_rn((float)i + 0.5f, g.vy, g.y_p0);
+}
+__device__ __forceinline__ float vox_z(const nr_geom& g, int i) {
+    return __fmaf_rn((float)i + 0.5f, g.vz, g.z_p0);
+}
+
+__host__ inline bool geom_ok(const nr_geom* g) {
+    if (!g) return false;
+    if (g->nx <= 0 || g->ny <= 0 || g->nz <= 0 || g->nbx <= 0 || g->nby <= 0 || g->n_angles <= 0)
+        return false;
+    if (!(g->vx > 0.f) || !(g->vy > 0.f) || !(g->vz > 0.f) || !(g->bx > 0.f) || !(g->by > 0.f))
+        return false;
+    if ((int64_t)g->nx * g->ny * g->nz >= (int64_t)1 << 31) return false;
+    if ((int64_t)g->nbx * g->nby * g->n_angles >= (int64_t)1 << 31) return false;
+    return true;
+}
+
+__host__ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+__host__ inline nr_status launch_status() {
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? NR_OK : NR_ERR_LAUNCH;
+}
+
+__host__ inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
+
+}  // namespace nr

@@ -1,0 +1,175 @@
+// fp.cu -- ray-driven cone-beam forward projectors (Siddon exact chord lengths).
+//
+// One thread per detector bin, a warp per 32 consecutive bins of one detector
+// column j (lanes along i, the detector x axis).  Adjacent lanes trace nearly
+// parallel rays 1 bin apart in x, so at every step their volume reads fall on
+// the same few 128-byte lines of one volume row (the volume is x-fastest):
+// the gathers coalesce.  Views of a launch run on gridDim.z.  The walk itself
+// is in siddon.cuh.
+#include "siddon.cuh"
+
+namespace nr {
+
+// Detector offset of bin (i, j) of one view: JI -> [j][i] (i fastest, the
+// layout of the fused path and of the scanner files); otherwise [i][j] (the
+// reference's in-memory layout, Tomo_OSTR.cu:1365).
+template <bool JI>
+__device__ __forceinline__ int64_t bin_off(const nr_geom& g, int i, int j) {
+    return JI ? (int64_t)j * g.nbx + i : (int64_t)i * g.nby + j;
+}
+
+// Reference-shaped projector: out[(a-a0)] = cos * line integral (MODE 0) or
+// gamma (MODE 1 chord, MODE 2 length); missed rays leave out untouched
+// (Tomo_OSTR.cu:1367-1373, :1440-1446).
+template <int MODE, bool JI>
+__global__ void __launch_bounds__(128) fp_kernel(const __grid_constant__ Geo G,
+                                                 const float* __restrict__ vol,
+                                                 float* __restrict__ out,
+                                                 const float* __restrict__ angles,
+                                                 const int32_t* __restrict__ index, int a0) {
+    const nr_geom& g = G.g;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.nbx || j >= g.nby) return;
+    const int a = a0 + blockIdx.z;
+    const float theta = angles[index[a]];
+    float x0, y0, z0, ct;
+    source_pos(g, theta, &x0, &y0, &z0, &ct);
+    float v;
+    if (trace<MODE>(G, vol, x0, y0, z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v)) {
+        const int64_t o = (int64_t)blockIdx.z * g.nbx * g.nby + bin_off<JI>(g, i, j);
+        out[o] = (MODE == 0) ? v * ct : v;
+    }
+}
+
+// Fused forward projection + OSTR gradient h for the subset views of the
+// device-resident path.  Detector arrays are [view][j][i] in subset order;
+// y, b (and r) are indexed by the subset position a.  Rays that miss the
+// volume have line = 0 (the reference zeroes the line buffer every subset,
+// Tomo_OSTR_gold.cpp:843).  h = (y/(b e^-l + r) - 1) b e^-l,
+// Tomo_OSTR_gold.cpp:245-260.
+__global__ void __launch_bounds__(128) fp_h_kernel(const __grid_constant__ Geo G,
+                                                   const float* __restrict__ vol,
+                                                   float* __restrict__ h,
+                                                   const float* __restrict__ angles,
+                                                   const int32_t* __restrict__ index, int a0,
+                                                   const float* __restrict__ y,
+                                                   const float* __restrict__ b,
+                                                   const float* __restrict__ r) {
+    const nr_geom& g = G.g;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.nbx || j >= g.nby) return;
+    const int a = a0 + blockIdx.z;
+    const float theta = angles[index[a]];
+    float x0, y0, z0, ct;
+    source_pos(g, theta, &x0, &y0, &z0, &ct);
+    float v = 0.f;
+    float l = 0.f;
+    if (trace<0>(G, vol, x0, y0, z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v)) l = v * ct;
+    const int64_t B = (int64_t)g.nbx * g.nby;
+    const int64_t o = (int64_t)a * B + bin_off<true>(g, i, j);
+    const float yb = b[o] * expf(-l);
+    const float den = yb + (r ? r[o] : 0.f);
+    h[(int64_t)blockIdx.z * B + bin_off<true>(g, i, j)] = (__fdiv_rn(y[o], den) - 1.f) * yb;
+}
+
+// gamma * yry for every view in one pass (the d precompute's detector term,
+// Tomo_OSTR_gold.cpp:183-218), [view][j][i], original view order, identity
+// index.  yry = (y-r)^2/y with the reference's guards.
+template <int MODE>
+__global__ void __launch_bounds__(128) gamma_yry_kernel(const __grid_constant__ Geo G,
+                                                        float* __restrict__ out,
+                                                        const float* __restrict__ angles,
+                                                        const float* __restrict__ y,
+                                                        const float* __restrict__ r) {
+    const nr_geom& g = G.g;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.nbx || j >= g.nby) return;
+    const int a = blockIdx.z;
+    float x0, y0, z0, ct;
+    source_pos(g, angles[a], &x0, &y0, &z0, &ct);
+    float gam = 0.f;  // gamma buffer is zeroed before the projection (Tomo_OSTR_gold.cpp:441)
+    float v;
+    if (trace<MODE>(G, nullptr, x0, y0, z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v)) gam = v;
+    const int64_t o = (int64_t)a * g.nbx * g.nby + bin_off<true>(g, i, j);
+    const float yy = y[o];
+    float c = 0.f;
+    if (yy != 0.f) {
+        float dif = yy - (r ? r[o] : 0.f);
+        if (dif <= 0.f) dif = yy;
+        c = __fdiv_rn(dif * dif, yy);
+    }
+    out[o] = c * gam;
+}
+
+}  // namespace nr
+
+using namespace nr;
+
+static nr_status check_views(const nr_geom* g, const float* angles, const int32_t* index,
+                             int32_t a0, int32_t a1) {
+    if (!geom_ok(g)) return NR_ERR_BAD_GEOMETRY;
+    if (!angles || !index || a0 < 0 || a1 < a0) return NR_ERR_BAD_ARGUMENT;
+    if (a1 - a0 > 65535) return NR_ERR_BAD_ARGUMENT;
+    return NR_OK;
+}
+
+NR_API nr_status nr_fp_ostr(const nr_geom* g, const float* x, float* line, const float* angles,
+                            const int32_t* index, int32_t a0, int32_t a1, void* stream) {
+    nr_status st = check_views(g, angles, index, a0, a1);
+    if (st != NR_OK) return st;
+    if (!x || !line) return NR_ERR_BAD_ARGUMENT;
+    if (a1 == a0) return NR_OK;
+    dim3 blk(32, 4), grd(cdiv(g->nbx, 32), cdiv(g->nby, 4), a1 - a0);
+    fp_kernel<0, false><<<grd, blk, 0, as_stream(stream)>>>(make_geo(*g), x, line, angles, index, a0);
+    return launch_status();
+}
+
+NR_API nr_status nr_fp_gamma(const nr_geom* g, float* gamma, const float* angles,
+                             const int32_t* index, int32_t a0, int32_t a1, int32_t mode,
+                             void* stream) {
+    nr_status st = check_views(g, angles, index, a0, a1);
+    if (st != NR_OK) return st;
+    if (!gamma || (mode != NR_GAMMA_LENGTH && mode != NR_GAMMA_CHORD)) return NR_ERR_BAD_ARGUMENT;
+    if (a1 == a0) return NR_OK;
+    dim3 blk(32, 4), grd(cdiv(g->nbx, 32), cdiv(g->nby, 4), a1 - a0);
+    if (mode == NR_GAMMA_LENGTH)
+        fp_kernel<2, false><<<grd, blk, 0, as_stream(stream)>>>(make_geo(*g), nullptr, gamma,
+                                                                angles, index, a0);
+    else
+        fp_kernel<1, false><<<grd, blk, 0, as_stream(stream)>>>(make_geo(*g), nullptr, gamma,
+                                                                angles, index, a0);
+    return launch_status();
+}
+
+// Internal launchers used by the device-resident path (ostr.cu).
+namespace nr {
+
+nr_status launch_fp_h(const nr_geom& g, const float* x, float* h, const float* angles,
+                      const int32_t* index, int a0, int nviews, const float* y, const float* b,
+                      const float* r, cudaStream_t st) {
+    dim3 blk(32, 4), grd(cdiv(g.nbx, 32), cdiv(g.nby, 4), nviews);
+    fp_h_kernel<<<grd, blk, 0, st>>>(make_geo(g), x, h, angles, index, a0, y, b, r);
+    return launch_status();
+}
+
+nr_status launch_fp_ji(const nr_geom& g, const float* x, float* line, const float* angles,
+                       const int32_t* index, int a0, int nviews, cudaStream_t st) {
+    dim3 blk(32, 4), grd(cdiv(g.nbx, 32), cdiv(g.nby, 4), nviews);
+    fp_kernel<0, true><<<grd, blk, 0, st>>>(make_geo(g), x, line, angles, index, a0);
+    return launch_status();
+}
+
+nr_status launch_gamma_yry(const nr_geom& g, int gamma_mode, float* out, const float* angles,
+                           const float* y, const float* r, cudaStream_t st) {
+    dim3 blk(32, 4), grd(cdiv(g.nbx, 32), cdiv(g.nby, 4), g.n_angles);
+    if (gamma_mode == NR_GAMMA_CHORD)
+        gamma_yry_kernel<1><<<grd, blk, 0, st>>>(make_geo(g), out, angles, y, r);
+    else
+        gamma_yry_kernel<2><<<grd, blk, 0, st>>>(make_geo(g), out, angles, y, r);
+    return launch_status();
+}
+
+}  // namespace nr

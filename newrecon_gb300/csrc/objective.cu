@@ -1,0 +1,202 @@
+// objective.cu -- FP64 penalized-likelihood objective of the device-resident
+// path (the reference has no objective; the nearest is the ML cost of
+// ReconDBT/ML_dbt.m:88-106):
+//
+//   data    = sum_i (ybar_i + r_i - y_i log(ybar_i + r_i)),  ybar = b exp(-FP_cos(x))
+//   penalty = 1/2 sum_j sum_{k in N26(j)} w_jk psi(x_j - x_k)
+//           = sum over neighbour pairs {j,k} inside the volume of w_jk psi(t)
+//
+// with psi the potential whose derivative is omega(t) t (Q2 t^2/2; Lange
+// d^2(|t|/d - log(1+|t|/d)); hyperbola d^2(sqrt(1+(t/d)^2) - 1); Huber t^2/2 or
+// d|t| - d^2/2).  Out-of-volume neighbours have t = 0 and psi(0) = 0.
+// Per-bin and per-pair terms are summed in double: per thread, then warp
+// shuffles, then a per-block partial; a single block adds the partials in a
+// fixed order, so the value is deterministic.
+#include <cmath>
+
+#include "siddon.cuh"
+
+namespace nr {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block sum of v written to red[blk] by thread 0 (blockDim multiple of 32, <= 1024).
+__device__ __forceinline__ void block_partial(double v, double* red, int64_t blk) {
+    __shared__ double ws[32];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nt = blockDim.x * blockDim.y;
+    v = warp_sum(v);
+    if ((t & 31) == 0) ws[t >> 5] = v;
+    __syncthreads();
+    if (t < 32) {
+        double s = (t < (nt >> 5)) ? ws[t] : 0.0;
+        s = warp_sum(s);
+        if (t == 0) red[blk] = s;
+    }
+}
+
+__global__ void __launch_bounds__(128) data_term_kernel(
+    const __grid_constant__ Geo G, const float* __restrict__ x, const float* __restrict__ angles,
+    const int32_t* __restrict__ index, const float* __restrict__ y, const float* __restrict__ b,
+    const float* __restrict__ r, double* __restrict__ red) {
+    const nr_geom& g = G.g;
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int a = blockIdx.z;
+    double term = 0.0;
+    if (i < g.nbx && j < g.nby) {
+        float x0, y0, z0, ct;
+        source_pos(g, angles[index[a]], &x0, &y0, &z0, &ct);
+        float v;
+        float l = 0.f;
+        if (trace<0>(G, x, x0, y0, z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v)) l = v * ct;
+        const int64_t o = (int64_t)a * g.nbx * g.nby + (int64_t)j * g.nbx + i;
+        const double yb = (double)b[o] * exp(-(double)l);
+        const double m = yb + (r ? (double)r[o] : 0.0);
+        const double yy = (double)y[o];
+        term = m - (yy > 0.0 ? yy * log(m) : 0.0);
+    }
+    const int64_t blk = ((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    block_partial(term, red, blk);
+}
+
+template <int POT>
+__device__ __forceinline__ double psi(float t, float delta) {
+    if (POT == NR_POT_Q2) return 0.5 * (double)t * (double)t;
+    if (POT == NR_POT_LANGE) {
+        const double a = fabs((double)t) / (double)delta;
+        return (double)delta * (double)delta * (a - log1p(a));
+    }
+    if (POT == NR_POT_HYPERBOLA) {
+        // d^2 (sqrt(1+u^2) - 1) = d^2 u^2 / (sqrt(1+u^2) + 1): no cancellation
+        const float u = t / delta;
+        const float u2 = u * u;
+        return (double)delta * (double)delta * (double)(u2 / (sqrtf(1.f + u2) + 1.f));
+    }
+    const float a = fabsf(t);
+    return a <= delta ? 0.5 * (double)t * (double)t
+                      : (double)delta * (double)a - 0.5 * (double)delta * (double)delta;
+}
+
+struct PairW {
+    float w[13];  // forward neighbours: dz=+1 (9), dz=0 dy=+1 (3), dz=0 dy=0 dx=+1 (1)
+};
+
+__host__ inline PairW make_pair_weights(float zxy) {
+    PairW p;
+    int k = 0;
+    auto put = [&](int dx, int dy, int dz) {
+        float dist = std::sqrt((float)(dx * dx + dy * dy) + (float)(dz * dz) * zxy * zxy);
+        p.w[k++] = (float)(1.0 / (double)dist);
+    };
+    for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) put(dx, dy, 1);
+    for (int dx = -1; dx <= 1; dx++) put(dx, 1, 0);
+    put(1, 0, 0);
+    return p;
+}
+
+template <int POT>
+__global__ void __launch_bounds__(128) penalty_kernel(const __grid_constant__ Geo G,
+                                                      const __grid_constant__ PairW W,
+                                                      const float* __restrict__ x, float delta,
+                                                      double* __restrict__ red) {
+    const nr_geom& g = G.g;
+    const int ix = blockIdx.x * 32 + threadIdx.x;
+    const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    const int iz = blockIdx.z;
+    double acc = 0.0;
+    if (ix < g.nx && iy < g.ny) {
+        const int64_t plane = (int64_t)g.nx * g.ny;
+        const int64_t v = iz * plane + (int64_t)iy * g.nx + ix;
+        const float xc = x[v];
+        int k = 0;
+        auto pair = [&](int dx, int dy, int dz) {
+            const int kx = ix + dx, ky = iy + dy, kz = iz + dz;
+            if ((unsigned)kx < (unsigned)g.nx && (unsigned)ky < (unsigned)g.ny &&
+                (unsigned)kz < (unsigned)g.nz) {
+                const float t = xc - __ldg(x + kz * plane + (int64_t)ky * g.nx + kx);
+                acc += (double)W.w[k] * psi<POT>(t, delta);
+            }
+            k++;
+        };
+#pragma unroll
+        for (int dy = -1; dy <= 1; dy++)
+#pragma unroll
+            for (int dx = -1; dx <= 1; dx++) pair(dx, dy, 1);
+#pragma unroll
+        for (int dx = -1; dx <= 1; dx++) pair(dx, 1, 0);
+        pair(1, 0, 0);
+    }
+    const int64_t blk = ((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    block_partial(acc, red, blk);
+}
+
+// Fixed-order sum of n partials by one block of 1024 threads.
+__global__ void __launch_bounds__(1024) final_sum_kernel(const double* __restrict__ red, int64_t n0,
+                                                         int64_t n1, double* __restrict__ out) {
+    __shared__ double ws[32];
+    for (int part = 0; part < 2; part++) {
+        const double* p = red + (part == 0 ? 0 : n0);
+        const int64_t n = part == 0 ? n0 : n1;
+        double s = 0.0;
+        for (int64_t k = threadIdx.x; k < n; k += blockDim.x) s += p[k];
+        s = warp_sum(s);
+        if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double t = ws[threadIdx.x];
+            t = warp_sum(t);
+            if (threadIdx.x == 0) out[part] = t;
+        }
+        __syncthreads();
+    }
+}
+
+static int64_t data_blocks(const nr_geom& g) {
+    return (int64_t)cdiv(g.nbx, 32) * cdiv(g.nby, 4) * g.n_angles;
+}
+static int64_t pen_blocks(const nr_geom& g) {
+    return (int64_t)cdiv(g.nx, 32) * cdiv(g.ny, 4) * g.nz;
+}
+
+int64_t objective_partials(const nr_geom& g) { return data_blocks(g) + pen_blocks(g); }
+
+nr_status launch_objective(const nr_geom& g, int pot, float delta, const float* x,
+                           const float* angles, const int32_t* index, const float* y,
+                           const float* b, const float* r, double* red, int64_t red_n,
+                           double* out, cudaStream_t st) {
+    const int64_t nd = data_blocks(g), np = pen_blocks(g);
+    if (nd + np > red_n) return NR_ERR_WORKSPACE;
+    const Geo G = make_geo(g);
+    {
+        dim3 blk(32, 4), grd(cdiv(g.nbx, 32), cdiv(g.nby, 4), g.n_angles);
+        data_term_kernel<<<grd, blk, 0, st>>>(G, x, angles, index, y, b, r, red);
+    }
+    {
+        dim3 blk(32, 4), grd(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz);
+        const PairW W = make_pair_weights(g.vz / g.vx);
+        const float dl = pot == NR_POT_Q2 ? 1.f : delta;
+        switch (pot) {
+        case NR_POT_Q2: penalty_kernel<NR_POT_Q2><<<grd, blk, 0, st>>>(G, W, x, dl, red + nd); break;
+        case NR_POT_LANGE:
+            penalty_kernel<NR_POT_LANGE><<<grd, blk, 0, st>>>(G, W, x, dl, red + nd);
+            break;
+        case NR_POT_HYPERBOLA:
+            penalty_kernel<NR_POT_HYPERBOLA><<<grd, blk, 0, st>>>(G, W, x, dl, red + nd);
+            break;
+        case NR_POT_HUBER:
+            penalty_kernel<NR_POT_HUBER><<<grd, blk, 0, st>>>(G, W, x, dl, red + nd);
+            break;
+        default: return NR_ERR_BAD_ARGUMENT;
+        }
+    }
+    final_sum_kernel<<<1, 1024, 0, st>>>(red, nd, np, out);
+    return launch_status();
+}
+
+}  // namespace nr

@@ -1,0 +1,318 @@
+// ostr.cu -- the device-resident OSTR driver: workspace layout, scan setup
+// (regroup + transpose, gamma*yry, curvature d), the subset loop, the FP64
+// objective and the status word.
+//
+// Workspace (caller-allocated, 256-byte aligned sections):
+//   status   int32[64]                  device status word (NR_FLAG_*)
+//   red      double[red_n]              per-block partial sums of the objective
+//   index    int32[A]                   view order (subset-major)
+//   angles   float[A]
+//   y, b, r  float[A][BINSy][BINSx]     scan in subset order, detector i fastest
+//   d        float[N]                   curvature denominators
+//   xtmp     float[N]                   second volume buffer (ping-pong)
+//   h        float[Vs][BINSy][BINSx]    subset gradient in the detector domain
+//   gc       float[A][BINSy][BINSx]     gamma*yry (setup only)
+//   gr       float[A][BINSy][BINSx]     scatter in original order (setup only; with scatter)
+#include "common.cuh"
+
+namespace nr {
+
+nr_status launch_fp_h(const nr_geom& g, const float* x, float* h, const float* angles,
+                      const int32_t* index, int a0, int nviews, const float* y, const float* b,
+                      const float* r, cudaStream_t st);
+nr_status launch_gamma_yry(const nr_geom& g, int gamma_mode, float* out, const float* angles,
+                           const float* y, const float* r, cudaStream_t st);
+nr_status launch_bp(const nr_geom& g, bool ji, float* vol, const float* prj, const float* angles,
+                    const int32_t* index, int a0, int nv, cudaStream_t st);
+nr_status launch_update(const nr_geom& g, int pot, const float* x, float* x_out, const float* d,
+                        const float* h, const float* angles, const int32_t* index, int a0, int nv,
+                        float M, float beta, float delta, int* status, cudaStream_t st);
+nr_status launch_transpose(float* out, const float* in, int rows, int cols, int nviews, int M,
+                           int Vs, cudaStream_t st);
+nr_status launch_objective(const nr_geom& g, int pot, float delta, const float* x,
+                           const float* angles, const int32_t* index, const float* y,
+                           const float* b, const float* r, double* red, int64_t red_n,
+                           double* out, cudaStream_t st);
+int64_t objective_partials(const nr_geom& g);
+
+struct Layout {
+    size_t status, red, index, angles, y, b, r, d, xtmp, h, gc, gr, total;
+    int64_t red_n;
+};
+
+static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static Layout layout(const nr_geom& g, const nr_ostr_params& p) {
+    const int64_t A = g.n_angles, B = (int64_t)g.nbx * g.nby;
+    const int64_t N = (int64_t)g.nx * g.ny * g.nz;
+    const int64_t Vs = A / p.subset_num;
+    Layout L;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        size_t at = o;
+        o = align256(o + bytes);
+        return at;
+    };
+    L.red_n = objective_partials(g);
+    L.status = take(64 * sizeof(int32_t));
+    L.red = take((size_t)L.red_n * sizeof(double));
+    L.index = take(A * sizeof(int32_t));
+    L.angles = take(A * sizeof(float));
+    L.y = take(A * B * sizeof(float));
+    L.b = take(A * B * sizeof(float));
+    L.r = p.has_scatter ? take(A * B * sizeof(float)) : (size_t)-1;
+    L.d = take(N * sizeof(float));
+    L.xtmp = take(N * sizeof(float));
+    L.h = take(Vs * B * sizeof(float));
+    L.gc = take(A * B * sizeof(float));
+    L.gr = p.has_scatter ? take(A * B * sizeof(float)) : (size_t)-1;
+    L.total = o;
+    return L;
+}
+
+struct WS {
+    int* status;
+    double* red;
+    int32_t* index;
+    float *angles, *y, *b, *r, *d, *xtmp, *h, *gc, *gr;
+    int64_t red_n;
+};
+
+static WS carve(void* base, const Layout& L) {
+    char* c = (char*)base;
+    WS w;
+    w.status = (int*)(c + L.status);
+    w.red = (double*)(c + L.red);
+    w.index = (int32_t*)(c + L.index);
+    w.angles = (float*)(c + L.angles);
+    w.y = (float*)(c + L.y);
+    w.b = (float*)(c + L.b);
+    w.r = L.r == (size_t)-1 ? nullptr : (float*)(c + L.r);
+    w.d = (float*)(c + L.d);
+    w.xtmp = (float*)(c + L.xtmp);
+    w.h = (float*)(c + L.h);
+    w.gc = (float*)(c + L.gc);
+    w.gr = L.gr == (size_t)-1 ? nullptr : (float*)(c + L.gr);
+    w.red_n = L.red_n;
+    return w;
+}
+
+static nr_status check_params(const nr_geom* g, const nr_ostr_params* p) {
+    if (!geom_ok(g)) return NR_ERR_BAD_GEOMETRY;
+    if (!p) return NR_ERR_BAD_ARGUMENT;
+    if (p->subset_num <= 0 || g->n_angles % p->subset_num != 0) return NR_ERR_BAD_GEOMETRY;
+    if (g->vx != g->vy) return NR_ERR_BAD_GEOMETRY;  // Tomo_OSTR_gold.cpp:380-386
+    if (p->potential < NR_POT_Q2 || p->potential > NR_POT_HUBER) return NR_ERR_BAD_ARGUMENT;
+    if (p->potential != NR_POT_Q2 && !(p->delta > 0.f)) return NR_ERR_BAD_ARGUMENT;
+    if (p->gamma_mode != NR_GAMMA_LENGTH && p->gamma_mode != NR_GAMMA_CHORD)
+        return NR_ERR_BAD_ARGUMENT;
+    if (!(p->beta >= 0.f)) return NR_ERR_BAD_ARGUMENT;
+    if (g->n_angles / p->subset_num > 32) return NR_ERR_BAD_ARGUMENT;  // views per subset in smem
+    if (g->ny > 65535 || g->nz > 65535 || g->n_angles > 65535) return NR_ERR_BAD_GEOMETRY;
+    return NR_OK;
+}
+
+static nr_status check_ws(const nr_geom* g, const nr_ostr_params* p, void* ws, size_t bytes,
+                          Layout* L) {
+    nr_status st = check_params(g, p);
+    if (st != NR_OK) return st;
+    *L = layout(*g, *p);
+    if (!ws || bytes < L->total || ((uintptr_t)ws & 255) != 0) return NR_ERR_WORKSPACE;
+    return NR_OK;
+}
+
+// Subset-major view order, Tomo_OSTR_gold.cpp:628-642: position i*Vs + j
+// holds original view j*M + i.
+__global__ void index_kernel(int32_t* idx, const float* __restrict__ angles_in,
+                             float* __restrict__ angles_out, int A, int M) {
+    const int Vs = A / M;
+    for (int p = threadIdx.x; p < A; p += blockDim.x) {
+        idx[p] = (p % Vs) * M + p / Vs;
+        angles_out[p] = angles_in[p];
+    }
+}
+
+__global__ void clear_status_kernel(int* s) {
+    if (threadIdx.x < 64) s[threadIdx.x] = 0;
+}
+
+}  // namespace nr
+
+using namespace nr;
+
+NR_API nr_status nr_validate_geometry(const nr_geom* g, int32_t subset_num) {
+    if (!geom_ok(g)) return NR_ERR_BAD_GEOMETRY;
+    if (g->vx != g->vy) return NR_ERR_BAD_GEOMETRY;
+    if (subset_num > 0 && g->n_angles % subset_num != 0) return NR_ERR_BAD_GEOMETRY;
+    return NR_OK;
+}
+
+NR_API nr_status nr_ostr_workspace_size(const nr_geom* g, const nr_ostr_params* p,
+                                        size_t* bytes) {
+    nr_status st = check_params(g, p);
+    if (st != NR_OK) return st;
+    if (!bytes) return NR_ERR_BAD_ARGUMENT;
+    *bytes = layout(*g, *p).total;
+    return NR_OK;
+}
+
+NR_API nr_status nr_ostr_setup(const nr_geom* g, const nr_ostr_params* p, const float* angles,
+                               const float* prj, const float* blank, const float* scat,
+                               void* workspace, size_t ws_bytes, void* stream) {
+    Layout L;
+    nr_status st = check_ws(g, p, workspace, ws_bytes, &L);
+    if (st != NR_OK) return st;
+    if (!angles || !prj || !blank || (p->has_scatter && !scat)) return NR_ERR_BAD_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    WS w = carve(workspace, L);
+    const int A = g->n_angles, M = p->subset_num, Vs = A / M;
+    const int64_t N = (int64_t)g->nx * g->ny * g->nz;
+    clear_status_kernel<<<1, 64, 0, s>>>(w.status);
+    index_kernel<<<1, 256, 0, s>>>(w.index, angles, w.angles, A, M);
+    if ((st = launch_status()) != NR_OK) return st;
+    // [view][i][j] original order -> [view][j][i] subset order.
+    if ((st = launch_transpose(w.y, prj, g->nbx, g->nby, A, M, Vs, s)) != NR_OK) return st;
+    if ((st = launch_transpose(w.b, blank, g->nbx, g->nby, A, M, Vs, s)) != NR_OK) return st;
+    if (w.r && (st = launch_transpose(w.r, scat, g->nbx, g->nby, A, M, Vs, s)) != NR_OK) return st;
+    // gamma*yry is formed in original view order (identity index, as the
+    // reference does before it regroups): stage y (and r) there.
+    if ((st = launch_transpose(w.gc, prj, g->nbx, g->nby, A, 0, 1, s)) != NR_OK) return st;
+    if (w.r && (st = launch_transpose(w.gr, scat, g->nbx, g->nby, A, 0, 1, s)) != NR_OK) return st;
+    // gc <- yry(gc, r) * gamma, original order, identity index.
+    if ((st = launch_gamma_yry(*g, p->gamma_mode, w.gc, angles, w.gc, w.gr, s)) != NR_OK)
+        return st;
+    if (cudaMemsetAsync(w.d, 0, N * sizeof(float), s) != cudaSuccess) return NR_ERR_CUDA;
+    // d = SBP(gamma*yry) over all views, original order (Tomo_OSTR_gold.cpp:528-565).
+    if ((st = launch_bp(*g, true, w.d, w.gc, angles, nullptr, 0, A, s)) != NR_OK) return st;
+    return NR_OK;
+}
+
+NR_API nr_status nr_ostr_project(const nr_geom* g, const nr_ostr_params* p, const float* x,
+                                 int32_t subset, void* workspace, size_t ws_bytes, void* stream) {
+    Layout L;
+    nr_status st = check_ws(g, p, workspace, ws_bytes, &L);
+    if (st != NR_OK) return st;
+    if (!x || subset < 0 || subset >= p->subset_num) return NR_ERR_BAD_ARGUMENT;
+    WS w = carve(workspace, L);
+    const int Vs = g->n_angles / p->subset_num;
+    return launch_fp_h(*g, x, w.h, w.angles, w.index, subset * Vs, Vs, w.y, w.b, w.r,
+                       as_stream(stream));
+}
+
+NR_API nr_status nr_ostr_update(const nr_geom* g, const nr_ostr_params* p, const float* x,
+                                float* x_out, int32_t subset, void* workspace, size_t ws_bytes,
+                                void* stream) {
+    Layout L;
+    nr_status st = check_ws(g, p, workspace, ws_bytes, &L);
+    if (st != NR_OK) return st;
+    if (!x || !x_out || x == x_out || subset < 0 || subset >= p->subset_num)
+        return NR_ERR_BAD_ARGUMENT;
+    WS w = carve(workspace, L);
+    const int M = p->subset_num, Vs = g->n_angles / M;
+    return launch_update(*g, p->potential, x, x_out, w.d, w.h, w.angles, w.index, subset * Vs, Vs,
+                         (float)M, p->beta, p->delta, w.status, as_stream(stream));
+}
+
+NR_API nr_status nr_ostr_workspace_section(const nr_geom* g, const nr_ostr_params* p,
+                                           int32_t section, void* workspace, size_t ws_bytes,
+                                           void** ptr, size_t* bytes) {
+    Layout L;
+    nr_status st = check_ws(g, p, workspace, ws_bytes, &L);
+    if (st != NR_OK) return st;
+    if (!ptr || !bytes) return NR_ERR_BAD_ARGUMENT;
+    WS w = carve(workspace, L);
+    const int64_t A = g->n_angles, B = (int64_t)g->nbx * g->nby;
+    const int64_t N = (int64_t)g->nx * g->ny * g->nz;
+    switch (section) {
+    case NR_WS_D: *ptr = w.d; *bytes = N * sizeof(float); break;
+    case NR_WS_H: *ptr = w.h; *bytes = (A / p->subset_num) * B * sizeof(float); break;
+    case NR_WS_Y: *ptr = w.y; *bytes = A * B * sizeof(float); break;
+    case NR_WS_GAMMA_YRY: *ptr = w.gc; *bytes = A * B * sizeof(float); break;
+    case NR_WS_INDEX: *ptr = w.index; *bytes = A * sizeof(int32_t); break;
+    default: return NR_ERR_BAD_ARGUMENT;
+    }
+    return NR_OK;
+}
+
+NR_API nr_status nr_ostr_subiter(const nr_geom* g, const nr_ostr_params* p, float* x,
+                                 int32_t subset, void* workspace, size_t ws_bytes, void* stream) {
+    Layout L;
+    nr_status st = check_ws(g, p, workspace, ws_bytes, &L);
+    if (st != NR_OK) return st;
+    if (!x || subset < 0 || subset >= p->subset_num) return NR_ERR_BAD_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    WS w = carve(workspace, L);
+    const int A = g->n_angles, M = p->subset_num, Vs = A / M;
+    const int64_t N = (int64_t)g->nx * g->ny * g->nz;
+    const int a0 = subset * Vs;
+    if ((st = launch_fp_h(*g, x, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, s)) != NR_OK)
+        return st;
+    if ((st = launch_update(*g, p->potential, x, w.xtmp, w.d, w.h, w.angles, w.index, a0, Vs,
+                            (float)M, p->beta, p->delta, w.status, s)) != NR_OK)
+        return st;
+    if (cudaMemcpyAsync(x, w.xtmp, N * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        return NR_ERR_CUDA;
+    return NR_OK;
+}
+
+NR_API nr_status nr_ostr_iterate(const nr_geom* g, const nr_ostr_params* p, float* x,
+                                 int32_t n_iters, void* workspace, size_t ws_bytes, void* stream) {
+    Layout L;
+    nr_status st = check_ws(g, p, workspace, ws_bytes, &L);
+    if (st != NR_OK) return st;
+    if (!x || n_iters < 0) return NR_ERR_BAD_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    WS w = carve(workspace, L);
+    const int A = g->n_angles, M = p->subset_num, Vs = A / M;
+    const int64_t N = (int64_t)g->nx * g->ny * g->nz;
+    float* cur = x;
+    float* nxt = w.xtmp;
+    for (int it = 0; it < n_iters; it++) {
+        for (int a = 0; a < M; a++) {
+            const int a0 = a * Vs;
+            if ((st = launch_fp_h(*g, cur, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, s)) !=
+                NR_OK)
+                return st;
+            if ((st = launch_update(*g, p->potential, cur, nxt, w.d, w.h, w.angles, w.index, a0, Vs,
+                                    (float)M, p->beta, p->delta, w.status, s)) != NR_OK)
+                return st;
+            float* t = cur;
+            cur = nxt;
+            nxt = t;
+        }
+    }
+    if (cur != x &&
+        cudaMemcpyAsync(x, cur, N * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        return NR_ERR_CUDA;
+    return NR_OK;
+}
+
+NR_API nr_status nr_ostr_objective(const nr_geom* g, const nr_ostr_params* p, const float* x,
+                                   double* out, void* workspace, size_t ws_bytes, void* stream) {
+    Layout L;
+    nr_status st = check_ws(g, p, workspace, ws_bytes, &L);
+    if (st != NR_OK) return st;
+    if (!x || !out) return NR_ERR_BAD_ARGUMENT;
+    WS w = carve(workspace, L);
+    return launch_objective(*g, p->potential, p->delta, x, w.angles, w.index, w.y, w.b, w.r, w.red,
+                            w.red_n, out, as_stream(stream));
+}
+
+NR_API nr_status nr_ostr_check(void* workspace, size_t ws_bytes, int32_t* flags, void* stream) {
+    if (!workspace || ws_bytes < 256 || !flags) return NR_ERR_BAD_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    int v = 0;
+    if (cudaMemcpyAsync(&v, workspace, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return NR_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return NR_ERR_CUDA;
+    *flags = v;
+    if (v) {
+        clear_status_kernel<<<1, 64, 0, s>>>((int*)workspace);
+        if (launch_status() != NR_OK) return NR_ERR_LAUNCH;
+    }
+    if (v & NR_FLAG_TIMEOUT) return NR_ERR_TIMEOUT;
+    if (v & NR_FLAG_NONFINITE) return NR_ERR_NONFINITE;
+    return NR_OK;
+}
+
+NR_API const char* nr_version(void) { return "nrgb300 0.1.0 sm_103a"; }
