@@ -16,11 +16,6 @@
 
 namespace nr {
 
-// Per-view source terms, computed once per block into shared memory.
-struct ViewSrc {
-    float x0, y0, z0, s2;  // source position and x0^2+y0^2+z0^2 (depth weight numerator)
-};
-
 constexpr int BP_VIEWS_SMEM = 64;
 
 __device__ __forceinline__ void load_views(const nr_geom& g, ViewSrc* sv,
@@ -28,12 +23,7 @@ __device__ __forceinline__ void load_views(const nr_geom& g, ViewSrc* sv,
                                            const int32_t* __restrict__ index, int a0, int nv) {
     for (int t = threadIdx.x; t < nv; t += blockDim.x) {
         const int s = index ? index[a0 + t] : a0 + t;
-        float x0, y0, z0, ct;
-        source_pos(g, angles[s], &x0, &y0, &z0, &ct);
-        sv[t].x0 = x0;
-        sv[t].y0 = y0;
-        sv[t].z0 = z0;
-        sv[t].s2 = x0 * x0 + y0 * y0 + z0 * z0;
+        sv[t] = view_source(g, angles[s]);
     }
 }
 

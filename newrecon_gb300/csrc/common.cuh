@@ -30,16 +30,26 @@ __host__ inline Geo make_geo(const nr_geom& g) {
     return d;
 }
 
-// Source position for view angle theta: rotation about the y axis at the
-// origin, Tomo_OSTR.cu:1340-1345 (sinf/cosf of a float32 angle).
-__device__ __forceinline__ void source_pos(const nr_geom& g, float theta, float* x0, float* y0,
-                                           float* z0, float* ct) {
-    float s, c;
-    sincosf(theta, &s, &c);
-    *x0 = g.sourceR * s;
-    *z0 = g.sourceR * c;
-    *y0 = g.sourceY;
-    *ct = c;
+// Source of one view: rotation about the y axis at the origin,
+// (R sin t, sourceY, R cos t), Tomo_OSTR.cu:1340-1345.  Evaluated in double
+// and rounded once (the reference uses float sinf/cosf; a 2-ulp sine moves the
+// source by ~2e-5 mm, which shows up against the FP64 oracle wherever a ray
+// grazes a high-contrast edge).  s2 = |source|^2, the SBP depth-weight
+// numerator (Tomo_OSTR.cu:1634).  One thread per block computes it.
+struct ViewSrc {
+    float x0, y0, z0, ct, s2;
+};
+
+__device__ __forceinline__ ViewSrc view_source(const nr_geom& g, float theta) {
+    double s, c;
+    sincos((double)theta, &s, &c);
+    ViewSrc v;
+    v.x0 = (float)((double)g.sourceR * s);
+    v.z0 = (float)((double)g.sourceR * c);
+    v.y0 = g.sourceY;
+    v.ct = (float)c;
+    v.s2 = v.x0 * v.x0 + v.y0 * v.y0 + v.z0 * v.z0;
+    return v;
 }
 
 // Bin centre on the stationary detector, Tomo_OSTR.cu:1349-1356.  The

@@ -27,18 +27,18 @@ __global__ void __launch_bounds__(128) fp_kernel(const __grid_constant__ Geo G,
                                                  float* __restrict__ out,
                                                  const float* __restrict__ angles,
                                                  const int32_t* __restrict__ index, int a0) {
+    __shared__ ViewSrc src;
     const nr_geom& g = G.g;
+    const int a = a0 + blockIdx.z;
+    if (threadIdx.x == 0 && threadIdx.y == 0) src = view_source(g, angles[index[a]]);
+    __syncthreads();
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nbx || j >= g.nby) return;
-    const int a = a0 + blockIdx.z;
-    const float theta = angles[index[a]];
-    float x0, y0, z0, ct;
-    source_pos(g, theta, &x0, &y0, &z0, &ct);
     float v;
-    if (trace<MODE>(G, vol, x0, y0, z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v)) {
+    if (trace<MODE>(G, vol, src.x0, src.y0, src.z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v)) {
         const int64_t o = (int64_t)blockIdx.z * g.nbx * g.nby + bin_off<JI>(g, i, j);
-        out[o] = (MODE == 0) ? v * ct : v;
+        out[o] = (MODE == 0) ? v * src.ct : v;
     }
 }
 
@@ -56,17 +56,18 @@ __global__ void __launch_bounds__(128) fp_h_kernel(const __grid_constant__ Geo G
                                                    const float* __restrict__ y,
                                                    const float* __restrict__ b,
                                                    const float* __restrict__ r) {
+    __shared__ ViewSrc src;
     const nr_geom& g = G.g;
+    const int a = a0 + blockIdx.z;
+    if (threadIdx.x == 0 && threadIdx.y == 0) src = view_source(g, angles[index[a]]);
+    __syncthreads();
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nbx || j >= g.nby) return;
-    const int a = a0 + blockIdx.z;
-    const float theta = angles[index[a]];
-    float x0, y0, z0, ct;
-    source_pos(g, theta, &x0, &y0, &z0, &ct);
     float v = 0.f;
     float l = 0.f;
-    if (trace<0>(G, vol, x0, y0, z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v)) l = v * ct;
+    if (trace<0>(G, vol, src.x0, src.y0, src.z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v))
+        l = v * src.ct;
     const int64_t B = (int64_t)g.nbx * g.nby;
     const int64_t o = (int64_t)a * B + bin_off<true>(g, i, j);
     const float yb = b[o] * expf(-l);
@@ -83,16 +84,18 @@ __global__ void __launch_bounds__(128) gamma_yry_kernel(const __grid_constant__ 
                                                         const float* __restrict__ angles,
                                                         const float* __restrict__ y,
                                                         const float* __restrict__ r) {
+    __shared__ ViewSrc src;
     const nr_geom& g = G.g;
+    const int a = blockIdx.z;
+    if (threadIdx.x == 0 && threadIdx.y == 0) src = view_source(g, angles[a]);
+    __syncthreads();
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.nbx || j >= g.nby) return;
-    const int a = blockIdx.z;
-    float x0, y0, z0, ct;
-    source_pos(g, angles[a], &x0, &y0, &z0, &ct);
     float gam = 0.f;  // gamma buffer is zeroed before the projection (Tomo_OSTR_gold.cpp:441)
     float v;
-    if (trace<MODE>(G, nullptr, x0, y0, z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v)) gam = v;
+    if (trace<MODE>(G, nullptr, src.x0, src.y0, src.z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v))
+        gam = v;
     const int64_t o = (int64_t)a * g.nbx * g.nby + bin_off<true>(g, i, j);
     const float yy = y[o];
     float c = 0.f;

