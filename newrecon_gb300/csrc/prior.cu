@@ -23,10 +23,11 @@ nr_status launch_bp(const nr_geom& g, bool ji, float* vol, const float* prj, con
                     const int32_t* index, int a0, int nv, cudaStream_t st);
 
 struct PriorW {
-    float w[27];  // weight of neighbour (dx,dy,dz) at ((dz+1)*3+(dy+1))*3+(dx+1); centre 0
+    float w[27];   // weight of neighbour (dx,dy,dz) at ((dz+1)*3+(dy+1))*3+(dx+1); centre 0
+    float wd[27];  // w * delta (Huber)
 };
 
-__host__ inline PriorW make_weights(float zxy) {
+__host__ inline PriorW make_weights(float zxy, float delta = 1.f) {
     PriorW p;
     for (int dz = -1; dz <= 1; dz++)
         for (int dy = -1; dy <= 1; dy++)
@@ -36,6 +37,7 @@ __host__ inline PriorW make_weights(float zxy) {
                 float dist = std::sqrt((float)(dx * dx + dy * dy) + (float)(dz * dz) * zxy * zxy);
                 int k = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
                 p.w[k] = (dist == 0.f) ? 0.f : (float)(1.0 / (double)dist);
+                p.wd[k] = p.w[k] * delta;
             }
     return p;
 }
@@ -104,67 +106,150 @@ __global__ void __launch_bounds__(128) prior_kernel(const __grid_constant__ Geo 
 }
 
 constexpr int UPD_VIEWS_SMEM = 32;
+constexpr int UTX = 32, UTY = 8, UZC = 16;      // tile: 32 x 8 columns, 16 planes per block
+constexpr int USW = UTX + 2, USH = UTY + 2;     // plane tile with a 1-voxel halo
+constexpr int UPLANE = USW * USH;
+
+// w * omega(t) for neighbour weight w (wd = w * delta, inv_delta = 1/delta),
+// with the approximate MUFU reciprocal / rsqrt (<= 2 ulp).
+template <int POT>
+__device__ __forceinline__ float w_omega(float t, float w, float wd, float delta, float inv_delta) {
+    if (POT == NR_POT_Q2) return w;
+    if (POT == NR_POT_LANGE) return __fdividef(w, __fmaf_rn(fabsf(t), inv_delta, 1.f));
+    if (POT == NR_POT_HYPERBOLA) {
+        const float u = t * inv_delta;
+        return w * rsqrtf(__fmaf_rn(u, u, 1.f));
+    }
+    return __fdividef(wd, fmaxf(fabsf(t), delta));  // Huber: w * min(1, delta/|t|)
+}
+
+// Penalty sums from the shared-memory planes (below, centre, above), centre
+// at (r, c).  EDGE: out-of-volume cells hold NaN and count as t = 0.
+template <int POT, bool EDGE>
+__device__ __forceinline__ void prior_sums_tile(const PriorW& W, const float* __restrict__ pb,
+                                                const float* __restrict__ pc,
+                                                const float* __restrict__ pa, int r, int c,
+                                                float xc, float delta, float inv_delta,
+                                                float* rdd, float* rd) {
+    float sdd = 0.f, sd = 0.f;
+#pragma unroll
+    for (int dz = -1; dz <= 1; dz++) {
+        const float* pl = dz < 0 ? pb : (dz == 0 ? pc : pa);
+#pragma unroll
+        for (int dy = -1; dy <= 1; dy++) {
+#pragma unroll
+            for (int dx = -1; dx <= 1; dx++) {
+                if (dx == 0 && dy == 0 && dz == 0) continue;
+                const int k = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
+                float t = xc - pl[(r + dy) * USW + (c + dx)];
+                if (EDGE) t = (t == t) ? t : 0.f;
+                const float wo = w_omega<POT>(t, W.w[k], W.wd[k], delta, inv_delta);
+                sdd += wo;
+                sd = __fmaf_rn(wo, t, sd);
+            }
+        }
+    }
+    *rdd = sdd;
+    *rd = sd;
+}
 
 // One sub-iteration's update, fused: SBP of h (subset views, [view][j][i]),
-// the penalty, and the update_est step.  Writes x_out; flags non-finite values.
+// the penalty, and the update_est step.  Each block owns a 32 x 8 tile of
+// (x, y) columns and walks UZC planes in z, keeping planes z-1, z, z+1 of x
+// (with halo) in a 3-slot shared-memory ring, so every neighbour read is a
+// shared-memory load at a fixed offset.  Writes x_out; flags non-finite values.
 template <int POT>
-__global__ void __launch_bounds__(128) update_kernel(
+__global__ void __launch_bounds__(256) update_kernel(
     const __grid_constant__ Geo G, const __grid_constant__ PriorW W,
     const float* __restrict__ x, float* __restrict__ x_out, const float* __restrict__ d,
     const float* __restrict__ h, const float* __restrict__ angles,
     const int32_t* __restrict__ index, int a0, int nv, float M, float beta, float delta,
     int* __restrict__ status) {
+    __shared__ float tile[3][UPLANE];
     __shared__ ViewSrc sv[UPD_VIEWS_SMEM];
     const nr_geom& g = G.g;
-    for (int t = threadIdx.y * blockDim.x + threadIdx.x; t < nv; t += blockDim.x * blockDim.y) {
-        sv[t] = view_source(g, angles[index[a0 + t]]);
-    }
-    __syncthreads();
-    const int ix = blockIdx.x * 32 + threadIdx.x;
-    const int iy = blockIdx.y * blockDim.y + threadIdx.y;
-    const int iz = blockIdx.z;
-    if (ix >= g.nx || iy >= g.ny) return;
-    const int64_t v = ((int64_t)iz * g.ny + iy) * g.nx + ix;
-    const float xc = x[v];
-    // M * SBP(h)
-    const float x1 = vox_x(g, ix), y1 = vox_y(g, iy), z1 = vox_z(g, iz);
+    const int tid = threadIdx.y * UTX + threadIdx.x;
+    for (int t = tid; t < nv; t += UTX * UTY) sv[t] = view_source(g, angles[index[a0 + t]]);
+    const int x0t = blockIdx.x * UTX, y0t = blockIdx.y * UTY;
+    const int zb = blockIdx.z * UZC, ze = min(zb + UZC, g.nz);
+    const int64_t plane = (int64_t)g.nx * g.ny;
+    auto load_plane = [&](float* dst, int z) {
+        const bool zin = z >= 0 && z < g.nz;
+        for (int k = tid; k < UPLANE; k += UTX * UTY) {
+            const int r = k / USW, c = k - r * USW;
+            const int gx = x0t - 1 + c, gy = y0t - 1 + r;
+            float v = __int_as_float(0x7fc00000);  // NaN: outside the volume
+            if (zin && gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny)
+                v = __ldg(x + (int64_t)z * plane + (int64_t)gy * g.nx + gx);
+            dst[k] = v;
+        }
+    };
+    float* pb = tile[0];
+    float* pc = tile[1];
+    float* pa = tile[2];
+    load_plane(pb, zb - 1);
+    load_plane(pc, zb);
+    const int ix = x0t + threadIdx.x, iy = y0t + threadIdx.y;
+    const bool active = ix < g.nx && iy < g.ny;
+    const bool edge_xy = x0t == 0 || x0t + UTX >= g.nx || y0t == 0 || y0t + UTY >= g.ny;
+    const float inv_delta = 1.f / delta;
+    const float x1 = vox_x(g, ix), y1 = vox_y(g, iy);
     const int64_t B = (int64_t)g.nbx * g.nby;
-    float capL = 0.f;
-    for (int t = 0; t < nv; t++) {
-        const ViewSrc vs = sv[t];
-        const float ddx = vs.x0 - x1, ddy = vs.y0 - y1, ddz = vs.z0 - z1;
-        const float dw = __fdiv_rn(vs.s2, ddx * ddx + ddy * ddy + ddz * ddz);
-        if (z1 == vs.z0) continue;
-        const float tt = __fdiv_rn(-g.detectorR - vs.z0, z1 - vs.z0);
-        const float x2 = vs.x0 + (x1 - vs.x0) * tt;
-        const float y2 = vs.y0 + (y1 - vs.y0) * tt;
-        const float imb = __fdiv_rn(x2 - g.x_d0, g.bx);
-        const float jmb = __fdiv_rn(y2 - g.y_d0, g.by);
-        int ilb = (int)floorf(imb);
-        if (imb < (float)ilb + 0.5f) ilb -= 1;
-        int jlb = (int)floorf(jmb);
-        if (jmb < (float)jlb + 0.5f) jlb -= 1;
-        const float fracI = imb - ((float)ilb + 0.5f);
-        const float fracJ = jmb - ((float)jlb + 0.5f);
-        const float* p = h + (int64_t)t * B;
-        const bool i0 = (ilb < g.nbx) && (ilb >= 0);
-        const bool i1 = (ilb < g.nbx - 1) && (ilb >= -1);
-        const bool j0 = (jlb < g.nby) && (jlb >= 0);
-        const bool j1 = (jlb < g.nby - 1) && (jlb >= -1);
-        float d1 = 0.f, d2 = 0.f;
-        const int64_t r0 = (int64_t)jlb * g.nbx, r1 = r0 + g.nbx;
-        if (i0 && j0) d1 = (1.f - fracI) * __ldg(p + r0 + ilb);
-        if (i1 && j0) d1 = d1 + fracI * __ldg(p + r0 + ilb + 1);
-        if (i0 && j1) d2 = (1.f - fracI) * __ldg(p + r1 + ilb);
-        if (i1 && j1) d2 = d2 + fracI * __ldg(p + r1 + ilb + 1);
-        capL = capL + ((1.f - fracJ) * d1 + fracJ * d2) * g.vz * dw;
+    const int r = threadIdx.y + 1, c = threadIdx.x + 1;
+    for (int z = zb; z < ze; z++) {
+        load_plane(pa, z + 1);
+        __syncthreads();
+        if (active) {
+            const float xc = pc[r * USW + c];
+            const float z1 = vox_z(g, z);
+            // M * SBP(h): same arithmetic as bp.cu's sbp_term on the [j][i] layout
+            float capL = 0.f;
+            for (int t = 0; t < nv; t++) {
+                const ViewSrc vs = sv[t];
+                const float ddx = vs.x0 - x1, ddy = vs.y0 - y1, ddz = vs.z0 - z1;
+                const float dw = __fdiv_rn(vs.s2, ddx * ddx + ddy * ddy + ddz * ddz);
+                if (z1 == vs.z0) continue;
+                const float tt = __fdiv_rn(-g.detectorR - vs.z0, z1 - vs.z0);
+                const float x2 = vs.x0 + (x1 - vs.x0) * tt;
+                const float y2 = vs.y0 + (y1 - vs.y0) * tt;
+                const float imb = __fdiv_rn(x2 - g.x_d0, g.bx);
+                const float jmb = __fdiv_rn(y2 - g.y_d0, g.by);
+                int ilb = (int)floorf(imb);
+                if (imb < (float)ilb + 0.5f) ilb -= 1;
+                int jlb = (int)floorf(jmb);
+                if (jmb < (float)jlb + 0.5f) jlb -= 1;
+                const float fracI = imb - ((float)ilb + 0.5f);
+                const float fracJ = jmb - ((float)jlb + 0.5f);
+                const float* p = h + (int64_t)t * B;
+                const bool i0 = (ilb < g.nbx) && (ilb >= 0);
+                const bool i1 = (ilb < g.nbx - 1) && (ilb >= -1);
+                const bool j0 = (jlb < g.nby) && (jlb >= 0);
+                const bool j1 = (jlb < g.nby - 1) && (jlb >= -1);
+                float d1 = 0.f, d2 = 0.f;
+                const int64_t r0 = (int64_t)jlb * g.nbx, r1 = r0 + g.nbx;
+                if (i0 && j0) d1 = (1.f - fracI) * __ldg(p + r0 + ilb);
+                if (i1 && j0) d1 = d1 + fracI * __ldg(p + r0 + ilb + 1);
+                if (i0 && j1) d2 = (1.f - fracI) * __ldg(p + r1 + ilb);
+                if (i1 && j1) d2 = d2 + fracI * __ldg(p + r1 + ilb + 1);
+                capL = capL + ((1.f - fracJ) * d1 + fracJ * d2) * g.vz * dw;
+            }
+            capL = M * capL;
+            float rdd, rd;
+            if (edge_xy || z == 0 || z == g.nz - 1)
+                prior_sums_tile<POT, true>(W, pb, pc, pa, r, c, xc, delta, inv_delta, &rdd, &rd);
+            else
+                prior_sums_tile<POT, false>(W, pb, pc, pa, r, c, xc, delta, inv_delta, &rdd, &rd);
+            const int64_t v = (int64_t)z * plane + (int64_t)iy * g.nx + ix;
+            const float xn = xc - __fdividef(capL + beta * rd, d[v] + 2.f * beta * rdd);
+            if (!(fabsf(xn) < __int_as_float(0x7f800000))) atomicOr(status, NR_FLAG_NONFINITE);
+            x_out[v] = xn < 0.f ? 0.f : xn;
+        }
+        __syncthreads();
+        float* t = pb;
+        pb = pc;
+        pc = pa;
+        pa = t;
     }
-    capL = M * capL;
-    float rdd, rd;
-    prior_sums<POT>(g, W, x, ix, iy, iz, xc, delta, 1.f / delta, &rdd, &rd);
-    float xn = xc - __fdiv_rn(capL + beta * rd, d[v] + 2.f * beta * rdd);
-    if (!(fabsf(xn) < __int_as_float(0x7f800000))) atomicOr(status, NR_FLAG_NONFINITE);
-    x_out[v] = xn < 0.f ? 0.f : xn;
 }
 
 template <int POT>
@@ -191,9 +276,10 @@ static nr_status launch_update_t(const nr_geom& g, const float* x, float* x_out,
                                  const float* h, const float* angles, const int32_t* index,
                                  int a0, int nv, float M, float beta, float delta, int* status,
                                  cudaStream_t st) {
-    dim3 blk(32, 4), grd(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz);
-    update_kernel<POT><<<grd, blk, 0, st>>>(make_geo(g), make_weights(g.vz / g.vx), x, x_out, d, h,
-                                            angles, index, a0, nv, M, beta, delta, status);
+    dim3 blk(UTX, UTY), grd(cdiv(g.nx, UTX), cdiv(g.ny, UTY), cdiv(g.nz, UZC));
+    update_kernel<POT><<<grd, blk, 0, st>>>(make_geo(g), make_weights(g.vz / g.vx, delta), x,
+                                            x_out, d, h, angles, index, a0, nv, M, beta, delta,
+                                            status);
     return launch_status();
 }
 
