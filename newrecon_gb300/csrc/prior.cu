@@ -157,7 +157,9 @@ __device__ __forceinline__ void prior_sums_tile(const PriorW& W, const float* __
 // the penalty, and the update_est step.  Each block owns a 32 x 8 tile of
 // (x, y) columns and walks UZC planes in z, keeping planes z-1, z, z+1 of x
 // (with halo) in a 3-slot shared-memory ring, so every neighbour read is a
-// shared-memory load at a fixed offset.  Writes x_out; flags non-finite values.
+// shared-memory load at a fixed offset.  The global loads of plane z+2 are
+// issued before plane z is computed (register prefetch), so they overlap the
+// arithmetic.  Writes x_out; flags non-finite values.
 template <int POT>
 __global__ void __launch_bounds__(256) update_kernel(
     const __grid_constant__ Geo G, const __grid_constant__ PriorW W,
@@ -173,47 +175,71 @@ __global__ void __launch_bounds__(256) update_kernel(
     const int x0t = blockIdx.x * UTX, y0t = blockIdx.y * UTY;
     const int zb = blockIdx.z * UZC, ze = min(zb + UZC, g.nz);
     const int64_t plane = (int64_t)g.nx * g.ny;
-    auto load_plane = [&](float* dst, int z) {
+    // This thread's (at most two) cells of a halo plane tile.
+    constexpr int NT = UTX * UTY;
+    static_assert(UPLANE <= 2 * NT, "two cells per thread");
+    const int e1 = tid + NT;
+    const bool has1 = e1 < UPLANE;
+    auto cell_off = [&](int k, bool& ok) -> int64_t {
+        const int r = k / USW, c = k - r * USW;
+        const int gx = x0t - 1 + c, gy = y0t - 1 + r;
+        ok = gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny;
+        return ok ? (int64_t)gy * g.nx + gx : 0;
+    };
+    bool ok0, ok1 = false;
+    const int64_t off0 = cell_off(tid, ok0);
+    const int64_t off1 = has1 ? cell_off(e1, ok1) : 0;
+    const float qnan = __int_as_float(0x7fc00000);  // outside the volume
+    auto fetch = [&](int z, float& v0, float& v1) {
         const bool zin = z >= 0 && z < g.nz;
-        for (int k = tid; k < UPLANE; k += UTX * UTY) {
-            const int r = k / USW, c = k - r * USW;
-            const int gx = x0t - 1 + c, gy = y0t - 1 + r;
-            float v = __int_as_float(0x7fc00000);  // NaN: outside the volume
-            if (zin && gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny)
-                v = __ldg(x + (int64_t)z * plane + (int64_t)gy * g.nx + gx);
-            dst[k] = v;
-        }
+        v0 = (zin && ok0) ? __ldg(x + (int64_t)z * plane + off0) : qnan;
+        v1 = (zin && ok1) ? __ldg(x + (int64_t)z * plane + off1) : qnan;
     };
     float* pb = tile[0];
     float* pc = tile[1];
     float* pa = tile[2];
-    load_plane(pb, zb - 1);
-    load_plane(pc, zb);
+    {
+        float v0, v1;
+        fetch(zb - 1, v0, v1);
+        pb[tid] = v0;
+        if (has1) pb[e1] = v1;
+        fetch(zb, v0, v1);
+        pc[tid] = v0;
+        if (has1) pc[e1] = v1;
+    }
+    float n0, n1;
+    fetch(zb + 1, n0, n1);
     const int ix = x0t + threadIdx.x, iy = y0t + threadIdx.y;
     const bool active = ix < g.nx && iy < g.ny;
     const bool edge_xy = x0t == 0 || x0t + UTX >= g.nx || y0t == 0 || y0t + UTY >= g.ny;
     const float inv_delta = 1.f / delta;
+    const float inv_bx = 1.f / g.bx, inv_by = 1.f / g.by;
     const float x1 = vox_x(g, ix), y1 = vox_y(g, iy);
     const int64_t B = (int64_t)g.nbx * g.nby;
     const int r = threadIdx.y + 1, c = threadIdx.x + 1;
     for (int z = zb; z < ze; z++) {
-        load_plane(pa, z + 1);
+        pa[tid] = n0;
+        if (has1) pa[e1] = n1;
         __syncthreads();
+        if (z + 1 < ze) fetch(z + 2, n0, n1);
         if (active) {
+            const int64_t v = (int64_t)z * plane + (int64_t)iy * g.nx + ix;
+            const float dv = __ldg(d + v);
             const float xc = pc[r * USW + c];
             const float z1 = vox_z(g, z);
-            // M * SBP(h): same arithmetic as bp.cu's sbp_term on the [j][i] layout
+            // M * SBP(h): the arithmetic of bp.cu's sbp_term on the [j][i]
+            // layout, with reciprocal multiplies in place of divisions.
             float capL = 0.f;
             for (int t = 0; t < nv; t++) {
                 const ViewSrc vs = sv[t];
                 const float ddx = vs.x0 - x1, ddy = vs.y0 - y1, ddz = vs.z0 - z1;
-                const float dw = __fdiv_rn(vs.s2, ddx * ddx + ddy * ddy + ddz * ddz);
+                const float dw = __fdividef(vs.s2, ddx * ddx + ddy * ddy + ddz * ddz);
                 if (z1 == vs.z0) continue;
-                const float tt = __fdiv_rn(-g.detectorR - vs.z0, z1 - vs.z0);
+                const float tt = __fdividef(-g.detectorR - vs.z0, z1 - vs.z0);
                 const float x2 = vs.x0 + (x1 - vs.x0) * tt;
                 const float y2 = vs.y0 + (y1 - vs.y0) * tt;
-                const float imb = __fdiv_rn(x2 - g.x_d0, g.bx);
-                const float jmb = __fdiv_rn(y2 - g.y_d0, g.by);
+                const float imb = (x2 - g.x_d0) * inv_bx;
+                const float jmb = (y2 - g.y_d0) * inv_by;
                 int ilb = (int)floorf(imb);
                 if (imb < (float)ilb + 0.5f) ilb -= 1;
                 int jlb = (int)floorf(jmb);
@@ -239,8 +265,7 @@ __global__ void __launch_bounds__(256) update_kernel(
                 prior_sums_tile<POT, true>(W, pb, pc, pa, r, c, xc, delta, inv_delta, &rdd, &rd);
             else
                 prior_sums_tile<POT, false>(W, pb, pc, pa, r, c, xc, delta, inv_delta, &rdd, &rd);
-            const int64_t v = (int64_t)z * plane + (int64_t)iy * g.nx + ix;
-            const float xn = xc - __fdividef(capL + beta * rd, d[v] + 2.f * beta * rdd);
+            const float xn = xc - __fdividef(capL + beta * rd, dv + 2.f * beta * rdd);
             if (!(fabsf(xn) < __int_as_float(0x7f800000))) atomicOr(status, NR_FLAG_NONFINITE);
             x_out[v] = xn < 0.f ? 0.f : xn;
         }

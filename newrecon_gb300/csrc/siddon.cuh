@@ -61,7 +61,12 @@ __device__ __forceinline__ Axis axis_setup(float e, float d, float L, int n, flo
 // Traces the ray (x0,y0,z0) -> (x1,y1,z1).  MODE 0: sum_j len_j * vol_j;
 // MODE 1: in-volume chord length; MODE 2: full length |src - bin|.
 // Returns false when the ray misses the volume (the reference's status -1).
-template <int MODE>
+//
+// MODE 0 walks in batches of K steps: the voxel indices and chord lengths of
+// K segments are computed first (they do not depend on the volume), then the
+// K gathers are issued together and accumulated in segment order, so a warp
+// keeps K loads in flight instead of one.  The sum is bit-identical for every K.
+template <int MODE, int K = 4>
 __device__ __forceinline__ bool trace(const Geo& G, const float* __restrict__ vol, float x0,
                                       float y0, float z0, float x1, float y1, float z1,
                                       float* out) {
@@ -116,24 +121,40 @@ __device__ __forceinline__ bool trace(const Geo& G, const float* __restrict__ vo
     float cx = 0.f, cy = 0.f, cz = 0.f;
     float s = 0.f, sum = 0.f;
     while (s < smax) {
-        const float m = fminf(fminf(tx, ty), tz);
-        sum = __fmaf_rn(m - s, __ldg(vol + idx), sum);
-        s = m;
-        if (tx == m) {
-            cx += 1.f;
-            tx = __fmaf_rn(cx, ax.step, ax.first);
-            idx += sx;
+        float seg[K];
+        int id[K];
+        bool on[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            on[k] = s < smax;
+            const float m = fminf(fminf(tx, ty), tz);
+            seg[k] = m - s;
+            id[k] = idx;
+            if (on[k]) {
+                s = m;
+                if (tx == m) {
+                    cx += 1.f;
+                    tx = __fmaf_rn(cx, ax.step, ax.first);
+                    idx += sx;
+                }
+                if (ty == m) {
+                    cy += 1.f;
+                    ty = __fmaf_rn(cy, ay.step, ay.first);
+                    idx += sy;
+                }
+                if (tz == m) {
+                    cz += 1.f;
+                    tz = __fmaf_rn(cz, az.step, az.first);
+                    idx += sz;
+                }
+            }
         }
-        if (ty == m) {
-            cy += 1.f;
-            ty = __fmaf_rn(cy, ay.step, ay.first);
-            idx += sy;
-        }
-        if (tz == m) {
-            cz += 1.f;
-            tz = __fmaf_rn(cz, az.step, az.first);
-            idx += sz;
-        }
+        float v[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] = on[k] ? __ldg(vol + id[k]) : 0.f;
+#pragma unroll
+        for (int k = 0; k < K; k++)
+            if (on[k]) sum = __fmaf_rn(seg[k], v[k], sum);
     }
     *out = sum;
     return true;
