@@ -14,6 +14,7 @@
 //     x' = max(0, x - (capL + beta RD) / (d + 2 beta RDD))   (update_est :265-295)
 // and writes x' to a second buffer (neighbours must see the old x).
 #include <cmath>
+#include <utility>
 
 #include "common.cuh"
 
@@ -23,11 +24,10 @@ nr_status launch_bp(const nr_geom& g, bool ji, float* vol, const float* prj, con
                     const int32_t* index, int a0, int nv, cudaStream_t st);
 
 struct PriorW {
-    float w[27];   // weight of neighbour (dx,dy,dz) at ((dz+1)*3+(dy+1))*3+(dx+1); centre 0
-    float wd[27];  // w * delta (Huber)
+    float w[27];  // weight of neighbour (dx,dy,dz) at ((dz+1)*3+(dy+1))*3+(dx+1); centre 0
 };
 
-__host__ inline PriorW make_weights(float zxy, float delta = 1.f) {
+__host__ inline PriorW make_weights(float zxy) {
     PriorW p;
     for (int dz = -1; dz <= 1; dz++)
         for (int dy = -1; dy <= 1; dy++)
@@ -37,7 +37,6 @@ __host__ inline PriorW make_weights(float zxy, float delta = 1.f) {
                 float dist = std::sqrt((float)(dx * dx + dy * dy) + (float)(dz * dz) * zxy * zxy);
                 int k = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
                 p.w[k] = (dist == 0.f) ? 0.f : (float)(1.0 / (double)dist);
-                p.wd[k] = p.w[k] * delta;
             }
     return p;
 }
@@ -110,47 +109,103 @@ constexpr int UTX = 32, UTY = 8, UZC = 16;      // tile: 32 x 8 columns, 16 plan
 constexpr int USW = UTX + 2, USH = UTY + 2;     // plane tile with a 1-voxel halo
 constexpr int UPLANE = USW * USH;
 
-// w * omega(t) for neighbour weight w (wd = w * delta, inv_delta = 1/delta),
-// with the approximate MUFU reciprocal / rsqrt (<= 2 ulp).
-template <int POT>
-__device__ __forceinline__ float w_omega(float t, float w, float wd, float delta, float inv_delta) {
-    if (POT == NR_POT_Q2) return w;
-    if (POT == NR_POT_LANGE) return __fdividef(w, __fmaf_rn(fabsf(t), inv_delta, 1.f));
-    if (POT == NR_POT_HYPERBOLA) {
-        const float u = t * inv_delta;
-        return w * rsqrtf(__fmaf_rn(u, u, 1.f));
-    }
-    return __fdividef(wd, fmaxf(fabsf(t), delta));  // Huber: w * min(1, delta/|t|)
+// The five distinct neighbour weights 1/sqrt(dx^2+dy^2+(dz zr)^2) of the
+// 26-neighbourhood (in-plane face, in-plane diagonal, z face, z edge, z
+// corner) and the same times delta (Huber).
+struct PriorW5 {
+    float w1, w2, wz, wz1, wz2;
+    float d1, d2, dz, dz1, dz2;
+};
+
+__host__ inline PriorW5 make_w5(float zxy, float delta) {
+    auto w = [&](int dx, int dy, int dz) {
+        const float dist = std::sqrt((float)(dx * dx + dy * dy) + (float)(dz * dz) * zxy * zxy);
+        return (float)(1.0 / (double)dist);
+    };
+    PriorW5 p;
+    p.w1 = w(1, 0, 0);
+    p.w2 = w(1, 1, 0);
+    p.wz = w(0, 0, 1);
+    p.wz1 = w(1, 0, 1);
+    p.wz2 = w(1, 1, 1);
+    p.d1 = p.w1 * delta;
+    p.d2 = p.w2 * delta;
+    p.dz = p.wz * delta;
+    p.dz1 = p.wz1 * delta;
+    p.dz2 = p.wz2 * delta;
+    return p;
 }
 
-// Penalty sums from the shared-memory planes (below, centre, above), centre
-// at (r, c).  EDGE: out-of-volume cells hold NaN and count as t = 0.
-template <int POT, bool EDGE>
-__device__ __forceinline__ void prior_sums_tile(const PriorW& W, const float* __restrict__ pb,
-                                                const float* __restrict__ pc,
-                                                const float* __restrict__ pa, int r, int c,
-                                                float xc, float delta, float inv_delta,
-                                                float* rdd, float* rd) {
-    float sdd = 0.f, sd = 0.f;
-#pragma unroll
-    for (int dz = -1; dz <= 1; dz++) {
+// Approximate reciprocal / reciprocal square root (the MUFU unit, <= 1 ulp
+// relative error; arguments here are >= 1 or >= delta, never denormal).
+__device__ __forceinline__ float rcp_approx(float v) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+    return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float v) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
+    return r;
+}
+
+// Neighbour K = ((dz+1)*3 + (dy+1))*3 + (dx+1) of the centre at offset
+// `base` in the shared-memory planes: adds w omega(t) to sdd and w omega(t) t
+// to sd (two accumulator pairs, even/odd K, to shorten the dependency
+// chains).  EDGE: out-of-volume cells hold NaN and count as t = 0.
+template <int POT, bool EDGE, int K>
+__device__ __forceinline__ void nb_term(const float* __restrict__ pb, const float* __restrict__ pc,
+                                        const float* __restrict__ pa, int base, float xc,
+                                        const PriorW5& W, float delta, float inv_delta,
+                                        float& sdd0, float& sd0, float& sdd1, float& sd1) {
+    constexpr int dz = K / 9 - 1, dy = (K / 3) % 3 - 1, dx = K % 3 - 1;
+    if constexpr (K == 13) {
+        return;  // the centre itself
+    } else {
+        constexpr int nxy = (dx != 0) + (dy != 0);
         const float* pl = dz < 0 ? pb : (dz == 0 ? pc : pa);
-#pragma unroll
-        for (int dy = -1; dy <= 1; dy++) {
-#pragma unroll
-            for (int dx = -1; dx <= 1; dx++) {
-                if (dx == 0 && dy == 0 && dz == 0) continue;
-                const int k = ((dz + 1) * 3 + (dy + 1)) * 3 + (dx + 1);
-                float t = xc - pl[(r + dy) * USW + (c + dx)];
-                if (EDGE) t = (t == t) ? t : 0.f;
-                const float wo = w_omega<POT>(t, W.w[k], W.wd[k], delta, inv_delta);
-                sdd += wo;
-                sd = __fmaf_rn(wo, t, sd);
-            }
+        float t = xc - pl[base + dy * USW + dx];
+        if (EDGE) t = (t == t) ? t : 0.f;
+        float w, wd;
+        if (dz == 0) {
+            w = nxy == 1 ? W.w1 : W.w2;
+            wd = nxy == 1 ? W.d1 : W.d2;
+        } else {
+            w = nxy == 0 ? W.wz : (nxy == 1 ? W.wz1 : W.wz2);
+            wd = nxy == 0 ? W.dz : (nxy == 1 ? W.dz1 : W.dz2);
+        }
+        float wo;
+        if (POT == NR_POT_Q2) {
+            wo = w;
+        } else if (POT == NR_POT_LANGE) {
+            wo = w * rcp_approx(__fmaf_rn(fabsf(t), inv_delta, 1.f));
+        } else if (POT == NR_POT_HYPERBOLA) {
+            const float u = t * inv_delta;
+            wo = w * rsqrt_approx(__fmaf_rn(u, u, 1.f));
+        } else {
+            wo = wd * rcp_approx(fmaxf(fabsf(t), delta));  // w min(1, delta/|t|)
+        }
+        if (K & 1) {
+            sdd1 += wo;
+            sd1 = __fmaf_rn(wo, t, sd1);
+        } else {
+            sdd0 += wo;
+            sd0 = __fmaf_rn(wo, t, sd0);
         }
     }
-    *rdd = sdd;
-    *rd = sd;
+}
+
+template <int POT, bool EDGE, int... Ks>
+__device__ __forceinline__ void prior_all(std::integer_sequence<int, Ks...>,
+                                          const float* __restrict__ pb,
+                                          const float* __restrict__ pc,
+                                          const float* __restrict__ pa, int base, float xc,
+                                          const PriorW5& W, float delta, float inv_delta,
+                                          float* rdd, float* rd) {
+    float a0 = 0.f, b0 = 0.f, a1 = 0.f, b1 = 0.f;
+    (nb_term<POT, EDGE, Ks>(pb, pc, pa, base, xc, W, delta, inv_delta, a0, b0, a1, b1), ...);
+    *rdd = a0 + a1;
+    *rd = b0 + b1;
 }
 
 // One sub-iteration's update, fused: SBP of h (subset views, [view][j][i]),
@@ -162,7 +217,7 @@ __device__ __forceinline__ void prior_sums_tile(const PriorW& W, const float* __
 // arithmetic.  Writes x_out; flags non-finite values.
 template <int POT>
 __global__ void __launch_bounds__(256) update_kernel(
-    const __grid_constant__ Geo G, const __grid_constant__ PriorW W,
+    const __grid_constant__ Geo G, const __grid_constant__ PriorW5 W,
     const float* __restrict__ x, float* __restrict__ x_out, const float* __restrict__ d,
     const float* __restrict__ h, const float* __restrict__ angles,
     const int32_t* __restrict__ index, int a0, int nv, float M, float beta, float delta,
@@ -261,10 +316,13 @@ __global__ void __launch_bounds__(256) update_kernel(
             }
             capL = M * capL;
             float rdd, rd;
+            const int base = r * USW + c;
             if (edge_xy || z == 0 || z == g.nz - 1)
-                prior_sums_tile<POT, true>(W, pb, pc, pa, r, c, xc, delta, inv_delta, &rdd, &rd);
+                prior_all<POT, true>(std::make_integer_sequence<int, 27>{}, pb, pc, pa, base, xc, W,
+                                     delta, inv_delta, &rdd, &rd);
             else
-                prior_sums_tile<POT, false>(W, pb, pc, pa, r, c, xc, delta, inv_delta, &rdd, &rd);
+                prior_all<POT, false>(std::make_integer_sequence<int, 27>{}, pb, pc, pa, base, xc, W,
+                                      delta, inv_delta, &rdd, &rd);
             const float xn = xc - __fdividef(capL + beta * rd, dv + 2.f * beta * rdd);
             if (!(fabsf(xn) < __int_as_float(0x7f800000))) atomicOr(status, NR_FLAG_NONFINITE);
             x_out[v] = xn < 0.f ? 0.f : xn;
@@ -302,7 +360,7 @@ static nr_status launch_update_t(const nr_geom& g, const float* x, float* x_out,
                                  int a0, int nv, float M, float beta, float delta, int* status,
                                  cudaStream_t st) {
     dim3 blk(UTX, UTY), grd(cdiv(g.nx, UTX), cdiv(g.ny, UTY), cdiv(g.nz, UZC));
-    update_kernel<POT><<<grd, blk, 0, st>>>(make_geo(g), make_weights(g.vz / g.vx, delta), x,
+    update_kernel<POT><<<grd, blk, 0, st>>>(make_geo(g), make_w5(g.vz / g.vx, delta), x,
                                             x_out, d, h, angles, index, a0, nv, M, beta, delta,
                                             status);
     return launch_status();
