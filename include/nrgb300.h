@@ -209,6 +209,24 @@ nr_status nr_ostr_objective(const nr_geom* g, const nr_ostr_params* p,
 nr_status nr_ostr_check(void* workspace, size_t ws_bytes, int32_t* flags,
                         void* stream);
 
+/* The penalty of nr_ostr_objective (out[1] there) computed without any
+ * workspace, into out[0] (one device double), for callers that may not
+ * allocate device memory: a scanner-side reconstruction service whose memory
+ * is fixed at start-up, or a host framework that owns every device buffer.
+ * No counterpart in the reference.  It allocates nothing: its scratch (the
+ * per-block partial sums) is a file-scope device array of NR_STATIC_PARTIALS
+ * = 2^18 doubles (2 MiB, held on every GPU that loads the library until the
+ * process exits), which limits the volume to 2^18 blocks of 32 x 4 voxel
+ * columns per plane, i.e. ceil(nx/32) * ceil(ny/4) * nz <= 262144
+ * (1024x512x64 fits); larger volumes return NR_ERR_WORKSPACE.  The first call
+ * on each device looks up the array's device address (cudaGetSymbolAddress)
+ * with that device current; make that first call before any stream capture.
+ * Every call shares the one array: calls that overlap on the GPU (other
+ * streams, other host threads) race on it and must be serialised by the
+ * caller.  Each call overwrites the partials it uses, so nothing carries over. */
+nr_status nr_penalty_fp64_static(const nr_geom* g, const float* x, int32_t potential,
+                                 float delta, double* out, void* stream);
+
 /* Library version string. */
 const char* nr_version(void);
 

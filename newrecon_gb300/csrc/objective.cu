@@ -13,6 +13,7 @@
 // shuffles, then a per-block partial; a single block adds the partials in a
 // fixed order, so the value is deterministic.
 #include <cmath>
+#include <mutex>
 
 #include "siddon.cuh"
 
@@ -202,3 +203,90 @@ nr_status launch_objective(const nr_geom& g, int pot, float delta, const float* 
 }
 
 }  // namespace nr
+
+// ---------------------------------------------------------------------------
+// Penalty without a workspace, for callers that may not allocate device memory.
+//
+// Scratch: the per-block partial sums of penalty_kernel live in this
+// file-scope device array (2 MiB, one copy on every GPU that loads the
+// library, kept until the process exits).  In host code the name
+// g_static_partials is only a host-side stand-in; the device address is
+// obtained once per device with cudaGetSymbolAddress and cached.
+#define NR_STATIC_PARTIALS (1 << 18)
+
+static __device__ __align__(256) double g_static_partials[NR_STATIC_PARTIALS];
+
+namespace nr {
+
+// Sum of n partials into out[0], fixed order (one block of 1024 threads).
+__global__ void __launch_bounds__(1024) static_sum_kernel(const double* __restrict__ red, int64_t n,
+                                                          double* __restrict__ out) {
+    __shared__ double ws[32];
+    double s = 0.0;
+    for (int64_t k = threadIdx.x; k < n; k += blockDim.x) s += red[k];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = ws[threadIdx.x];
+        t = warp_sum(t);
+        if (threadIdx.x == 0) out[0] = t;
+    }
+}
+
+// Device address of g_static_partials on the current device.  The first call
+// on a device looks it up (cudaGetSymbolAddress) with that device current.
+static double* static_partials(nr_status* st) {
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu;
+    static double* ptrs[kMaxDevices] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        *st = NR_ERR_CUDA;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ptrs[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_static_partials) != cudaSuccess || !p) {
+            *st = NR_ERR_CUDA;
+            return nullptr;
+        }
+        ptrs[dev] = (double*)p;
+    }
+    return ptrs[dev];
+}
+
+}  // namespace nr
+
+using namespace nr;
+
+NR_API nr_status nr_penalty_fp64_static(const nr_geom* g, const float* x, int32_t potential,
+                                        float delta, double* out, void* stream) {
+    if (!geom_ok(g)) return NR_ERR_BAD_GEOMETRY;
+    if (!x || !out) return NR_ERR_BAD_ARGUMENT;
+    if (potential < NR_POT_Q2 || potential > NR_POT_HUBER) return NR_ERR_BAD_ARGUMENT;
+    if (potential != NR_POT_Q2 && !(delta > 0.f)) return NR_ERR_BAD_ARGUMENT;
+    if (g->vx != g->vy || g->nz > 65535) return NR_ERR_BAD_GEOMETRY;
+    const int64_t np = pen_blocks(*g);
+    if (np > NR_STATIC_PARTIALS) return NR_ERR_WORKSPACE;  // volume too large for the scratch
+    nr_status st = NR_OK;
+    double* red = static_partials(&st);
+    if (!red) return st;
+    cudaStream_t s = as_stream(stream);
+    const Geo G = make_geo(*g);
+    const PairW W = make_pair_weights(g->vz / g->vx);
+    const float dl = potential == NR_POT_Q2 ? 1.f : delta;
+    dim3 blk(32, 4), grd(cdiv(g->nx, 32), cdiv(g->ny, 4), g->nz);
+    // every block overwrites its own partial: nothing to clear between calls
+    switch (potential) {
+    case NR_POT_Q2: penalty_kernel<NR_POT_Q2><<<grd, blk, 0, s>>>(G, W, x, dl, red); break;
+    case NR_POT_LANGE: penalty_kernel<NR_POT_LANGE><<<grd, blk, 0, s>>>(G, W, x, dl, red); break;
+    case NR_POT_HYPERBOLA:
+        penalty_kernel<NR_POT_HYPERBOLA><<<grd, blk, 0, s>>>(G, W, x, dl, red);
+        break;
+    default: penalty_kernel<NR_POT_HUBER><<<grd, blk, 0, s>>>(G, W, x, dl, red); break;
+    }
+    static_sum_kernel<<<1, 1024, 0, s>>>(red, np, out);
+    return launch_status();
+}

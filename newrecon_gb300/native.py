@@ -56,6 +56,7 @@ SIGNATURES = {
                                          ctypes.POINTER(ctypes.c_void_p),
                                          ctypes.POINTER(ctypes.c_size_t)]),
     "nr_ostr_check": (_I32, [_P, ctypes.c_size_t, ctypes.POINTER(_I32), _P]),
+    "nr_penalty_fp64_static": (_I32, [_GP, _P, _I32, _F, _P, _P]),
     "nr_version": (ctypes.c_char_p, []),
 }
 
