@@ -261,7 +261,7 @@ def run_ours(args):
     if os.path.isfile(prof_traffic):
         for ln in open(prof_traffic):
             parts = ln.split()
-            if len(parts) >= 2 and parts[0] == dom and not ln.startswith("#"):
+            if len(parts) >= 2 and not ln.startswith("#") and parts[0] == dom:
                 traffic = float(parts[1])
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
