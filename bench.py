@@ -51,13 +51,6 @@ def parse():
     return ap.parse_args()
 
 
-def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
-
-
 def make_scan_gpu(cfg, seed):
     """Phantom + counts; the counts' forward projection runs on the GPU."""
     import torch
@@ -178,17 +171,18 @@ def run_ours(args):
     import torch
     import torch.distributed as dist
 
-    from newrecon_gb300 import native, ostr
+    from newrecon_gb300 import native, ostr, replicas
     from newrecon_gb300.geometry import config
 
-    ws, rank, local = dist_env()
+    ws, rank, local = replicas.env()
     if ws > 1:
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     native.load()
-    cfg = config(args.config, seed=rank)
+    seed = replicas.case_seed(0, rank)
+    cfg = config(args.config, seed=seed)
     g = cfg.geom
-    x_true, y, b = make_scan_gpu(cfg, seed=rank)
+    x_true, y, b = make_scan_gpu(cfg, seed=seed)
     plan = ostr.OSTR(g, subset_num=cfg.subset_num, beta=cfg.beta, delta=cfg.delta,
                      potential=cfg.potential)
     plan.setup(cfg.angles, y, b)
@@ -232,15 +226,11 @@ def run_ours(args):
         dist.barrier()
     clk = clocks.stop()
     elapsed = t_start.elapsed_time(t_end) / 1e3
-    if ws > 1:
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed, n_sub = replicas.reduce_timing(elapsed, M * args.steps)
     plan.check()
     fp_ms = np.array([events[3 * k].elapsed_time(events[3 * k + 1]) for k in range(M * args.steps)])
     up_ms = np.array([events[3 * k + 1].elapsed_time(events[3 * k + 2])
                       for k in range(M * args.steps)])
-    n_sub = M * args.steps * ws
     value = n_sub / elapsed
     N = g.n_voxels
     B = g.n_bins
@@ -327,7 +317,9 @@ def e2e_ours(args, cfg, y, b):
 
 
 def run_reference(args):
-    ws, rank, local = dist_env()
+    from newrecon_gb300 import replicas
+
+    ws, rank, local = replicas.env()
     if rank != 0:
         return
     from newrecon_gb300.geometry import config
