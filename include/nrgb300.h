@@ -195,6 +195,52 @@ nr_status nr_ostr_subiter(const nr_geom* g, const nr_ostr_params* p, float* x,
                           int32_t subset, void* workspace, size_t ws_bytes,
                           void* stream);
 
+/* Captures n_iters iterations of nr_ostr_iterate on x (fixed pointers: x and
+ * the workspace are baked in) into a CUDA graph and instantiates it; *graph
+ * receives an opaque handle.  stream must be a non-default stream (capture
+ * runs on it; nothing executes).  The handle is host memory owned by the
+ * caller: release it with nr_ostr_graph_destroy.  No reference counterpart
+ * (the reference relaunches and synchronises every kernel). */
+nr_status nr_ostr_graph_create(const nr_geom* g, const nr_ostr_params* p, float* x,
+                               int32_t n_iters, void* workspace, size_t ws_bytes,
+                               void* stream, void** graph);
+/* Replays a captured graph (iteration loop or batch) on stream. */
+nr_status nr_ostr_graph_launch(void* graph, void* stream);
+/* Releases a graph handle (NULL is a no-op). */
+nr_status nr_ostr_graph_destroy(void* graph);
+
+/* ---------------------------------------------------------------------------
+ * Batched reconstructions (no reference counterpart: the reference runs one
+ * case per process).  Each case has its own geometry, parameters, volume and
+ * workspace (set up with nr_ostr_setup); a batch step advances every
+ * unfinished case by one sub-iteration with two persistent launches over all
+ * cases' work items.  Up to 64 cases.
+ * ------------------------------------------------------------------------- */
+typedef struct nr_batch_case {
+    nr_geom g;
+    nr_ostr_params p;
+    int32_t n_iters;       /* iterations of this case (n_iters * M sub-iterations) */
+    float* x;              /* volume, updated in place                            */
+    void* workspace;       /* this case's workspace after nr_ostr_setup           */
+    size_t ws_bytes;
+} nr_batch_case;
+
+/* Bytes of the device table describing n_cases cases. */
+nr_status nr_batch_table_size(int32_t n_cases, size_t* bytes);
+/* Writes the case table (256-byte aligned device memory of nr_batch_table_size
+ * bytes) and returns the number of batch steps (the largest n_iters * M).
+ * Synchronises stream (the table image is copied from host memory). */
+nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, void* table,
+                           size_t table_bytes, int32_t* n_steps, void* stream);
+/* One batch step (step = 0, 1, ... in order). */
+nr_status nr_batch_step(const void* table, int32_t step, void* stream);
+/* After the last step: moves results that ended in the ping-pong buffer into x. */
+nr_status nr_batch_finish(const void* table, void* stream);
+/* Captures steps 0 .. n_steps-1 and the finish into a CUDA graph (replay with
+ * nr_ostr_graph_launch, release with nr_ostr_graph_destroy); stream must be a
+ * non-default stream. */
+nr_status nr_batch_graph_create(const void* table, int32_t n_steps, void* stream, void** graph);
+
 /* Penalized-likelihood objective in FP64 (no reference counterpart; the
  * reference has no objective):
  *   out[0] = sum_i (ybar_i + r_i - y_i log(ybar_i + r_i)),  ybar = b exp(-FP_cos(x))

@@ -93,4 +93,31 @@ __host__ inline nr_status launch_status() {
 
 __host__ inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
 
+// A captured launch sequence: the graph and its executable instance (the
+// opaque handle of nr_ostr_graph_create / nr_batch_graph_create).
+struct GraphHandle {
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+};
+
+// Ends the capture on s (always), instantiates on success and returns the
+// handle in *out; on any failure nothing is left allocated.
+__host__ inline nr_status finish_capture(cudaStream_t s, nr_status st, void** out) {
+    cudaGraph_t gr = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(s, &gr);
+    if (st != NR_OK || ec != cudaSuccess || !gr) {
+        if (gr) cudaGraphDestroy(gr);
+        cudaGetLastError();
+        return st != NR_OK ? st : NR_ERR_CUDA;
+    }
+    cudaGraphExec_t ex = nullptr;
+    if (cudaGraphInstantiate(&ex, gr, 0) != cudaSuccess) {
+        cudaGraphDestroy(gr);
+        cudaGetLastError();
+        return NR_ERR_CUDA;
+    }
+    *out = new GraphHandle{gr, ex};
+    return NR_OK;
+}
+
 }  // namespace nr

@@ -6,17 +6,9 @@
 // the same few 128-byte lines of one volume row (the volume is x-fastest):
 // the gathers coalesce.  Views of a launch run on gridDim.z.  The walk itself
 // is in siddon.cuh.
-#include "siddon.cuh"
+#include "project.cuh"
 
 namespace nr {
-
-// Detector offset of bin (i, j) of one view: JI -> [j][i] (i fastest, the
-// layout of the fused path and of the scanner files); otherwise [i][j] (the
-// reference's in-memory layout, Tomo_OSTR.cu:1365).
-template <bool JI>
-__device__ __forceinline__ int64_t bin_off(const nr_geom& g, int i, int j) {
-    return JI ? (int64_t)j * g.nbx + i : (int64_t)i * g.nby + j;
-}
 
 // Reference-shaped projector: out[(a-a0)] = cos * line integral (MODE 0) or
 // gamma (MODE 1 chord, MODE 2 length); missed rays leave out untouched
@@ -42,12 +34,7 @@ __global__ void __launch_bounds__(128) fp_kernel(const __grid_constant__ Geo G,
     }
 }
 
-// Fused forward projection + OSTR gradient h for the subset views of the
-// device-resident path.  Detector arrays are [view][j][i] in subset order;
-// y, b (and r) are indexed by the subset position a.  Rays that miss the
-// volume have line = 0 (the reference zeroes the line buffer every subset,
-// Tomo_OSTR_gold.cpp:843).  h = (y/(b e^-l + r) - 1) b e^-l,
-// Tomo_OSTR_gold.cpp:245-260.
+// Fused forward projection + h, one block per 32 x 4 bins of one subset view.
 __global__ void __launch_bounds__(128) fp_h_kernel(const __grid_constant__ Geo G,
                                                    const float* __restrict__ vol,
                                                    float* __restrict__ h,
@@ -57,22 +44,7 @@ __global__ void __launch_bounds__(128) fp_h_kernel(const __grid_constant__ Geo G
                                                    const float* __restrict__ b,
                                                    const float* __restrict__ r) {
     __shared__ ViewSrc src;
-    const nr_geom& g = G.g;
-    const int a = a0 + blockIdx.z;
-    if (threadIdx.x == 0 && threadIdx.y == 0) src = view_source(g, angles[index[a]]);
-    __syncthreads();
-    const int i = blockIdx.x * 32 + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.nbx || j >= g.nby) return;
-    float v = 0.f;
-    float l = 0.f;
-    if (trace<0>(G, vol, src.x0, src.y0, src.z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v))
-        l = v * src.ct;
-    const int64_t B = (int64_t)g.nbx * g.nby;
-    const int64_t o = (int64_t)a * B + bin_off<true>(g, i, j);
-    const float yb = b[o] * expf(-l);
-    const float den = yb + (r ? r[o] : 0.f);
-    h[(int64_t)blockIdx.z * B + bin_off<true>(g, i, j)] = (__fdiv_rn(y[o], den) - 1.f) * yb;
+    fp_h_tile(G, vol, h, angles, index, a0, y, b, r, blockIdx.x, blockIdx.y, blockIdx.z, src);
 }
 
 // gamma * yry for every view in one pass (the d precompute's detector term,

@@ -136,6 +136,27 @@ __global__ void clear_status_kernel(int* s) {
     if (threadIdx.x < 64) s[threadIdx.x] = 0;
 }
 
+// Section pointers of a set-up workspace, for the batched path (batch.cu).
+nr_status ostr_sections(const nr_geom* g, const nr_ostr_params* p, void* ws, size_t bytes,
+                        float** xtmp, float** h, const float** d, const float** y,
+                        const float** b, const float** r, const float** angles,
+                        const int32_t** index, int** status) {
+    Layout L;
+    nr_status st = check_ws(g, p, ws, bytes, &L);
+    if (st != NR_OK) return st;
+    WS w = carve(ws, L);
+    *xtmp = w.xtmp;
+    *h = w.h;
+    *d = w.d;
+    *y = w.y;
+    *b = w.b;
+    *r = w.r;
+    *angles = w.angles;
+    *index = w.index;
+    *status = w.status;
+    return NR_OK;
+}
+
 }  // namespace nr
 
 using namespace nr;
@@ -255,16 +276,12 @@ NR_API nr_status nr_ostr_subiter(const nr_geom* g, const nr_ostr_params* p, floa
     return NR_OK;
 }
 
-NR_API nr_status nr_ostr_iterate(const nr_geom* g, const nr_ostr_params* p, float* x,
-                                 int32_t n_iters, void* workspace, size_t ws_bytes, void* stream) {
-    Layout L;
-    nr_status st = check_ws(g, p, workspace, ws_bytes, &L);
-    if (st != NR_OK) return st;
-    if (!x || n_iters < 0) return NR_ERR_BAD_ARGUMENT;
-    cudaStream_t s = as_stream(stream);
-    WS w = carve(workspace, L);
+// Enqueues n_iters iterations on stream s (ping-pong between x and xtmp).
+static nr_status enqueue_iterations(const nr_geom* g, const nr_ostr_params* p, float* x,
+                                    int32_t n_iters, const WS& w, cudaStream_t s) {
     const int A = g->n_angles, M = p->subset_num, Vs = A / M;
     const int64_t N = (int64_t)g->nx * g->ny * g->nz;
+    nr_status st;
     float* cur = x;
     float* nxt = w.xtmp;
     for (int it = 0; it < n_iters; it++) {
@@ -284,6 +301,45 @@ NR_API nr_status nr_ostr_iterate(const nr_geom* g, const nr_ostr_params* p, floa
     if (cur != x &&
         cudaMemcpyAsync(x, cur, N * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
         return NR_ERR_CUDA;
+    return NR_OK;
+}
+
+NR_API nr_status nr_ostr_iterate(const nr_geom* g, const nr_ostr_params* p, float* x,
+                                 int32_t n_iters, void* workspace, size_t ws_bytes, void* stream) {
+    Layout L;
+    nr_status st = check_ws(g, p, workspace, ws_bytes, &L);
+    if (st != NR_OK) return st;
+    if (!x || n_iters < 0) return NR_ERR_BAD_ARGUMENT;
+    return enqueue_iterations(g, p, x, n_iters, carve(workspace, L), as_stream(stream));
+}
+
+NR_API nr_status nr_ostr_graph_create(const nr_geom* g, const nr_ostr_params* p, float* x,
+                                      int32_t n_iters, void* workspace, size_t ws_bytes,
+                                      void* stream, void** graph) {
+    Layout L;
+    nr_status st = check_ws(g, p, workspace, ws_bytes, &L);
+    if (st != NR_OK) return st;
+    if (!x || n_iters < 1 || !graph || !stream) return NR_ERR_BAD_ARGUMENT;
+    *graph = nullptr;
+    cudaStream_t s = as_stream(stream);
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return NR_ERR_CUDA;
+    st = enqueue_iterations(g, p, x, n_iters, carve(workspace, L), s);
+    return finish_capture(s, st, graph);
+}
+
+NR_API nr_status nr_ostr_graph_launch(void* graph, void* stream) {
+    if (!graph) return NR_ERR_BAD_ARGUMENT;
+    auto* h = static_cast<GraphHandle*>(graph);
+    return cudaGraphLaunch(h->exec, as_stream(stream)) == cudaSuccess ? NR_OK : NR_ERR_CUDA;
+}
+
+NR_API nr_status nr_ostr_graph_destroy(void* graph) {
+    if (!graph) return NR_OK;
+    auto* h = static_cast<GraphHandle*>(graph);
+    cudaGraphExecDestroy(h->exec);
+    cudaGraphDestroy(h->graph);
+    delete h;
     return NR_OK;
 }
 

@@ -46,6 +46,15 @@ class NrOstrParams(ctypes.Structure):
     ]
 
 
+class NrBatchCase(ctypes.Structure):
+    """ctypes image of ``nr_batch_case`` (include/nrgb300.h)."""
+
+    _fields_ = [
+        ("g", NrGeom), ("p", NrOstrParams), ("n_iters", ctypes.c_int32),
+        ("x", ctypes.c_void_p), ("workspace", ctypes.c_void_p), ("ws_bytes", ctypes.c_size_t),
+    ]
+
+
 POTENTIALS = {"q2": 0, "lange": 1, "hyperbola": 2, "huber": 3}
 GAMMA_MODES = {"length": 0, "chord": 1}
 
@@ -199,6 +208,35 @@ def config(name: str, seed: int = 0) -> ReconConfig:
 
 
 CONFIG_NAMES: List[str] = ["tiny", "small", "clinical", "fullres"]
+
+
+def batch_configs(n_cases: int = 16, seed: int = 0, iter_num: int = 50,
+                  scale: float = 1.0) -> List[ReconConfig]:
+    """The batched workload: independent cases with uneven thickness and views.
+
+    Per case (seeded): thickness U(30, 80) slices of 1 mm, in-plane size
+    U(512, 1024) x U(256, 512) voxels of 0.14 mm, 9, 15 or 25 views over
+    +-U(7.5, 25) deg with one view per subset, I0 U(3e3, 2e4), glandular
+    fraction U(10 %, 50 %) (the case's n_glandular holds the percentage);
+    detector 1664 x 832 of 0.14 mm, hyperbola delta 0.002, beta 50.  `scale`
+    shrinks every length in voxels / bins (for tests).
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for c in range(n_cases):
+        nz = int(round(rng.uniform(30, 80) * scale)) or 1
+        nx = max(8, int(round(rng.uniform(512, 1024) * scale)))
+        ny = max(8, int(round(rng.uniform(256, 512) * scale)))
+        views = int(rng.choice([9, 15, 25]))
+        span = float(rng.uniform(7.5, 25.0))
+        I0 = float(rng.uniform(3e3, 2e4))
+        gland = float(rng.uniform(0.10, 0.50))
+        g = Geometry.dbt(nx, ny, nz, 0.14, 1.0, max(8, int(round(1664 * scale))),
+                         max(8, int(round(832 * scale))), 0.14, views)
+        out.append(ReconConfig(f"batch{c}", g, view_angles(views, span), I0, views, iter_num,
+                               "hyperbola", 50.0, 0.002, int(round(100 * gland)), 20,
+                               float(nz), seed * 1000 + c))
+    return out
 
 
 def geometry_dict(g: Geometry) -> Dict[str, float]:

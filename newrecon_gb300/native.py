@@ -55,6 +55,15 @@ SIGNATURES = {
     "nr_ostr_workspace_section": (_I32, [_GP, _PP, _I32, _P, ctypes.c_size_t,
                                          ctypes.POINTER(ctypes.c_void_p),
                                          ctypes.POINTER(ctypes.c_size_t)]),
+    "nr_ostr_graph_create": (_I32, [_GP, _PP, _P, _I32, _P, ctypes.c_size_t, _P,
+                                    ctypes.POINTER(ctypes.c_void_p)]),
+    "nr_ostr_graph_launch": (_I32, [_P, _P]),
+    "nr_ostr_graph_destroy": (_I32, [_P]),
+    "nr_batch_table_size": (_I32, [_I32, ctypes.POINTER(ctypes.c_size_t)]),
+    "nr_batch_prepare": (_I32, [_P, _I32, _P, ctypes.c_size_t, ctypes.POINTER(_I32), _P]),
+    "nr_batch_step": (_I32, [_P, _I32, _P]),
+    "nr_batch_finish": (_I32, [_P, _P]),
+    "nr_batch_graph_create": (_I32, [_P, _I32, _P, ctypes.POINTER(ctypes.c_void_p)]),
     "nr_ostr_check": (_I32, [_P, ctypes.c_size_t, ctypes.POINTER(_I32), _P]),
     "nr_penalty_fp64_static": (_I32, [_GP, _P, _I32, _F, _P, _P]),
     "nr_version": (ctypes.c_char_p, []),

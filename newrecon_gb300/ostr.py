@@ -31,7 +31,7 @@ import numpy as np
 import torch
 
 from . import native
-from .geometry import GAMMA_MODES, POTENTIALS, Geometry, NrOstrParams
+from .geometry import GAMMA_MODES, POTENTIALS, Geometry, NrBatchCase, NrOstrParams
 
 # ---------------------------------------------------------------------------
 # Module-level configuration, as in the reference (ostr.py:21-75).  Values are
@@ -425,6 +425,10 @@ class OSTR:
         off = int(ptr.value) - self.ws.data_ptr()
         return self.ws[off:off + int(nb.value)].view(dt)
 
+    def graph(self, x: torch.Tensor, n_iters: int) -> "OstrGraph":
+        """n_iters iterations on x captured once as a CUDA graph; replay with .launch()."""
+        return OstrGraph(self, x, n_iters)
+
     def objective(self, x: torch.Tensor) -> Tuple[float, float]:
         """(data term, penalty) in FP64; total = data + beta * penalty."""
         ws, n = self._ws()
@@ -443,6 +447,119 @@ class OSTR:
         flags = ctypes.c_int32(0)
         native.call("nr_ostr_check", ws, n, ctypes.byref(flags), _stream())
         return int(flags.value)
+
+
+class OstrGraph:
+    """A captured iteration loop (nr_ostr_graph_*): x and the plan's workspace
+    are fixed; each launch() runs the iterations again on the current x."""
+
+    def __init__(self, plan: OSTR, x: torch.Tensor, n_iters: int):
+        self.plan = plan
+        self.x = x
+        self.n_iters = int(n_iters)
+        self.handle = ctypes.c_void_p(0)
+        self._stream = torch.cuda.Stream()
+        self._stream.wait_stream(torch.cuda.current_stream())
+        ws, n = plan._ws()
+        native.call("nr_ostr_graph_create", ctypes.byref(plan.gc), ctypes.byref(plan.params),
+                    _p(x), self.n_iters, ws, n, ctypes.c_void_p(self._stream.cuda_stream),
+                    ctypes.byref(self.handle))
+
+    def launch(self) -> None:
+        native.call("nr_ostr_graph_launch", self.handle, _stream())
+
+    def close(self) -> None:
+        if self.handle and self.handle.value:
+            torch.cuda.synchronize()
+            native.call("nr_ostr_graph_destroy", self.handle)
+            self.handle = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent reconstructions advanced together by persistent
+    batched launches (nr_batch_*): each case has its own geometry, view
+    count, potential and iteration count.
+
+    >>> b = Batch([dict(geom=g1, angles=a1, prj=y1, blank=b1, subset_num=9, iter_num=50,
+    ...                 beta=50, delta=0.002, potential="hyperbola"), ...])
+    >>> volumes = b.run()            # or: gr = b.graph(); gr.launch()
+    """
+
+    def __init__(self, cases):
+        if not 1 <= len(cases) <= 64:
+            raise ValueError("a batch holds 1 to 64 cases")
+        self.plans, self.x = [], []
+        arr = (NrBatchCase * len(cases))()
+        for k, c in enumerate(cases):
+            scat = c.get("scat")
+            plan = OSTR(c["geom"], subset_num=c["subset_num"], beta=c["beta"], delta=c["delta"],
+                        potential=c.get("potential", "lange"),
+                        gamma_mode=c.get("gamma_mode", "length"), has_scatter=scat is not None)
+            plan.setup(c["angles"], c["prj"], c["blank"], scat)
+            x0 = c.get("x0")
+            x = (torch.zeros(c["geom"].n_voxels, dtype=torch.float32, device=plan.ws.device)
+                 if x0 is None else _in(x0).clone())
+            self.plans.append(plan)
+            self.x.append(x)
+            arr[k] = NrBatchCase(plan.gc, plan.params, int(c["iter_num"]),
+                                 ctypes.c_void_p(x.data_ptr()),
+                                 ctypes.c_void_p(plan.ws.data_ptr()), plan.ws_bytes)
+        self._cases = arr
+        size = ctypes.c_size_t(0)
+        native.call("nr_batch_table_size", len(cases), ctypes.byref(size))
+        self.table = torch.empty(int(size.value), dtype=torch.uint8, device=self.x[0].device)
+        steps = ctypes.c_int32(0)
+        native.call("nr_batch_prepare", arr, len(cases), _p(self.table), size,
+                    ctypes.byref(steps), _stream())
+        self.n_steps = int(steps.value)
+
+    def run(self):
+        """All steps and the finish on the current stream; returns the volumes."""
+        for k in range(self.n_steps):
+            native.call("nr_batch_step", _p(self.table), k, _stream())
+        native.call("nr_batch_finish", _p(self.table), _stream())
+        self.check()
+        return self.x
+
+    def check(self) -> None:
+        for p in self.plans:
+            p.check()
+
+    def graph(self) -> "BatchGraph":
+        return BatchGraph(self)
+
+
+class BatchGraph:
+    """The whole batch loop (all steps + finish) captured once as a CUDA graph."""
+
+    def __init__(self, batch: Batch):
+        self.batch = batch
+        self.handle = ctypes.c_void_p(0)
+        self._stream = torch.cuda.Stream()
+        self._stream.wait_stream(torch.cuda.current_stream())
+        native.call("nr_batch_graph_create", _p(batch.table), batch.n_steps,
+                    ctypes.c_void_p(self._stream.cuda_stream), ctypes.byref(self.handle))
+
+    def launch(self) -> None:
+        native.call("nr_ostr_graph_launch", self.handle, _stream())
+
+    def close(self) -> None:
+        if self.handle and self.handle.value:
+            torch.cuda.synchronize()
+            native.call("nr_ostr_graph_destroy", self.handle)
+            self.handle = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def reconstruct(geom: Geometry, prj, blank, scatter=None, *, angles, subset_num: int,

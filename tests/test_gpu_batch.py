@@ -1,0 +1,121 @@
+"""CUDA-graph replay of the subset loop and the batched persistent path, against
+the single-reconstruction path (same tile code, so results agree to float
+rounding of possibly different instruction scheduling; in practice exactly)."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+from test_oracle_golden import geom_of
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mod():
+    from newrecon_gb300 import native, ostr
+
+    native.load()
+    return ostr
+
+
+def close(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) <= 1e-6 * max(np.linalg.norm(b), 1e-30) and \
+        np.abs(a - b).max() <= 1e-5 * max(np.abs(b).max(), 1e-30)
+
+
+def small_scan():
+    from newrecon_gb300.geometry import config
+    from newrecon_gb300.phantom import breast_phantom, poisson_counts
+    from oracle.oracle import Oracle
+
+    cfg = config("small")
+    g = cfg.geom
+    x = breast_phantom(g, 0, cfg.n_glandular, cfg.n_calc).ravel()
+    idx = np.arange(g.n_angles, dtype=np.int32)
+    y = poisson_counts(Oracle(np.float64).fp_ostr(g, x, cfg.angles, idx, 0, g.n_angles),
+                       cfg.I0, 0)
+    return cfg, y, np.full_like(y, cfg.I0)
+
+
+def test_graph_replay_matches_iterate(mod):
+    cfg, y, b = small_scan()
+    plan = mod.OSTR(cfg.geom, subset_num=cfg.subset_num, beta=cfg.beta, delta=cfg.delta,
+                    potential=cfg.potential)
+    plan.setup(cfg.angles, y, b)
+    x1 = torch.zeros(cfg.geom.n_voxels, device="cuda")
+    x2 = torch.zeros(cfg.geom.n_voxels, device="cuda")
+    gr = plan.graph(x2, 2)
+    plan.iterate(x1, 2)
+    gr.launch()
+    torch.cuda.synchronize()
+    assert torch.equal(x1, x2)
+    plan.iterate(x1, 2)
+    gr.launch()  # replays continue from the current x
+    torch.cuda.synchronize()
+    assert torch.equal(x1, x2)
+    gr.close()
+
+
+def test_graph_with_odd_subiteration_count(mod):
+    z = golden("tiny")
+    g = geom_of(z)
+    plan = mod.OSTR(g, subset_num=3, beta=float(z["beta"]), delta=float(z["delta"]),
+                    potential="lange")
+    plan.setup(z["angles"], z["y"], z["b"])
+    x1 = torch.zeros(g.n_voxels, device="cuda")
+    x2 = torch.zeros(g.n_voxels, device="cuda")
+    gr = plan.graph(x2, 1)  # 3 sub-iterations: ends in the ping-pong buffer, copied back
+    plan.iterate(x1, 1)
+    gr.launch()
+    torch.cuda.synchronize()
+    assert torch.equal(x1, x2)
+    gr.close()
+
+
+def batch_cases():
+    cfg, y, b = small_scan()
+    zt, zr = golden("tiny"), golden("ragged")
+    return [
+        dict(geom=cfg.geom, angles=cfg.angles, prj=y, blank=b, subset_num=cfg.subset_num,
+             iter_num=2, beta=cfg.beta, delta=cfg.delta, potential="hyperbola"),
+        dict(geom=geom_of(zt), angles=zt["angles"], prj=zt["y"], blank=zt["b"], subset_num=3,
+             iter_num=1, beta=float(zt["beta"]), delta=float(zt["delta"]), potential="lange"),
+        dict(geom=geom_of(zr), angles=zr["angles"], prj=zr["y"], blank=zr["b"], scat=zr["s"],
+             subset_num=2, iter_num=3, beta=float(zr["beta"]), delta=float(zr["delta"]),
+             potential="huber"),
+        dict(geom=geom_of(zt), angles=zt["angles"], prj=zt["y"], blank=zt["b"], subset_num=6,
+             iter_num=2, beta=float(zt["beta"]), delta=float(zt["delta"]), potential="q2"),
+    ]
+
+
+def single(mod, c):
+    return mod.reconstruct(c["geom"], c["prj"], c["blank"], c.get("scat"), angles=c["angles"],
+                           subset_num=c["subset_num"], iter_num=c["iter_num"], beta=c["beta"],
+                           delta=c["delta"], potential=c["potential"])
+
+
+def test_batch_matches_single_reconstructions(mod):
+    cases = batch_cases()
+    bt = mod.Batch(cases)
+    assert bt.n_steps == max(c["iter_num"] * c["subset_num"] for c in cases)
+    out = [x.cpu().numpy() for x in bt.run()]
+    for c, xb in zip(cases, out):
+        xs = single(mod, c)
+        assert close(xb, xs), c["potential"]
+
+
+def test_batch_graph_matches_run(mod):
+    cases = batch_cases()
+    b1 = mod.Batch(cases)
+    r1 = [x.clone() for x in b1.run()]
+    b2 = mod.Batch(cases)
+    gr = b2.graph()
+    gr.launch()
+    torch.cuda.synchronize()
+    b2.check()
+    for x1, x2 in zip(r1, b2.x):
+        assert torch.equal(x1, x2)
+    gr.close()
