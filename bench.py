@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--cpu-subiters", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="also time N batched reconstructions (persistent launches)")
+    ap.add_argument("--batch-steps", type=int, default=25)
+    ap.add_argument("--no-tune", action="store_true")
     return ap.parse_args()
 
 
@@ -189,6 +193,7 @@ def run_ours(args):
     M = cfg.subset_num
     xa = torch.zeros(g.n_voxels, device="cuda")
     xb = torch.zeros(g.n_voxels, device="cuda")
+    tuned = None if args.no_tune else plan.autotune(xa)
     stream = torch.cuda.current_stream()
 
     def step(evs=None):
@@ -263,6 +268,8 @@ def run_ours(args):
                    "step": "1 OSTR iteration = 25 sub-iterations", "parallelism": f"replicas x{ws}",
                    "l2": "inputs larger than L2 (x, x', d: 3 x 126 MB; y, b: 2 x 138 MB)"},
         "gpu_launches": 2 * M * args.steps,
+        "tuned": None if tuned is None else {"fp_batch": tuned["fp_batch"],
+                                             "upd_planes": tuned["upd_planes"]},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / peak,
                      "traffic": traffic, "kernels": kern},
@@ -280,10 +287,93 @@ def run_ours(args):
                                "kind": "port",
                                "sample": f"{len(times)} sub-iterations of the clinical workload "
                                          f"(FP32 restatement, OpenMP), {model}"}
+    if args.batch:
+        out["batch"] = batch_bench(args, rank)
     if ws > 1:
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def batch_bench(args, rank):
+    """N independent reconstructions of uneven size and view count, advanced by
+    persistent batched launches; the same cases one after another for scale."""
+    import torch
+
+    from newrecon_gb300 import ostr, replicas
+    from newrecon_gb300.geometry import batch_configs
+    from newrecon_gb300.phantom import breast_phantom, poisson_counts
+
+    cfgs = batch_configs(args.batch, seed=replicas.case_seed(7, rank))
+    cases = []
+    for c in cfgs:
+        g = c.geom
+        x = breast_phantom(g, c.seed, 0, c.n_calc, glandular_fraction=c.n_glandular / 100.0)
+        ostr.set_geometry(g)
+        idx = np.arange(g.n_angles, dtype=np.int32)
+        line = torch.zeros(g.n_angles * g.n_bins, device="cuda")
+        ostr.fprojectCB_1R_GPU_OSTR_cos(torch.from_numpy(x.ravel()).cuda(), line,
+                                        torch.from_numpy(c.angles).cuda(),
+                                        torch.from_numpy(idx).cuda(), 0, g.n_angles)
+        y = poisson_counts(line.cpu().numpy(), c.I0, c.seed)
+        cases.append(dict(geom=g, angles=c.angles, prj=y, blank=np.full_like(y, c.I0),
+                          subset_num=c.subset_num, iter_num=c.iter_num, beta=c.beta,
+                          delta=c.delta, potential=c.potential))
+    bt = ostr.Batch(cases)
+    steps = min(args.batch_steps, bt.n_steps)
+    stream = torch.cuda.current_stream()
+    from newrecon_gb300 import native
+    tab = ctypes_ptr(bt.table)
+    for k in range(min(3, steps)):  # warm-up (advances the cases; timing only)
+        native.call("nr_batch_step", tab, k, stream_ptr())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(steps):
+        native.call("nr_batch_step", tab, k, stream_ptr())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_batch = e0.elapsed_time(e1) / 1e3
+    bt.check()
+    subits = sum(min(steps, cs["iter_num"] * cs["subset_num"]) for cs in cases)
+    # the same cases one at a time (single-reconstruction kernels), same steps
+    t_seq = 0.0
+    for p, xx in zip(bt.plans, bt.x):
+        xo = torch.empty_like(xx)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for k in range(steps):
+            s_ = k % p.params.subset_num
+            p.project(xx, s_)
+            p.update(xx, xo, s_)
+            xx, xo = xo, xx
+        a1.record(stream)
+        torch.cuda.synchronize()
+        t_seq += a0.elapsed_time(a1) / 1e3
+    full_steps = bt.n_steps
+    vox = sum(cs["geom"].n_voxels for cs in cases)
+    return {"cases": len(cases), "steps_timed": steps, "voxels_total": vox,
+            "subset_iters_per_s": subits / t_batch,
+            "projections_per_s": subits / t_batch,
+            "volumes_per_hour": len(cases) * 3600.0 / (t_batch / steps * full_steps),
+            "sequential_subset_iters_per_s": subits / t_seq,
+            "workload": "batch: thickness U(30,80), in-plane U(512,1024)xU(256,512) @0.14mm, "
+                        "9/15/25 views over +-U(7.5,25) deg, I0 U(3e3,2e4), gland U(10,50)%, "
+                        "hyperbola, 50 iterations"}
+
+
+def ctypes_ptr(t):
+    import ctypes
+
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def stream_ptr():
+    import ctypes
+
+    import torch
+
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
 def e2e_ours(args, cfg, y, b):

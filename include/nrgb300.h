@@ -145,7 +145,13 @@ typedef struct nr_ostr_params {
     int32_t has_scatter;       /* 0: r = 0 everywhere                            */
     float beta;                /* penalty weight                                 */
     float delta;               /* potential scale (1/mm), > 0 unless Q2          */
+    int32_t fp_batch;          /* Siddon steps per gather round: 2, 4, 8 (0 = 4) */
+    int32_t upd_planes;        /* z planes per update block: 8, 16, 32 (0 = 16) */
 } nr_ostr_params;
+
+/* fp_batch and upd_planes select kernel variants only (every variant gives the
+ * same result); the autotuner (newrecon_gb300/autotune.py) picks them per
+ * geometry.  The batched path uses the defaults. */
 
 /* Bytes of workspace the fused path needs for this geometry and parameters. */
 nr_status nr_ostr_workspace_size(const nr_geom* g, const nr_ostr_params* p,

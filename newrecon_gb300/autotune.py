@@ -1,0 +1,114 @@
+"""Autotuner for the fused kernels' launch variants.
+
+Two knobs, each a compile-time variant of one fused kernel (every variant
+computes the same result, bit for bit):
+
+* ``fp_batch`` -- Siddon steps walked per gather round in the forward
+  projection (2, 4, 8): more steps keep more volume gathers in flight but use
+  more registers (fewer resident warps);
+* ``upd_planes`` -- z planes walked per block by the fused update (8, 16, 32):
+  deeper slabs amortise the halo planes, shallower ones give more blocks.
+
+The tuner times each variant on the plan's own geometry (CUDA events on the
+launching stream, best of a few repetitions over all subsets) and keeps the
+fastest of each knob.  Results are cached in a JSON file keyed by GPU name,
+geometry and the parameters that change the work, at
+``$NR_TUNE_CACHE`` or ``~/.cache/newrecon_gb300/tune.json``.
+"""
+from __future__ import annotations
+
+import json
+import os
+from typing import Dict, Optional, Tuple
+
+import torch
+
+FP_BATCHES = (2, 4, 8)
+UPD_PLANES = (8, 16, 32)
+
+
+def cache_path() -> str:
+    return os.environ.get("NR_TUNE_CACHE") or os.path.join(
+        os.path.expanduser("~"), ".cache", "newrecon_gb300", "tune.json")
+
+
+def signature(plan) -> str:
+    g = plan.geom
+    p = plan.params
+    dev = torch.cuda.get_device_name(plan.ws.device)
+    return (f"{dev}|{g.nx}x{g.ny}x{g.nz}|{g.nbx}x{g.nby}|A{g.n_angles}|M{p.subset_num}"
+            f"|pot{p.potential}|scat{p.has_scatter}")
+
+
+def _load() -> Dict[str, dict]:
+    try:
+        with open(cache_path()) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(key: str, val: dict) -> None:
+    path = cache_path()
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        data = _load()
+        data[key] = val
+        tmp = path + f".{os.getpid()}.tmp"
+        with open(tmp, "w") as f:
+            json.dump(data, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+    except OSError:
+        pass  # a read-only home: tune again next time
+
+
+def _time(fn, reps: int) -> float:
+    stream = torch.cuda.current_stream()
+    best = float("inf")
+    for _ in range(reps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        best = min(best, a.elapsed_time(b))
+    return best
+
+
+def tune(plan, x: Optional[torch.Tensor] = None, reps: int = 3,
+         use_cache: bool = True) -> Tuple[int, int, dict]:
+    """Picks (fp_batch, upd_planes) for a set-up plan and applies them."""
+    key = signature(plan)
+    if use_cache:
+        hit = _load().get(key)
+        if hit and hit.get("fp_batch") in FP_BATCHES and hit.get("upd_planes") in UPD_PLANES:
+            plan.params.fp_batch = int(hit["fp_batch"])
+            plan.params.upd_planes = int(hit["upd_planes"])
+            return plan.params.fp_batch, plan.params.upd_planes, hit
+    if x is None:
+        x = torch.zeros(plan.geom.n_voxels, dtype=torch.float32, device=plan.ws.device)
+    xo = torch.empty_like(x)
+    M = plan.params.subset_num
+    saved = (plan.params.fp_batch, plan.params.upd_planes)
+    fp_ms, up_ms = {}, {}
+    for k in FP_BATCHES:
+        plan.params.fp_batch = k
+        plan.project(x, 0)  # warm-up
+        fp_ms[k] = _time(lambda: [plan.project(x, a) for a in range(M)], reps)
+    plan.params.fp_batch = saved[0]
+    plan.project(x, 0)  # h of subset 0 for the update timings
+    for z in UPD_PLANES:
+        plan.params.upd_planes = z
+        plan.update(x, xo, 0)
+        up_ms[z] = _time(lambda: [plan.update(x, xo, 0) for _ in range(M)], reps)
+    best_k = min(fp_ms, key=fp_ms.get)
+    best_z = min(up_ms, key=up_ms.get)
+    plan.params.fp_batch = best_k
+    plan.params.upd_planes = best_z
+    rec = {"fp_batch": best_k, "upd_planes": best_z,
+           "fp_ms": {str(k): v for k, v in fp_ms.items()},
+           "update_ms": {str(k): v for k, v in up_ms.items()}}
+    if use_cache:
+        _store(key, rec)
+    return best_k, best_z, rec

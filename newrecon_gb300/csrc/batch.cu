@@ -38,6 +38,7 @@ struct BatchHdr {
     int n;
     int64_t fp_total, up_total;
     int64_t fp_off[BATCH_MAX + 1], up_off[BATCH_MAX + 1];
+    int64_t pot_lo[4], pot_hi[4];  // update items of each potential (cases sorted by potential)
 };
 
 constexpr size_t HDR_BYTES = (sizeof(BatchHdr) + 255) & ~(size_t)255;
@@ -46,6 +47,15 @@ __device__ __forceinline__ int find_case(const int64_t* off, int n, int64_t it) 
     int c = 0;
     while (c + 1 < n && it >= off[c + 1]) c++;
     return c;
+}
+
+// All threads copy case c's descriptor into shared memory (word by word).
+__device__ __forceinline__ void load_case(CaseDev& dst, const CaseDev* C, int c, int tid,
+                                          int nthreads) {
+    static_assert(sizeof(CaseDev) % 4 == 0, "word copy");
+    const int* src = (const int*)(C + c);
+    int* d = (int*)&dst;
+    for (int k = tid; k < (int)(sizeof(CaseDev) / 4); k += nthreads) d[k] = src[k];
 }
 
 __global__ void __launch_bounds__(128) fp_batch_kernel(const void* __restrict__ table, int step) {
@@ -57,7 +67,7 @@ __global__ void __launch_bounds__(128) fp_batch_kernel(const void* __restrict__ 
     for (int64_t it = blockIdx.x; it < H->fp_total; it += gridDim.x) {
         const int c = find_case(H->fp_off, H->n, it);
         __syncthreads();  // previous item's readers of cd / src are done
-        if (tid == 0) cd = C[c];
+        load_case(cd, C, c, tid, 128);
         __syncthreads();
         if (step >= cd.total_sub) continue;
         const int64_t local = it - H->fp_off[c];
@@ -70,17 +80,18 @@ __global__ void __launch_bounds__(128) fp_batch_kernel(const void* __restrict__ 
     }
 }
 
-__global__ void __launch_bounds__(256, 4) update_batch_kernel(const void* __restrict__ table,
+template <int POT>
+__global__ void __launch_bounds__(256, 5) update_batch_kernel(const void* __restrict__ table,
                                                            int step) {
     __shared__ CaseDev cd;
     __shared__ UpdSmem sm;
     const BatchHdr* H = (const BatchHdr*)table;
     const CaseDev* C = (const CaseDev*)((const char*)table + HDR_BYTES);
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    for (int64_t it = blockIdx.x; it < H->up_total; it += gridDim.x) {
+    for (int64_t it = H->pot_lo[POT] + blockIdx.x; it < H->pot_hi[POT]; it += gridDim.x) {
         const int c = find_case(H->up_off, H->n, it);
         __syncthreads();
-        if (tid == 0) cd = C[c];
+        load_case(cd, C, c, tid, 256);
         __syncthreads();
         if (step >= cd.total_sub) continue;
         const int64_t local = it - H->up_off[c];
@@ -90,25 +101,8 @@ __global__ void __launch_bounds__(256, 4) update_batch_kernel(const void* __rest
         const int a0 = (step % (int)cd.M) * cd.Vs;
         const float* cur = (step & 1) ? cd.xtmp : cd.x;
         float* nxt = (step & 1) ? cd.x : cd.xtmp;
-        switch (cd.pot) {
-        case NR_POT_Q2:
-            update_tile<NR_POT_Q2>(cd.G, cd.W, cur, nxt, cd.d, cd.h, cd.angles, cd.index, a0,
-                                   cd.Vs, cd.M, cd.beta, cd.delta, cd.status, bx, by, bz, sm);
-            break;
-        case NR_POT_LANGE:
-            update_tile<NR_POT_LANGE>(cd.G, cd.W, cur, nxt, cd.d, cd.h, cd.angles, cd.index, a0,
-                                      cd.Vs, cd.M, cd.beta, cd.delta, cd.status, bx, by, bz, sm);
-            break;
-        case NR_POT_HYPERBOLA:
-            update_tile<NR_POT_HYPERBOLA>(cd.G, cd.W, cur, nxt, cd.d, cd.h, cd.angles, cd.index,
-                                          a0, cd.Vs, cd.M, cd.beta, cd.delta, cd.status, bx, by,
-                                          bz, sm);
-            break;
-        default:
-            update_tile<NR_POT_HUBER>(cd.G, cd.W, cur, nxt, cd.d, cd.h, cd.angles, cd.index, a0,
-                                      cd.Vs, cd.M, cd.beta, cd.delta, cd.status, bx, by, bz, sm);
-            break;
-        }
+        update_tile<POT>(cd.G, cd.W, cur, nxt, cd.d, cd.h, cd.angles, cd.index, a0, cd.Vs, cd.M,
+                         cd.beta, cd.delta, cd.status, bx, by, bz, sm);
     }
 }
 
@@ -164,8 +158,18 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
     CaseDev* C = (CaseDev*)(img + HDR_BYTES);
     H->n = n_cases;
     int steps = 0;
+    // cases ordered by potential, so each potential's update items are one range
+    int order[BATCH_MAX];
+    int no = 0;
+    for (int pot = NR_POT_Q2; pot <= NR_POT_HUBER; pot++)
+        for (int c = 0; c < n_cases; c++)
+            if (cases[c].p.potential == pot) order[no++] = c;
+    if (no != n_cases) {
+        delete[] img;
+        return NR_ERR_BAD_ARGUMENT;  // unknown potential
+    }
     for (int c = 0; c < n_cases; c++) {
-        const nr_batch_case& k = cases[c];
+        const nr_batch_case& k = cases[order[c]];
         CaseDev& d = C[c];
         if (k.n_iters < 0 || !k.x) {
             delete[] img;
@@ -198,6 +202,16 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
     }
     H->fp_total = H->fp_off[n_cases];
     H->up_total = H->up_off[n_cases];
+    for (int pot = 0; pot < 4; pot++) {
+        H->pot_lo[pot] = H->up_total;
+        H->pot_hi[pot] = H->up_total;
+    }
+    for (int c = n_cases - 1; c >= 0; c--) {
+        const int pot = C[c].pot;
+        H->pot_lo[pot] = H->up_off[c];
+        if (H->pot_hi[pot] == H->up_total && (c == n_cases - 1 || C[c + 1].pot != pot))
+            H->pot_hi[pot] = H->up_off[c + 1];
+    }
     const cudaError_t e =
         cudaMemcpyAsync(table, img, need, cudaMemcpyHostToDevice, as_stream(stream));
     const cudaError_t e2 = cudaStreamSynchronize(as_stream(stream));  // img is pageable
@@ -207,12 +221,21 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
     return NR_OK;
 }
 
+// One step: the projection of all cases, then one update launch per potential
+// (each walks its own item range; a potential no case uses has an empty range).
 static nr_status enqueue_steps(const void* table, int32_t first, int32_t count, cudaStream_t s) {
     const int fp_blocks = persistent_blocks((const void*)fp_batch_kernel, 128, 0);
-    const int up_blocks = persistent_blocks((const void*)update_batch_kernel, 256, 0);
+    const int ub0 = persistent_blocks((const void*)update_batch_kernel<NR_POT_Q2>, 256, 0);
+    const int ub1 = persistent_blocks((const void*)update_batch_kernel<NR_POT_LANGE>, 256, 0);
+    const int ub2 = persistent_blocks((const void*)update_batch_kernel<NR_POT_HYPERBOLA>, 256, 0);
+    const int ub3 = persistent_blocks((const void*)update_batch_kernel<NR_POT_HUBER>, 256, 0);
+    const dim3 ut(UTX, UTY);
     for (int32_t k = first; k < first + count; k++) {
         fp_batch_kernel<<<fp_blocks, dim3(32, 4), 0, s>>>(table, k);
-        update_batch_kernel<<<up_blocks, dim3(UTX, UTY), 0, s>>>(table, k);
+        update_batch_kernel<NR_POT_Q2><<<ub0, ut, 0, s>>>(table, k);
+        update_batch_kernel<NR_POT_LANGE><<<ub1, ut, 0, s>>>(table, k);
+        update_batch_kernel<NR_POT_HYPERBOLA><<<ub2, ut, 0, s>>>(table, k);
+        update_batch_kernel<NR_POT_HUBER><<<ub3, ut, 0, s>>>(table, k);
     }
     return launch_status();
 }

@@ -34,7 +34,9 @@ __global__ void __launch_bounds__(128) fp_kernel(const __grid_constant__ Geo G,
     }
 }
 
-// Fused forward projection + h, one block per 32 x 4 bins of one subset view.
+// Fused forward projection + h, one block per 32 x 4 bins of one subset view;
+// K Siddon steps per gather round.
+template <int K>
 __global__ void __launch_bounds__(128) fp_h_kernel(const __grid_constant__ Geo G,
                                                    const float* __restrict__ vol,
                                                    float* __restrict__ h,
@@ -44,7 +46,7 @@ __global__ void __launch_bounds__(128) fp_h_kernel(const __grid_constant__ Geo G
                                                    const float* __restrict__ b,
                                                    const float* __restrict__ r) {
     __shared__ ViewSrc src;
-    fp_h_tile(G, vol, h, angles, index, a0, y, b, r, blockIdx.x, blockIdx.y, blockIdx.z, src);
+    fp_h_tile<K>(G, vol, h, angles, index, a0, y, b, r, blockIdx.x, blockIdx.y, blockIdx.z, src);
 }
 
 // gamma * yry for every view in one pass (the d precompute's detector term,
@@ -122,11 +124,17 @@ NR_API nr_status nr_fp_gamma(const nr_geom* g, float* gamma, const float* angles
 // Internal launchers used by the device-resident path (ostr.cu).
 namespace nr {
 
-nr_status launch_fp_h(const nr_geom& g, const float* x, float* h, const float* angles,
+nr_status launch_fp_h(const nr_geom& g, int k, const float* x, float* h, const float* angles,
                       const int32_t* index, int a0, int nviews, const float* y, const float* b,
                       const float* r, cudaStream_t st) {
     dim3 blk(32, 4), grd(cdiv(g.nbx, 32), cdiv(g.nby, 4), nviews);
-    fp_h_kernel<<<grd, blk, 0, st>>>(make_geo(g), x, h, angles, index, a0, y, b, r);
+    const Geo G = make_geo(g);
+    if (k == 2)
+        fp_h_kernel<2><<<grd, blk, 0, st>>>(G, x, h, angles, index, a0, y, b, r);
+    else if (k == 8)
+        fp_h_kernel<8><<<grd, blk, 0, st>>>(G, x, h, angles, index, a0, y, b, r);
+    else
+        fp_h_kernel<4><<<grd, blk, 0, st>>>(G, x, h, angles, index, a0, y, b, r);
     return launch_status();
 }
 

@@ -17,16 +17,17 @@
 
 namespace nr {
 
-nr_status launch_fp_h(const nr_geom& g, const float* x, float* h, const float* angles,
+nr_status launch_fp_h(const nr_geom& g, int k, const float* x, float* h, const float* angles,
                       const int32_t* index, int a0, int nviews, const float* y, const float* b,
                       const float* r, cudaStream_t st);
 nr_status launch_gamma_yry(const nr_geom& g, int gamma_mode, float* out, const float* angles,
                            const float* y, const float* r, cudaStream_t st);
 nr_status launch_bp(const nr_geom& g, bool ji, float* vol, const float* prj, const float* angles,
                     const int32_t* index, int a0, int nv, cudaStream_t st);
-nr_status launch_update(const nr_geom& g, int pot, const float* x, float* x_out, const float* d,
-                        const float* h, const float* angles, const int32_t* index, int a0, int nv,
-                        float M, float beta, float delta, int* status, cudaStream_t st);
+nr_status launch_update(const nr_geom& g, int pot, int zc, const float* x, float* x_out,
+                        const float* d, const float* h, const float* angles, const int32_t* index,
+                        int a0, int nv, float M, float beta, float delta, int* status,
+                        cudaStream_t st);
 nr_status launch_transpose(float* out, const float* in, int rows, int cols, int nviews, int M,
                            int Vs, cudaStream_t st);
 nr_status launch_objective(const nr_geom& g, int pot, float delta, const float* x,
@@ -108,6 +109,10 @@ static nr_status check_params(const nr_geom* g, const nr_ostr_params* p) {
         return NR_ERR_BAD_ARGUMENT;
     if (!(p->beta >= 0.f)) return NR_ERR_BAD_ARGUMENT;
     if (g->n_angles / p->subset_num > 32) return NR_ERR_BAD_ARGUMENT;  // views per subset in smem
+    if (p->fp_batch != 0 && p->fp_batch != 2 && p->fp_batch != 4 && p->fp_batch != 8)
+        return NR_ERR_BAD_ARGUMENT;
+    if (p->upd_planes != 0 && p->upd_planes != 8 && p->upd_planes != 16 && p->upd_planes != 32)
+        return NR_ERR_BAD_ARGUMENT;
     if (g->ny > 65535 || g->nz > 65535 || g->n_angles > 65535) return NR_ERR_BAD_GEOMETRY;
     return NR_OK;
 }
@@ -216,7 +221,7 @@ NR_API nr_status nr_ostr_project(const nr_geom* g, const nr_ostr_params* p, cons
     if (!x || subset < 0 || subset >= p->subset_num) return NR_ERR_BAD_ARGUMENT;
     WS w = carve(workspace, L);
     const int Vs = g->n_angles / p->subset_num;
-    return launch_fp_h(*g, x, w.h, w.angles, w.index, subset * Vs, Vs, w.y, w.b, w.r,
+    return launch_fp_h(*g, p->fp_batch, x, w.h, w.angles, w.index, subset * Vs, Vs, w.y, w.b, w.r,
                        as_stream(stream));
 }
 
@@ -230,7 +235,7 @@ NR_API nr_status nr_ostr_update(const nr_geom* g, const nr_ostr_params* p, const
         return NR_ERR_BAD_ARGUMENT;
     WS w = carve(workspace, L);
     const int M = p->subset_num, Vs = g->n_angles / M;
-    return launch_update(*g, p->potential, x, x_out, w.d, w.h, w.angles, w.index, subset * Vs, Vs,
+    return launch_update(*g, p->potential, p->upd_planes, x, x_out, w.d, w.h, w.angles, w.index, subset * Vs, Vs,
                          (float)M, p->beta, p->delta, w.status, as_stream(stream));
 }
 
@@ -266,9 +271,9 @@ NR_API nr_status nr_ostr_subiter(const nr_geom* g, const nr_ostr_params* p, floa
     const int A = g->n_angles, M = p->subset_num, Vs = A / M;
     const int64_t N = (int64_t)g->nx * g->ny * g->nz;
     const int a0 = subset * Vs;
-    if ((st = launch_fp_h(*g, x, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, s)) != NR_OK)
+    if ((st = launch_fp_h(*g, p->fp_batch, x, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, s)) != NR_OK)
         return st;
-    if ((st = launch_update(*g, p->potential, x, w.xtmp, w.d, w.h, w.angles, w.index, a0, Vs,
+    if ((st = launch_update(*g, p->potential, p->upd_planes, x, w.xtmp, w.d, w.h, w.angles, w.index, a0, Vs,
                             (float)M, p->beta, p->delta, w.status, s)) != NR_OK)
         return st;
     if (cudaMemcpyAsync(x, w.xtmp, N * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
@@ -287,10 +292,10 @@ static nr_status enqueue_iterations(const nr_geom* g, const nr_ostr_params* p, f
     for (int it = 0; it < n_iters; it++) {
         for (int a = 0; a < M; a++) {
             const int a0 = a * Vs;
-            if ((st = launch_fp_h(*g, cur, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, s)) !=
+            if ((st = launch_fp_h(*g, p->fp_batch, cur, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, s)) !=
                 NR_OK)
                 return st;
-            if ((st = launch_update(*g, p->potential, cur, nxt, w.d, w.h, w.angles, w.index, a0, Vs,
+            if ((st = launch_update(*g, p->potential, p->upd_planes, cur, nxt, w.d, w.h, w.angles, w.index, a0, Vs,
                                     (float)M, p->beta, p->delta, w.status, s)) != NR_OK)
                 return st;
             float* t = cur;

@@ -120,34 +120,53 @@ nr_status launch_prior(const nr_geom& g, int pot, float* RDD, float* RD, const f
     }
 }
 
-template <int POT>
+template <int POT, int ZC>
 static nr_status launch_update_t(const nr_geom& g, const float* x, float* x_out, const float* d,
                                  const float* h, const float* angles, const int32_t* index,
                                  int a0, int nv, float M, float beta, float delta, int* status,
                                  cudaStream_t st) {
-    dim3 blk(UTX, UTY), grd(cdiv(g.nx, UTX), cdiv(g.ny, UTY), cdiv(g.nz, UZC));
-    update_kernel<POT><<<grd, blk, 0, st>>>(make_geo(g), make_w5(g.vz / g.vx, delta), x,
-                                            x_out, d, h, angles, index, a0, nv, M, beta, delta,
-                                            status);
+    dim3 blk(UTX, UTY), grd(cdiv(g.nx, UTX), cdiv(g.ny, UTY), cdiv(g.nz, ZC));
+    update_kernel<POT, ZC><<<grd, blk, 0, st>>>(make_geo(g), make_w5(g.vz / g.vx, delta), x,
+                                                x_out, d, h, angles, index, a0, nv, M, beta, delta,
+                                                status);
     return launch_status();
 }
 
-nr_status launch_update(const nr_geom& g, int pot, const float* x, float* x_out, const float* d,
-                        const float* h, const float* angles, const int32_t* index, int a0, int nv,
-                        float M, float beta, float delta, int* status, cudaStream_t st) {
+template <int POT>
+static nr_status launch_update_z(const nr_geom& g, int zc, const float* x, float* x_out,
+                                 const float* d, const float* h, const float* angles,
+                                 const int32_t* index, int a0, int nv, float M, float beta,
+                                 float delta, int* status, cudaStream_t st) {
+    switch (zc) {
+    case 8:
+        return launch_update_t<POT, 8>(g, x, x_out, d, h, angles, index, a0, nv, M, beta, delta,
+                                       status, st);
+    case 32:
+        return launch_update_t<POT, 32>(g, x, x_out, d, h, angles, index, a0, nv, M, beta, delta,
+                                        status, st);
+    default:
+        return launch_update_t<POT, 16>(g, x, x_out, d, h, angles, index, a0, nv, M, beta, delta,
+                                        status, st);
+    }
+}
+
+nr_status launch_update(const nr_geom& g, int pot, int zc, const float* x, float* x_out,
+                        const float* d, const float* h, const float* angles, const int32_t* index,
+                        int a0, int nv, float M, float beta, float delta, int* status,
+                        cudaStream_t st) {
     if (nv > UPD_VIEWS_SMEM) return NR_ERR_BAD_ARGUMENT;
     switch (pot) {
     case NR_POT_Q2:
-        return launch_update_t<NR_POT_Q2>(g, x, x_out, d, h, angles, index, a0, nv, M, beta, delta,
-                                          status, st);
+        return launch_update_z<NR_POT_Q2>(g, zc, x, x_out, d, h, angles, index, a0, nv, M, beta,
+                                          delta, status, st);
     case NR_POT_LANGE:
-        return launch_update_t<NR_POT_LANGE>(g, x, x_out, d, h, angles, index, a0, nv, M, beta,
+        return launch_update_z<NR_POT_LANGE>(g, zc, x, x_out, d, h, angles, index, a0, nv, M, beta,
                                              delta, status, st);
     case NR_POT_HYPERBOLA:
-        return launch_update_t<NR_POT_HYPERBOLA>(g, x, x_out, d, h, angles, index, a0, nv, M, beta,
-                                                 delta, status, st);
+        return launch_update_z<NR_POT_HYPERBOLA>(g, zc, x, x_out, d, h, angles, index, a0, nv, M,
+                                                 beta, delta, status, st);
     case NR_POT_HUBER:
-        return launch_update_t<NR_POT_HUBER>(g, x, x_out, d, h, angles, index, a0, nv, M, beta,
+        return launch_update_z<NR_POT_HUBER>(g, zc, x, x_out, d, h, angles, index, a0, nv, M, beta,
                                              delta, status, st);
     default: return NR_ERR_BAD_ARGUMENT;
     }

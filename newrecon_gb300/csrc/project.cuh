@@ -23,6 +23,7 @@ __device__ __forceinline__ int64_t bin_off(const nr_geom& g, int i, int j) {
 // Tomo_OSTR_gold.cpp:245-260.
 // One block of 32 x 4 bins (bx, by) of subset view bz.  Every thread of the
 // block must call it (it synchronises once).
+template <int K = 4>
 __device__ __forceinline__ void fp_h_tile(const Geo& G, const float* __restrict__ vol,
                                           float* __restrict__ h, const float* __restrict__ angles,
                                           const int32_t* __restrict__ index, int a0,
@@ -38,7 +39,7 @@ __device__ __forceinline__ void fp_h_tile(const Geo& G, const float* __restrict_
     if (i >= g.nbx || j >= g.nby) return;
     float v = 0.f;
     float l = 0.f;
-    if (trace<0>(G, vol, src.x0, src.y0, src.z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v))
+    if (trace<0, K>(G, vol, src.x0, src.y0, src.z0, bin_x(g, i), bin_y(g, j), -g.detectorR, &v))
         l = v * src.ct;
     const int64_t B = (int64_t)g.nbx * g.nby;
     const int64_t o = (int64_t)a * B + bin_off<true>(g, i, j);

@@ -131,7 +131,7 @@ struct UpdSmem {
 // shared-memory load at a fixed offset.  The global loads of plane z+2 are
 // issued before plane z is computed (register prefetch), so they overlap the
 // arithmetic.  Writes x_out; flags non-finite values.
-template <int POT>
+template <int POT, int ZC = UZC>
 __device__ __forceinline__ void update_tile(
     const Geo& G, const PriorW5& W, const float* __restrict__ x, float* __restrict__ x_out,
     const float* __restrict__ d, const float* __restrict__ h, const float* __restrict__ angles,
@@ -143,7 +143,7 @@ __device__ __forceinline__ void update_tile(
     const int tid = threadIdx.y * UTX + threadIdx.x;
     for (int t = tid; t < nv; t += UTX * UTY) sv[t] = view_source(g, angles[index[a0 + t]]);
     const int x0t = bx * UTX, y0t = by * UTY;
-    const int zb = bz * UZC, ze = min(zb + UZC, g.nz);
+    const int zb = bz * ZC, ze = min(zb + ZC, g.nz);
     const int64_t plane = (int64_t)g.nx * g.ny;
     // This thread's (at most two) cells of a halo plane tile.
     constexpr int NT = UTX * UTY;
@@ -250,8 +250,8 @@ __device__ __forceinline__ void update_tile(
     }
 }
 
-// One block per (x, y) tile and z chunk.
-template <int POT>
+// One block per (x, y) tile and chunk of ZC planes.
+template <int POT, int ZC>
 __global__ void __launch_bounds__(256) update_kernel(
     const __grid_constant__ Geo G, const __grid_constant__ PriorW5 W,
     const float* __restrict__ x, float* __restrict__ x_out, const float* __restrict__ d,
@@ -259,8 +259,8 @@ __global__ void __launch_bounds__(256) update_kernel(
     const int32_t* __restrict__ index, int a0, int nv, float M, float beta, float delta,
     int* __restrict__ status) {
     __shared__ UpdSmem sm;
-    update_tile<POT>(G, W, x, x_out, d, h, angles, index, a0, nv, M, beta, delta, status,
-                     blockIdx.x, blockIdx.y, blockIdx.z, sm);
+    update_tile<POT, ZC>(G, W, x, x_out, d, h, angles, index, a0, nv, M, beta, delta, status,
+                         blockIdx.x, blockIdx.y, blockIdx.z, sm);
 }
 
 }  // namespace nr

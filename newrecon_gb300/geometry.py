@@ -43,6 +43,7 @@ class NrOstrParams(ctypes.Structure):
         ("subset_num", ctypes.c_int32), ("potential", ctypes.c_int32),
         ("gamma_mode", ctypes.c_int32), ("has_scatter", ctypes.c_int32),
         ("beta", ctypes.c_float), ("delta", ctypes.c_float),
+        ("fp_batch", ctypes.c_int32), ("upd_planes", ctypes.c_int32),
     ]
 
 

@@ -425,6 +425,13 @@ class OSTR:
         off = int(ptr.value) - self.ws.data_ptr()
         return self.ws[off:off + int(nb.value)].view(dt)
 
+    def autotune(self, x: Optional[torch.Tensor] = None, use_cache: bool = True) -> dict:
+        """Picks the fused kernels' variants for this geometry (newrecon_gb300.autotune)."""
+        from . import autotune
+
+        k, z, rec = autotune.tune(self, x, use_cache=use_cache)
+        return rec
+
     def graph(self, x: torch.Tensor, n_iters: int) -> "OstrGraph":
         """n_iters iterations on x captured once as a CUDA graph; replay with .launch()."""
         return OstrGraph(self, x, n_iters)

@@ -119,3 +119,37 @@ def test_batch_graph_matches_run(mod):
     for x1, x2 in zip(r1, b2.x):
         assert torch.equal(x1, x2)
     gr.close()
+
+
+def test_autotune_variants_agree_and_cache(mod, tmp_path, monkeypatch):
+    """Every kernel variant computes the same sub-iteration; the tuner caches."""
+    import json
+
+    from newrecon_gb300 import autotune
+
+    monkeypatch.setenv("NR_TUNE_CACHE", str(tmp_path / "tune.json"))
+    cfg, y, b = small_scan()
+    plan = mod.OSTR(cfg.geom, subset_num=cfg.subset_num, beta=cfg.beta, delta=cfg.delta,
+                    potential=cfg.potential)
+    plan.setup(cfg.angles, y, b)
+    x = torch.zeros(cfg.geom.n_voxels, device="cuda")
+    plan.iterate(x, 1)
+    outs = []
+    for k in autotune.FP_BATCHES:
+        for zc in autotune.UPD_PLANES:
+            plan.params.fp_batch, plan.params.upd_planes = k, zc
+            xo = torch.empty_like(x)
+            plan.project(x, 3)
+            plan.update(x, xo, 3)
+            outs.append(xo)
+    torch.cuda.synchronize()
+    for o in outs[1:]:
+        assert torch.equal(o, outs[0])
+    rec = plan.autotune(x)
+    assert plan.params.fp_batch in autotune.FP_BATCHES
+    assert plan.params.upd_planes in autotune.UPD_PLANES
+    data = json.load(open(tmp_path / "tune.json"))
+    assert autotune.signature(plan) in data
+    plan.params.fp_batch = plan.params.upd_planes = 0
+    rec2 = plan.autotune(x)  # served from the cache
+    assert (plan.params.fp_batch, plan.params.upd_planes) == (rec["fp_batch"], rec["upd_planes"])
