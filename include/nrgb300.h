@@ -247,6 +247,47 @@ nr_status nr_batch_finish(const void* table, void* stream);
  * non-default stream. */
 nr_status nr_batch_graph_create(const void* table, int32_t n_steps, void* stream, void** graph);
 
+/* ---------------------------------------------------------------------------
+ * Learned warm start (no reference counterpart; the nearest is the Keras 3D
+ * U-Net post-processor of recon1.ipynb:211).  A 3D residual CNN of six
+ * 3x3x3 convolutions (1 -> 32 -> 32 -> 32 -> 32 -> 32 -> 1 channels, ReLU)
+ * maps an early OSTR iterate x to x_warm = max(0, x + f(s x) / s), with BF16
+ * weights and activations on the tensor cores and FP32 accumulation.  Volumes
+ * are nb patches of nx x ny x nz voxels stored back to back ([b][z][y][x]);
+ * each patch is zero-padded at its own borders.  Parameters are one FP32
+ * array: for each layer W[27][out][in] (tap = (dz+1)*9 + (dy+1)*3 + (dx+1))
+ * then b[out].
+ * ------------------------------------------------------------------------- */
+typedef struct nr_cnn_dims {
+    int32_t nx, ny, nz, nb;
+} nr_cnn_dims;
+
+/* Number of FP32 parameters. */
+nr_status nr_cnn_param_count(int64_t* n);
+/* Workspace bytes for inference (training = 0) or training (training = 1). */
+nr_status nr_cnn_workspace_size(const nr_cnn_dims* d, int32_t training, size_t* bytes);
+/* x_out = max(0, x + f(s x)/s); s = in_scale > 0. */
+nr_status nr_cnn_forward(const nr_cnn_dims* d, const float* params, const float* x,
+                         float in_scale, float* x_out, void* workspace, size_t ws_bytes,
+                         void* stream);
+/* Loss L = mean((f(s x) - s (target - x))^2) into *loss (device double) and
+ * its parameter gradient into grad (device, param_count floats; NULL keeps it
+ * in the workspace).  Training workspace. */
+nr_status nr_cnn_loss_grad(const nr_cnn_dims* d, const float* params, const float* x,
+                           const float* target, float in_scale, float* grad, double* loss,
+                           void* workspace, size_t ws_bytes, void* stream);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8, bias-corrected; step >= 1). */
+nr_status nr_cnn_adam(float* params, float* m, float* v, const float* grad, int64_t n,
+                      int32_t step, float lr, void* stream);
+/* nr_cnn_loss_grad then nr_cnn_adam with the workspace's gradient. */
+nr_status nr_cnn_train_step(const nr_cnn_dims* d, float* params, float* adam_m, float* adam_v,
+                            int32_t step, float lr, const float* x, const float* target,
+                            float in_scale, double* loss, void* workspace, size_t ws_bytes,
+                            void* stream);
+/* Reads and clears the CNN workspace's status word (bounded tensor-core waits
+ * that expired report NR_ERR_TIMEOUT).  Synchronises the stream. */
+nr_status nr_cnn_check(void* workspace, int32_t* flags, void* stream);
+
 /* Penalized-likelihood objective in FP64 (no reference counterpart; the
  * reference has no objective):
  *   out[0] = sum_i (ybar_i + r_i - y_i log(ybar_i + r_i)),  ybar = b exp(-FP_cos(x))

@@ -1,0 +1,782 @@
+// cnn.cu -- the learned warm start: a 3D residual CNN (6 conv 3x3x3 layers,
+// 32 channels, ReLU) in BF16 on the tensor cores (tcgen05, FP32 accumulate in
+// TMEM), with its backward pass and Adam.
+//
+// Network, in scaled units u = s * x (s = in_scale):
+//     a1 = relu(conv1(u)), a_l = relu(conv_l(a_{l-1})) l = 2..5, f = conv6(a5)
+//     prediction  x_warm = x + f / s          (residual on the input volume)
+// Activations are channels-last BF16 [voxel][32]; a batch of nb patches is
+// stacked along z with zero padding at every patch boundary.
+//
+// Convolution = implicit GEMM.  An output tile is one run of 128 consecutive x
+// of a (patch, z, y) row (M = 128), N = output channels, K = 27 taps x input
+// channels.  For 32-channel inputs the tile stages, per (dz, dy), one strip of
+// 130 input rows (x0-1 .. x0+128, zero outside the volume) in shared memory in
+// the K-major core-matrix layout with rows 16 bytes apart; the three dx taps
+// are the same strip read from row offsets 0, 1, 2 (descriptor start + 16 B),
+// so each input row is staged 9 times per tile instead of 27.  Weights of all
+// 27 taps stay in shared memory.  One thread issues the MMAs (2 per tap,
+// K = 16 each); strips are triple-buffered and released by tcgen05.commit.
+// 1-channel inputs gather the 27 neighbours into one K = 32 row instead.
+// Weight gradients run on the CUDA cores (per-tap outer products with a
+// fixed-order reduction).
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+#include "tc.cuh"
+
+namespace nr {
+namespace cnn {
+
+constexpr int C = 32;                 // hidden channels
+constexpr int TM = 128;               // output voxels per tile
+constexpr int SROWS = TM + 2;         // strip rows incl. the x halo
+constexpr int KCH = 4;                // 16-byte K chunks per 32-channel row
+constexpr int STRIP = KCH * SROWS * 16;  // 8320 bytes
+constexpr int NSTAGE = 3;
+constexpr int WAIT_LIMIT = 1 << 24;   // polls before a wait gives up
+
+enum { EPI_RELU = 0, EPI_MASK = 1, EPI_RESID = 2 };
+
+struct Dims {
+    int nx, ny, nz, nb;
+};
+
+__host__ __device__ inline int64_t nvox(const Dims& d) { return (int64_t)d.nx * d.ny * d.nz * d.nb; }
+__host__ __device__ inline int xtiles(const Dims& d) { return (d.nx + TM - 1) / TM; }
+__host__ __device__ inline int64_t ntiles(const Dims& d) {
+    return (int64_t)d.ny * d.nz * d.nb * xtiles(d);
+}
+
+// Packed BF16 B operand of one tap: N rows (output channels) x 32 K in core
+// matrices [N/8][4][8 rows][16 B]: SBO = 512 B between row groups, LBO = 128 B.
+__host__ __device__ inline int bpk_index(int n, int k) {
+    return (n >> 3) * 256 + (k >> 3) * 64 + (n & 7) * 8 + (k & 7);
+}
+
+// Epilogue of one output row: 32 accumulator columns -> output voxel v.
+template <int EPI>
+__device__ __forceinline__ void epilogue(const uint32_t* acc, int64_t v, const float* __restrict__ bias,
+                                         void* out, const __nv_bfloat16* __restrict__ mask) {
+    if (EPI == EPI_RESID) {
+        ((float*)out)[v] = __uint_as_float(acc[0]) + bias[0];
+        return;
+    }
+    __align__(16) __nv_bfloat16 o[C];
+    if (EPI == EPI_RELU) {
+#pragma unroll
+        for (int c = 0; c < C; c++)
+            o[c] = __float2bfloat16(fmaxf(__uint_as_float(acc[c]) + bias[c], 0.f));
+    } else {
+        __align__(16) __nv_bfloat16 m[C];
+        const uint4* mp = (const uint4*)(mask + v * C);
+#pragma unroll
+        for (int q = 0; q < 4; q++) ((uint4*)m)[q] = __ldg(mp + q);
+#pragma unroll
+        for (int c = 0; c < C; c++)
+            o[c] = __bfloat162float(m[c]) > 0.f ? __float2bfloat16(__uint_as_float(acc[c]))
+                                                : __float2bfloat16(0.f);
+    }
+    uint4* op = (uint4*)((__nv_bfloat16*)out + v * C);
+#pragma unroll
+    for (int q = 0; q < 4; q++) op[q] = ((const uint4*)o)[q];
+}
+
+// Row (patch b, z, y) of tile t and its first x.
+__device__ __forceinline__ void tile_pos(const Dims& d, int64_t t, int& b, int& z, int& y, int& x0) {
+    const int xt = xtiles(d);
+    int64_t row = t / xt;
+    x0 = (int)(t - row * xt) * TM;
+    y = (int)(row % d.ny);
+    row /= d.ny;
+    z = (int)(row % d.nz);
+    b = (int)(row / d.nz);
+}
+
+// 32-channel input conv.  NOUT = 32 (hidden / dgrad) or 16 (the last layer,
+// output channel 0 real).  Weights: 27 packed taps of NOUT x 32.
+template <int NOUT, int EPI>
+__global__ void __launch_bounds__(128) conv32_kernel(Dims d, const __nv_bfloat16* __restrict__ in,
+                                                     const __nv_bfloat16* __restrict__ wpk,
+                                                     const float* __restrict__ bias, void* out,
+                                                     const __nv_bfloat16* __restrict__ mask,
+                                                     int* status) {
+    constexpr int WBYTES = 27 * NOUT * C * 2;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* sW = smem;
+    uint8_t* sA = smem + WBYTES;
+    uint64_t* bars = (uint64_t*)(sA + NSTAGE * STRIP);  // NSTAGE stage barriers, then "done"
+    uint32_t* tslot = (uint32_t*)(bars + NSTAGE + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int k = tid; k < WBYTES / 16; k += 128)
+        ((uint4*)sW)[k] = __ldg((const uint4*)wpk + k);
+    if (tid == 0) {
+        for (int s = 0; s <= NSTAGE; s++) tc::mbar_init(&bars[s], 1);
+    }
+    if (warp == 0) tc::tmem_alloc(tslot, 32);
+    tc::fence_async_smem();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = *tslot;
+    constexpr uint32_t idesc = tc::idesc_bf16(TM, NOUT);
+    const int64_t nt = ntiles(d);
+    int64_t qg = 0;  // strips staged so far by this CTA
+    int ntile = 0;   // tiles finished so far by this CTA
+    bool ok = true;
+    for (int64_t t = blockIdx.x; t < nt; t += gridDim.x) {
+        int b, z, y, x0;
+        tile_pos(d, t, b, z, y, x0);
+        for (int q = 0; q < 9; q++, qg++) {
+            const int dz = q / 3 - 1, dy = q % 3 - 1;
+            const int st = (int)(qg % NSTAGE);
+            if (qg >= NSTAGE && ok)
+                ok = tc::mbar_wait(&bars[st], (uint32_t)((qg / NSTAGE - 1) & 1), WAIT_LIMIT);
+            uint8_t* strip = sA + st * STRIP;
+            const int zz = z + dz, yy = y + dy;
+            const bool rin = zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny;
+            const int64_t rbase = (((int64_t)b * d.nz + zz) * d.ny + yy) * d.nx;
+            for (int r = tid; r < SROWS; r += 128) {
+                const int x = x0 - 1 + r;
+                uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0, v2 = v0, v3 = v0;
+                if (rin && x >= 0 && x < d.nx) {
+                    const uint4* p = (const uint4*)(in + (rbase + x) * C);
+                    v0 = __ldg(p);
+                    v1 = __ldg(p + 1);
+                    v2 = __ldg(p + 2);
+                    v3 = __ldg(p + 3);
+                }
+                *(uint4*)(strip + 0 * SROWS * 16 + r * 16) = v0;
+                *(uint4*)(strip + 1 * SROWS * 16 + r * 16) = v1;
+                *(uint4*)(strip + 2 * SROWS * 16 + r * 16) = v2;
+                *(uint4*)(strip + 3 * SROWS * 16 + r * 16) = v3;
+            }
+            tc::fence_async_smem();
+            __syncthreads();
+            if (tid == 0 && ok) {
+                tc::fence_after();
+                const uint32_t sa = tc::smem_u32(strip), sw = tc::smem_u32(sW);
+#pragma unroll
+                for (int dx = 0; dx < 3; dx++) {
+                    const int tap = q * 3 + dx;
+#pragma unroll
+                    for (int j = 0; j < 2; j++) {
+                        const uint64_t ad = tc::sdesc(sa + dx * 16 + j * 2 * SROWS * 16, SROWS * 16, 128);
+                        const uint64_t bd = tc::sdesc(sw + tap * NOUT * C * 2 + j * 256, 128, 512);
+                        tc::mma_bf16(tmem, ad, bd, idesc, (q | dx | j) != 0);
+                    }
+                }
+                tc::commit(&bars[st]);
+            }
+        }
+        if (tid == 0 && ok) tc::commit(&bars[NSTAGE]);
+        if (ok) ok = tc::mbar_wait(&bars[NSTAGE], (uint32_t)(ntile & 1), WAIT_LIMIT);
+        ntile++;
+        tc::fence_after();
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) atomicOr(status, NR_FLAG_TIMEOUT);
+            break;
+        }
+        uint32_t acc[32];
+        tc::ld32(tmem, (uint32_t)(warp * 32), 0, acc);
+        const int x = x0 + tid;
+        if (x < d.nx) {
+            const int64_t v = (((int64_t)b * d.nz + z) * d.ny + y) * d.nx + x;
+            epilogue<EPI>(acc, v, bias, out, mask);
+        }
+        tc::fence_before();
+        __syncthreads();  // TMEM read before the next tile's MMAs overwrite it
+    }
+    // drain: nothing may be in flight when TMEM is released
+    if (tid == 0) tc::commit(&bars[NSTAGE]);
+    tc::mbar_wait(&bars[NSTAGE], (uint32_t)(ntile & 1), WAIT_LIMIT);
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 32);
+}
+
+// 1-channel input conv (the first layer, and the back projection of the last
+// layer's gradient): each output row gathers its 27 neighbours (zero outside
+// its patch) x scale into one K = 32 row.  Weights: one packed 32 x 32 tile.
+template <int EPI>
+__global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restrict__ in, float scale,
+                                                    const __nv_bfloat16* __restrict__ wpk,
+                                                    const float* __restrict__ bias, void* out,
+                                                    const __nv_bfloat16* __restrict__ mask,
+                                                    int* status) {
+    __shared__ __align__(1024) uint8_t sW[C * C * 2];
+    __shared__ __align__(1024) uint8_t sA[KCH * TM * 16];
+    __shared__ __align__(8) uint64_t bars[1];
+    __shared__ uint32_t tslot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int k = tid; k < C * C * 2 / 16; k += 128) ((uint4*)sW)[k] = __ldg((const uint4*)wpk + k);
+    if (tid == 0) tc::mbar_init(&bars[0], 1);
+    if (warp == 0) tc::tmem_alloc(&tslot, 32);
+    tc::fence_async_smem();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tslot;
+    constexpr uint32_t idesc = tc::idesc_bf16(TM, C);
+    const int64_t nt = ntiles(d);
+    int ntile = 0;
+    bool ok = true;
+    for (int64_t t = blockIdx.x; t < nt; t += gridDim.x) {
+        int b, z, y, x0;
+        tile_pos(d, t, b, z, y, x0);
+        const int x = x0 + tid;
+        __align__(16) __nv_bfloat16 row[32];
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+            float v = 0.f;
+            if (k < 27) {
+                const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
+                const int zz = z + dz, yy = y + dy, xx = x + dx;
+                if (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny && xx >= 0 && xx < d.nx && x < d.nx)
+                    v = __ldg(in + (((int64_t)b * d.nz + zz) * d.ny + yy) * d.nx + xx) * scale;
+            }
+            row[k] = __float2bfloat16(v);
+        }
+        // previous tile's MMAs have completed (waited below), so sA is free
+#pragma unroll
+        for (int kc = 0; kc < KCH; kc++) *(uint4*)(sA + kc * TM * 16 + tid * 16) = ((uint4*)row)[kc];
+        tc::fence_async_smem();
+        __syncthreads();
+        if (tid == 0 && ok) {
+            tc::fence_after();
+            const uint32_t sa = tc::smem_u32(sA), sw = tc::smem_u32(sW);
+#pragma unroll
+            for (int j = 0; j < 2; j++)
+                tc::mma_bf16(tmem, tc::sdesc(sa + j * 2 * TM * 16, TM * 16, 128),
+                             tc::sdesc(sw + j * 256, 128, 512), idesc, j != 0);
+            tc::commit(&bars[0]);
+        }
+        if (ok) ok = tc::mbar_wait(&bars[0], (uint32_t)(ntile & 1), WAIT_LIMIT);
+        ntile++;
+        tc::fence_after();
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) atomicOr(status, NR_FLAG_TIMEOUT);
+            break;
+        }
+        uint32_t acc[32];
+        tc::ld32(tmem, (uint32_t)(warp * 32), 0, acc);
+        if (x < d.nx) {
+            const int64_t v = (((int64_t)b * d.nz + z) * d.ny + y) * d.nx + x;
+            epilogue<EPI>(acc, v, bias, out, mask);
+        }
+        tc::fence_before();
+        __syncthreads();
+    }
+    if (tid == 0) tc::commit(&bars[0]);
+    tc::mbar_wait(&bars[0], (uint32_t)(ntile & 1), WAIT_LIMIT);
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 32);
+}
+
+// ---------------------------------------------------------------------------
+// Weight gradients (CUDA cores).  dW[tap][o][i] = sum_v g[v][o] in[v+off(tap)][i]
+// over the stacked patches (zero outside each patch), db[o] = sum_v g[v][o].
+// Grid: (chunk of WG_CHUNK voxels, tap 0..27; tap 27 = bias).  Each block
+// writes one partial per output; wgrad_reduce_kernel adds the chunks in order.
+constexpr int WG_CHUNK = 2048;
+constexpr int WG_SUB = 64;
+
+__device__ __forceinline__ float ld_act(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+
+// Loads the shifted input (tap) and the output gradient of voxels s .. s+WG_SUB-1
+// into shared memory as FP32 (zero outside each patch / past the end).
+template <int NI, int NO, int GP, int XP>
+__device__ __forceinline__ void wg_stage(const Dims& d, int tap, int64_t s, int64_t V,
+                                         const void* __restrict__ g_, const void* __restrict__ in_,
+                                         float in_scale, float (*gs)[GP], float (*xs)[XP]) {
+    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+    for (int e = threadIdx.x; e < WG_SUB * NO; e += blockDim.x) {
+        const int vi = e / NO, o = e % NO;
+        const int64_t v = s + vi;
+        float gv = 0.f;
+        if (v < V) gv = NO == 1 ? ((const float*)g_)[v] : ld_act((const __nv_bfloat16*)g_ + v * C + o);
+        gs[vi][o] = gv;
+    }
+    for (int e = threadIdx.x; e < WG_SUB * NI; e += blockDim.x) {
+        const int vi = e / NI, i = e % NI;
+        const int64_t v = s + vi;
+        float xv = 0.f;
+        if (v < V) {
+            if (tap == 27) {
+                xv = 1.f;  // the bias "tap"
+            } else {
+                int64_t r = v;
+                const int x = (int)(r % d.nx);
+                r /= d.nx;
+                const int y = (int)(r % d.ny);
+                r /= d.ny;
+                const int z = (int)(r % d.nz);
+                const int b = (int)(r / d.nz);
+                const int xx = x + dx, yy = y + dy, zz = z + dz;
+                if (xx >= 0 && xx < d.nx && yy >= 0 && yy < d.ny && zz >= 0 && zz < d.nz) {
+                    const int64_t u = (((int64_t)b * d.nz + zz) * d.ny + yy) * d.nx + xx;
+                    xv = NI == 1 ? ((const float*)in_)[u] * in_scale
+                                 : ld_act((const __nv_bfloat16*)in_ + u * C + i);
+                }
+            }
+        }
+        xs[vi][i] = xv;
+    }
+}
+
+// 32 x 32 layers: thread -> output channel o = tid/8 and inputs i0..i0+3.
+__global__ void __launch_bounds__(256) wgrad32_kernel(Dims d, const __nv_bfloat16* __restrict__ g,
+                                                      const __nv_bfloat16* __restrict__ in,
+                                                      float* __restrict__ partial) {
+    __shared__ __align__(16) float gs[WG_SUB][C + 1];
+    __shared__ __align__(16) float xs[WG_SUB][C + 4];
+    const int tap = blockIdx.y;
+    const int64_t V = nvox(d);
+    const int64_t v0 = (int64_t)blockIdx.x * WG_CHUNK;
+    const int o = threadIdx.x >> 3, i0 = (threadIdx.x & 7) * 4;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+    for (int64_t s = v0; s < v0 + WG_CHUNK && s < V; s += WG_SUB) {
+        wg_stage<C, C, C + 1, C + 4>(d, tap, s, V, g, in, 1.f, gs, xs);
+        __syncthreads();
+#pragma unroll 8
+        for (int vi = 0; vi < WG_SUB; vi++) {
+            const float gv = gs[vi][o];
+            const float4 xv = *(const float4*)&xs[vi][i0];
+            a0 = fmaf(gv, xv.x, a0);
+            a1 = fmaf(gv, xv.y, a1);
+            a2 = fmaf(gv, xv.z, a2);
+            a3 = fmaf(gv, xv.w, a3);
+        }
+        __syncthreads();
+    }
+    const int64_t nchunk = gridDim.x;
+    const int64_t base = ((int64_t)tap * C * C + o * C + i0) * nchunk + blockIdx.x;
+    partial[base] = a0;
+    partial[base + nchunk] = a1;
+    partial[base + 2 * nchunk] = a2;
+    partial[base + 3 * nchunk] = a3;
+}
+
+// Thin layers (NI = 1 or NO = 1): 32 outputs per tap, one per thread of 32.
+template <int NI, int NO>
+__global__ void __launch_bounds__(32) wgrad_thin_kernel(Dims d, const void* __restrict__ g_,
+                                                        const void* __restrict__ in_,
+                                                        float in_scale,
+                                                        float* __restrict__ partial) {
+    __shared__ float gs[WG_SUB][NO + 1];
+    __shared__ float xs[WG_SUB][NI + 1];
+    const int tap = blockIdx.y;
+    const int64_t V = nvox(d);
+    const int64_t v0 = (int64_t)blockIdx.x * WG_CHUNK;
+    const int oi = threadIdx.x;  // NI * NO == 32
+    const int o = oi / NI, i = oi % NI;
+    float acc = 0.f;
+    for (int64_t s = v0; s < v0 + WG_CHUNK && s < V; s += WG_SUB) {
+        wg_stage<NI, NO, NO + 1, NI + 1>(d, tap, s, V, g_, in_, in_scale, gs, xs);
+        __syncthreads();
+        for (int vi = 0; vi < WG_SUB; vi++) acc = fmaf(gs[vi][o], xs[vi][i], acc);
+        __syncthreads();
+    }
+    partial[((int64_t)tap * 32 + oi) * gridDim.x + blockIdx.x] = acc;
+}
+
+// grad[tap][o][i] (and grad_b[o] from tap 27, i = 0) = sum over chunks, in order.
+__global__ void wgrad_reduce_kernel(const float* __restrict__ partial, int64_t nchunk, int nout,
+                                    int ni, float* __restrict__ gw, float* __restrict__ gb) {
+    const int64_t n = 28LL * nout;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const float* p = partial + e * nchunk;
+        double s = 0.0;
+        for (int64_t c = 0; c < nchunk; c++) s += p[c];
+        const int tap = (int)(e / nout), oi = (int)(e % nout);
+        if (tap < 27) gw[e] = (float)s;
+        else if (oi % ni == 0) gb[oi / ni] = (float)s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Packing FP32 master weights W[tap][o][i] into the BF16 B operands.
+// mode 0: forward of a 32-input layer: tap t, row n = o (NOUT rows, o >= NO zero), k = i.
+// mode 1: dgrad of a 32-output layer (input gradient has NO = 32 channels):
+//         tap t' , row n = i, k = o, from W[26 - t'] (flipped).
+// mode 2: forward of the 1-input layer: one tile, row n = o, k = tap.
+// mode 3: dgrad of the 1-output layer as a 1-channel conv: row n = i, k = tap',
+//         from W[26 - tap'][0][i].
+__global__ void pack_kernel(const float* __restrict__ w, int mode, int NI, int NO, int NOUT,
+                            __nv_bfloat16* __restrict__ out) {
+    const int per_tap = NOUT * C;
+    const int total = (mode == 2 || mode == 3) ? C * C : 27 * per_tap;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        float v = 0.f;
+        int dst;
+        if (mode == 0) {
+            const int t = e / per_tap, r = e % per_tap, n = r / C, k = r % C;
+            if (n < NO && k < NI) v = w[((int64_t)t * NO + n) * NI + k];
+            dst = t * per_tap + bpk_index(n, k);
+        } else if (mode == 1) {
+            const int t = e / per_tap, r = e % per_tap, n = r / C, k = r % C;
+            if (n < NI && k < NO) v = w[((int64_t)(26 - t) * NO + k) * NI + n];
+            dst = t * per_tap + bpk_index(n, k);
+        } else if (mode == 2) {
+            const int n = e / C, k = e % C;
+            if (k < 27 && n < NO) v = w[((int64_t)k * NO + n) * NI + 0];
+            dst = bpk_index(n, k);
+        } else {
+            const int n = e / C, k = e % C;
+            if (k < 27 && n < NI) v = w[((int64_t)(26 - k) * NO + 0) * NI + n];
+            dst = bpk_index(n, k);
+        }
+        out[dst] = __float2bfloat16(v);
+    }
+}
+
+// Loss 1/V sum (f - r)^2 (per-block FP64 partials) and its gradient 2(f - r)/V.
+__global__ void loss_kernel(const float* __restrict__ f, const float* __restrict__ r, int64_t V,
+                            float* __restrict__ g, double* __restrict__ partial) {
+    __shared__ double ws[8];
+    double s = 0.0;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < V;
+         v += (int64_t)gridDim.x * blockDim.x) {
+        const float e = f[v] - r[v];
+        g[v] = 2.f * e / (float)V;
+        s += (double)e * e;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) t += ws[k];
+        partial[blockIdx.x] = t;
+    }
+}
+
+__global__ void loss_final_kernel(const double* __restrict__ partial, int n, int64_t V,
+                                  double* __restrict__ out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < n; k++) t += partial[k];
+        out[0] = t / (double)V;
+    }
+}
+
+// Adam (Kingma & Ba 2015) with bias correction, FP32 master parameters.
+__global__ void adam_kernel(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v,
+                            const float* __restrict__ g, int64_t n, float lr, float b1, float b2,
+                            float eps, float c1, float c2) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const float gk = g[k];
+        const float mk = b1 * m[k] + (1.f - b1) * gk;
+        const float vk = b2 * v[k] + (1.f - b2) * gk * gk;
+        m[k] = mk;
+        v[k] = vk;
+        p[k] -= lr * (mk / c1) / (sqrtf(vk / c2) + eps);
+    }
+}
+
+// x_warm = x + f / s (and a non-negativity clamp, the OSTR constraint).
+__global__ void residual_out_kernel(const float* __restrict__ x, const float* __restrict__ f,
+                                    float inv_s, int64_t V, float* __restrict__ out) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < V;
+         v += (int64_t)gridDim.x * blockDim.x)
+        out[v] = fmaxf(x[v] + f[v] * inv_s, 0.f);
+}
+
+}  // namespace cnn
+}  // namespace nr
+
+// ---------------------------------------------------------------------------
+// Host side: parameter layout, workspace layout, forward / backward sequencing.
+namespace nr {
+namespace cnn {
+
+struct Layer {
+    int ni, no;
+};
+constexpr Layer LAYERS[6] = {{1, C}, {C, C}, {C, C}, {C, C}, {C, C}, {C, 1}};
+
+// FP32 parameters: for each layer W[27][no][ni] then b[no].
+static void param_offsets(int64_t* w, int64_t* b, int64_t* total) {
+    int64_t o = 0;
+    for (int l = 0; l < 6; l++) {
+        w[l] = o;
+        o += 27LL * LAYERS[l].no * LAYERS[l].ni;
+        b[l] = o;
+        o += LAYERS[l].no;
+    }
+    *total = o;
+}
+
+constexpr size_t PK_HID = 27 * C * C * 2;   // packed 32 -> 32 taps
+constexpr size_t PK_LAST = 27 * 16 * C * 2; // packed 32 -> 1 (16 rows)
+constexpr size_t PK_ONE = C * C * 2;        // packed 1-channel tile
+
+struct WSL {
+    size_t status, pk_fwd[6], pk_bwd[6], act[5], f, r, g6, dpre[2], part, grad, lpart, lout, total;
+    int64_t nchunk, lblocks;
+};
+
+static size_t al(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static WSL layout(const Dims& d, bool training) {
+    WSL L{};
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o = al(o + bytes);
+        return at;
+    };
+    const int64_t V = nvox(d);
+    int64_t wo[6], bo[6], P;
+    param_offsets(wo, bo, &P);
+    L.status = take(256);
+    L.pk_fwd[0] = take(PK_ONE);
+    for (int l = 1; l < 5; l++) L.pk_fwd[l] = take(PK_HID);
+    L.pk_fwd[5] = take(PK_LAST);
+    const int nact = training ? 5 : 2;
+    for (int k = 0; k < nact; k++) L.act[k] = take((size_t)V * C * 2);
+    L.f = take((size_t)V * 4);
+    L.nchunk = (V + WG_CHUNK - 1) / WG_CHUNK;
+    L.lblocks = 1024;
+    if (training) {
+        for (int l = 1; l < 5; l++) L.pk_bwd[l] = take(PK_HID);
+        L.pk_bwd[5] = take(PK_ONE);
+        L.r = take((size_t)V * 4);
+        L.g6 = take((size_t)V * 4);
+        L.dpre[0] = take((size_t)V * C * 2);
+        L.dpre[1] = take((size_t)V * C * 2);
+        L.part = take((size_t)28 * C * C * L.nchunk * 4);
+        L.grad = take((size_t)P * 4);
+        L.lpart = take((size_t)L.lblocks * 8);
+        L.lout = take(8);
+    }
+    L.total = o;
+    return L;
+}
+
+static int sm_count() {
+    int dev = 0, n = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n;
+}
+
+template <int NOUT, int EPI>
+static nr_status launch_conv32(const Dims& d, const __nv_bfloat16* in, const __nv_bfloat16* wpk,
+                               const float* bias, void* out, const __nv_bfloat16* mask,
+                               int* status, cudaStream_t s) {
+    const size_t smem = (size_t)27 * NOUT * C * 2 + NSTAGE * STRIP + 8 * (NSTAGE + 1) + 16;
+    if (cudaFuncSetAttribute(conv32_kernel<NOUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+        return NR_ERR_CUDA;
+    const int64_t nt = ntiles(d);
+    const int grid = (int)(nt < (int64_t)sm_count() * 2 ? nt : (int64_t)sm_count() * 2);
+    conv32_kernel<NOUT, EPI><<<grid, 128, smem, s>>>(d, in, wpk, bias, out, mask, status);
+    return launch_status();
+}
+
+template <int EPI>
+static nr_status launch_conv1(const Dims& d, const float* in, float scale,
+                              const __nv_bfloat16* wpk, const float* bias, void* out,
+                              const __nv_bfloat16* mask, int* status, cudaStream_t s) {
+    const int64_t nt = ntiles(d);
+    const int grid = (int)(nt < (int64_t)sm_count() * 4 ? nt : (int64_t)sm_count() * 4);
+    conv1_kernel<EPI><<<grid, 128, 0, s>>>(d, in, scale, wpk, bias, out, mask, status);
+    return launch_status();
+}
+
+static void pack(const float* w, int mode, int ni, int no, int nout, __nv_bfloat16* out,
+                 cudaStream_t s) {
+    pack_kernel<<<64, 256, 0, s>>>(w, mode, ni, no, nout, out);
+}
+
+// Forward through layer 6: f = conv6(a5) in `f`; activations in `acts`
+// (5 buffers when `keep`, else 2 ping-pong buffers).
+static nr_status forward(const Dims& d, const float* params, const float* x, float s,
+                         char* ws, const WSL& L, bool keep, cudaStream_t st) {
+    int64_t wo[6], bo[6], P;
+    param_offsets(wo, bo, &P);
+    int* status = (int*)(ws + L.status);
+    auto pkf = [&](int l) { return (__nv_bfloat16*)(ws + L.pk_fwd[l]); };
+    pack(params + wo[0], 2, 1, C, C, pkf(0), st);
+    for (int l = 1; l < 5; l++) pack(params + wo[l], 0, C, C, C, pkf(l), st);
+    pack(params + wo[5], 0, C, 1, 16, pkf(5), st);
+    auto act = [&](int l) {  // output of layer l (0-based, l < 5)
+        return (__nv_bfloat16*)(ws + L.act[keep ? l : (l & 1)]);
+    };
+    nr_status e;
+    if ((e = launch_conv1<EPI_RELU>(d, x, s, pkf(0), params + bo[0], act(0), nullptr, status, st)) != NR_OK)
+        return e;
+    for (int l = 1; l < 5; l++)
+        if ((e = launch_conv32<C, EPI_RELU>(d, act(l - 1), pkf(l), params + bo[l], act(l), nullptr,
+                                            status, st)) != NR_OK)
+            return e;
+    return launch_conv32<16, EPI_RESID>(d, act(4), pkf(5), params + bo[5], ws + L.f, nullptr,
+                                        status, st);
+}
+
+__global__ void target_kernel(const float* __restrict__ x, const float* __restrict__ t, float s,
+                              int64_t V, float* __restrict__ r) {
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < V;
+         v += (int64_t)gridDim.x * blockDim.x)
+        r[v] = s * (t[v] - x[v]);
+}
+
+static nr_status wgrad(const Dims& d, int l, const void* g, const void* in, float s, char* ws,
+                       const WSL& L, float* grad, cudaStream_t st) {
+    int64_t wo[6], bo[6], P;
+    param_offsets(wo, bo, &P);
+    float* part = (float*)(ws + L.part);
+    const dim3 grid((unsigned)L.nchunk, 28);
+    int nout, ni;
+    if (l == 0) {
+        wgrad_thin_kernel<1, C><<<grid, 32, 0, st>>>(d, g, in, s, part);
+        nout = C;
+        ni = 1;
+    } else if (l == 5) {
+        wgrad_thin_kernel<C, 1><<<grid, 32, 0, st>>>(d, g, in, 1.f, part);
+        nout = C;
+        ni = C;
+    } else {
+        wgrad32_kernel<<<grid, 256, 0, st>>>(d, (const __nv_bfloat16*)g, (const __nv_bfloat16*)in,
+                                              part);
+        nout = C * C;
+        ni = C;
+    }
+    wgrad_reduce_kernel<<<(28 * nout + 255) / 256, 256, 0, st>>>(part, L.nchunk, nout, ni,
+                                                                 grad + wo[l], grad + bo[l]);
+    return launch_status();
+}
+
+static nr_status loss_grad(const Dims& d, const float* params, const float* x, const float* target,
+                           float s, float* grad, char* ws, const WSL& L, cudaStream_t st) {
+    const int64_t V = nvox(d);
+    int64_t wo[6], bo[6], P;
+    param_offsets(wo, bo, &P);
+    int* status = (int*)(ws + L.status);
+    nr_status e;
+    if ((e = forward(d, params, x, s, ws, L, true, st)) != NR_OK) return e;
+    float* r = (float*)(ws + L.r);
+    float* g6 = (float*)(ws + L.g6);
+    target_kernel<<<1024, 256, 0, st>>>(x, target, s, V, r);
+    loss_kernel<<<(unsigned)L.lblocks, 256, 0, st>>>((const float*)(ws + L.f), r, V, g6,
+                                                      (double*)(ws + L.lpart));
+    loss_final_kernel<<<1, 32, 0, st>>>((const double*)(ws + L.lpart), (int)L.lblocks, V,
+                                        (double*)(ws + L.lout));
+    auto act = [&](int l) { return (const __nv_bfloat16*)(ws + L.act[l]); };
+    auto dpre = [&](int k) { return (__nv_bfloat16*)(ws + L.dpre[k & 1]); };
+    auto pkb = [&](int l) { return (__nv_bfloat16*)(ws + L.pk_bwd[l]); };
+    for (int l = 1; l < 5; l++) pack(params + wo[l], 1, C, C, C, pkb(l), st);
+    pack(params + wo[5], 3, C, 1, C, pkb(5), st);
+    // layer 6: weight gradient and the masked input gradient dpre5
+    if ((e = wgrad(d, 5, g6, act(4), 1.f, ws, L, grad, st)) != NR_OK) return e;
+    if ((e = launch_conv1<EPI_MASK>(d, g6, 1.f, pkb(5), nullptr, dpre(4), act(4), status, st)) !=
+        NR_OK)
+        return e;
+    // layers 5..2: dpre_l lives in dpre(l-1)
+    for (int l = 4; l >= 1; l--) {
+        if ((e = wgrad(d, l, dpre(l), act(l - 1), 1.f, ws, L, grad, st)) != NR_OK) return e;
+        if ((e = launch_conv32<C, EPI_MASK>(d, dpre(l), pkb(l), nullptr, dpre(l - 1), act(l - 1),
+                                            status, st)) != NR_OK)
+            return e;
+    }
+    return wgrad(d, 0, dpre(0), x, s, ws, L, grad, st);
+}
+
+}  // namespace cnn
+}  // namespace nr
+
+using namespace nr;
+using namespace nr::cnn;
+
+static bool dims_ok(const nr_cnn_dims* d) {
+    return d && d->nx > 0 && d->ny > 0 && d->nz > 0 && d->nb > 0 &&
+           (int64_t)d->nx * d->ny * d->nz * d->nb < ((int64_t)1 << 31);
+}
+
+static Dims to_dims(const nr_cnn_dims* d) { return Dims{d->nx, d->ny, d->nz, d->nb}; }
+
+NR_API nr_status nr_cnn_param_count(int64_t* n) {
+    if (!n) return NR_ERR_BAD_ARGUMENT;
+    int64_t wo[6], bo[6];
+    param_offsets(wo, bo, n);
+    return NR_OK;
+}
+
+NR_API nr_status nr_cnn_workspace_size(const nr_cnn_dims* d, int32_t training, size_t* bytes) {
+    if (!dims_ok(d) || !bytes) return NR_ERR_BAD_ARGUMENT;
+    *bytes = layout(to_dims(d), training != 0).total;
+    return NR_OK;
+}
+
+NR_API nr_status nr_cnn_forward(const nr_cnn_dims* d, const float* params, const float* x,
+                                float in_scale, float* x_out, void* ws, size_t ws_bytes,
+                                void* stream) {
+    if (!dims_ok(d) || !params || !x || !x_out || !(in_scale > 0.f)) return NR_ERR_BAD_ARGUMENT;
+    const Dims D = to_dims(d);
+    const WSL L = layout(D, false);
+    if (!ws || ws_bytes < L.total || ((uintptr_t)ws & 255)) return NR_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    nr_status e = forward(D, params, x, in_scale, (char*)ws, L, false, st);
+    if (e != NR_OK) return e;
+    residual_out_kernel<<<1024, 256, 0, st>>>(x, (const float*)((char*)ws + L.f), 1.f / in_scale,
+                                              nvox(D), x_out);
+    return launch_status();
+}
+
+NR_API nr_status nr_cnn_loss_grad(const nr_cnn_dims* d, const float* params, const float* x,
+                                  const float* target, float in_scale, float* grad, double* loss,
+                                  void* ws, size_t ws_bytes, void* stream) {
+    if (!dims_ok(d) || !params || !x || !target || !(in_scale > 0.f)) return NR_ERR_BAD_ARGUMENT;
+    const Dims D = to_dims(d);
+    const WSL L = layout(D, true);
+    if (!ws || ws_bytes < L.total || ((uintptr_t)ws & 255)) return NR_ERR_WORKSPACE;
+    cudaStream_t st = as_stream(stream);
+    char* w = (char*)ws;
+    float* g = grad ? grad : (float*)(w + L.grad);
+    nr_status e = loss_grad(D, params, x, target, in_scale, g, w, L, st);
+    if (e != NR_OK) return e;
+    if (loss &&
+        cudaMemcpyAsync(loss, w + L.lout, 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        return NR_ERR_CUDA;
+    return NR_OK;
+}
+
+NR_API nr_status nr_cnn_adam(float* params, float* m, float* v, const float* grad, int64_t n,
+                             int32_t step, float lr, void* stream) {
+    if (!params || !m || !v || !grad || n <= 0 || step < 1 || !(lr > 0.f)) return NR_ERR_BAD_ARGUMENT;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+    adam_kernel<<<256, 256, 0, as_stream(stream)>>>(params, m, v, grad, n, lr, b1, b2, 1e-8f, c1,
+                                                    c2);
+    return launch_status();
+}
+
+NR_API nr_status nr_cnn_train_step(const nr_cnn_dims* d, float* params, float* adam_m,
+                                   float* adam_v, int32_t step, float lr, const float* x,
+                                   const float* target, float in_scale, double* loss, void* ws,
+                                   size_t ws_bytes, void* stream) {
+    nr_status e = nr_cnn_loss_grad(d, params, x, target, in_scale, nullptr, loss, ws, ws_bytes,
+                                   stream);
+    if (e != NR_OK) return e;
+    const WSL L = layout(to_dims(d), true);
+    int64_t P;
+    nr_cnn_param_count(&P);
+    return nr_cnn_adam(params, adam_m, adam_v, (const float*)((char*)ws + L.grad), P, step, lr,
+                       stream);
+}
+
+NR_API nr_status nr_cnn_check(void* ws, int32_t* flags, void* stream) {
+    if (!ws || !flags) return NR_ERR_BAD_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    int v = 0;
+    if (cudaMemcpyAsync(&v, ws, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return NR_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return NR_ERR_CUDA;
+    *flags = v;
+    if (v) cudaMemsetAsync(ws, 0, sizeof(int), s);
+    return (v & NR_FLAG_TIMEOUT) ? NR_ERR_TIMEOUT : NR_OK;
+}

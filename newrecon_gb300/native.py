@@ -64,6 +64,14 @@ SIGNATURES = {
     "nr_batch_step": (_I32, [_P, _I32, _P]),
     "nr_batch_finish": (_I32, [_P, _P]),
     "nr_batch_graph_create": (_I32, [_P, _I32, _P, ctypes.POINTER(ctypes.c_void_p)]),
+    "nr_cnn_param_count": (_I32, [ctypes.POINTER(_I64)]),
+    "nr_cnn_workspace_size": (_I32, [_P, _I32, ctypes.POINTER(ctypes.c_size_t)]),
+    "nr_cnn_forward": (_I32, [_P, _P, _P, _F, _P, _P, ctypes.c_size_t, _P]),
+    "nr_cnn_loss_grad": (_I32, [_P, _P, _P, _P, _F, _P, _P, _P, ctypes.c_size_t, _P]),
+    "nr_cnn_adam": (_I32, [_P, _P, _P, _P, _I64, _I32, _F, _P]),
+    "nr_cnn_train_step": (_I32, [_P, _P, _P, _P, _I32, _F, _P, _P, _F, _P, _P, ctypes.c_size_t,
+                                 _P]),
+    "nr_cnn_check": (_I32, [_P, ctypes.POINTER(_I32), _P]),
     "nr_ostr_check": (_I32, [_P, ctypes.c_size_t, ctypes.POINTER(_I32), _P]),
     "nr_penalty_fp64_static": (_I32, [_GP, _P, _I32, _F, _P, _P]),
     "nr_version": (ctypes.c_char_p, []),
