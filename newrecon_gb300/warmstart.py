@@ -125,3 +125,337 @@ class WarmStartCNN:
 
     def state(self) -> np.ndarray:
         return self.params.cpu().numpy()
+
+
+# ---------------------------------------------------------------------------
+# Training data, training, evaluation.
+
+@dataclasses.dataclass
+class TrainConfig:
+    """Training / validation recipe (seeded end to end)."""
+
+    n_train: int = 512               # training phantoms
+    n_val: int = 64                  # held-out phantoms
+    crop: Tuple[int, int] = (256, 128)   # in-plane voxels per case (0.14 mm), full thickness
+    early_iters: int = 2             # the network's input: OSTR after this many iterations
+    full_iters: int = 50             # the target: OSTR after this many iterations
+    after_iters: int = 3             # OSTR iterations after the warm start
+    patch: Tuple[int, int, int] = (128, 32, 16)  # training patch (nx, ny, nz)
+    batch: int = 8                   # patches per Adam step
+    steps: int = 2000
+    lr: float = 2e-3
+    seed: int = 10_000               # training seeds seed .. seed+n_train-1, validation after
+    workers: int = 8                 # processes generating phantoms
+    last_scale: float = 0.1          # initial scale of the last layer (x He)
+
+
+def case_configs(n: int, seed: int, crop: Tuple[int, int]):
+    """Batched-workload cases (uneven thickness / views / dose) on a cropped
+    in-plane field with the detector fitted to the volume's shadow."""
+    from .geometry import Geometry, ReconConfig, view_angles
+
+    out = []
+    for c in range(n):
+        rng = np.random.default_rng(seed + c)
+        nz = int(round(rng.uniform(30, 80)))
+        views = int(rng.choice([9, 15, 25]))
+        span = float(rng.uniform(7.5, 25.0))
+        I0 = float(rng.uniform(3e3, 2e4))
+        gland = float(rng.uniform(0.10, 0.50))
+        nx, ny = crop
+        g0 = Geometry.dbt(nx, ny, nz, 0.14, 1.0, 8, 8, 0.14, views)
+        angles = view_angles(views, span)
+        g = fit_detector(g0, angles)
+        out.append(ReconConfig(f"case{seed + c}", g, angles, I0, views, 50, "hyperbola", 50.0,
+                               0.002, int(round(100 * gland)), 10, float(nz), seed + c))
+    return out
+
+
+def fit_detector(g, angles, margin: int = 4):
+    """A detector on the 0.14 mm bin grid covering the volume's shadow in every view."""
+    xs = [g.x_p0, g.x_p0 + g.nx * g.vx]
+    ys = [g.y_p0, g.y_p0 + g.ny * g.vy]
+    zs = [g.z_p0, g.z_p0 + g.nz * g.vz]
+    lo = [np.inf, np.inf]
+    hi = [-np.inf, -np.inf]
+    for th in np.asarray(angles, np.float64):
+        sx, sy, sz = g.sourceR * np.sin(th), g.sourceY, g.sourceR * np.cos(th)
+        for x in xs:
+            for y in ys:
+                for z in zs:
+                    t = (-g.detectorR - sz) / (z - sz)
+                    px, py = sx + (x - sx) * t, sy + (y - sy) * t
+                    lo = [min(lo[0], px), min(lo[1], py)]
+                    hi = [max(hi[0], px), max(hi[1], py)]
+    b = g.bx
+    i0 = int(np.floor(lo[0] / b)) - margin
+    i1 = int(np.ceil(hi[0] / b)) + margin
+    j0 = int(np.floor(lo[1] / b)) - margin
+    j1 = int(np.ceil(hi[1] / b)) + margin
+    return dataclasses.replace(g, nbx=i1 - i0, nby=j1 - j0, x_d0=i0 * b, y_d0=j0 * b)
+
+
+def _phantom_job(args):
+    from .phantom import breast_phantom
+
+    g, seed, gland, n_calc = args
+    return breast_phantom(g, seed, 0, n_calc, glandular_fraction=gland).ravel()
+
+
+def phantoms(cfgs, workers: int) -> List[np.ndarray]:
+    """Seeded phantoms, generated in `workers` spawned processes."""
+    jobs = [(c.geom, c.seed, c.n_glandular / 100.0, c.n_calc) for c in cfgs]
+    if workers <= 1:
+        return [_phantom_job(j) for j in jobs]
+    import multiprocessing as mp
+
+    with mp.get_context("spawn").Pool(workers) as pool:
+        return pool.map(_phantom_job, jobs)
+
+
+@dataclasses.dataclass
+class Pair:
+    cfg: object
+    x_early: torch.Tensor
+    x_full: torch.Tensor
+    y: np.ndarray
+    b: np.ndarray
+
+
+def make_pairs(cfgs, phantom_vols, early: int, full: int) -> List[Pair]:
+    """OSTR on each phantom's Poisson scan: the early iterate and the target."""
+    from . import ostr
+    from .phantom import poisson_counts
+
+    out = []
+    for c, xt in zip(cfgs, phantom_vols):
+        g = c.geom
+        ostr.set_geometry(g)
+        idx = np.arange(g.n_angles, dtype=np.int32)
+        line = torch.zeros(g.n_angles * g.n_bins, device="cuda")
+        ostr.fprojectCB_1R_GPU_OSTR_cos(torch.from_numpy(xt).cuda(), line,
+                                        torch.from_numpy(c.angles).cuda(),
+                                        torch.from_numpy(idx).cuda(), 0, g.n_angles)
+        y = poisson_counts(line.cpu().numpy(), c.I0, c.seed)
+        b = np.full_like(y, c.I0)
+        plan = OSTR(g, subset_num=c.subset_num, beta=c.beta, delta=c.delta,
+                    potential=c.potential)
+        plan.setup(c.angles, y, b)
+        x = torch.zeros(g.n_voxels, device="cuda")
+        plan.iterate(x, early)
+        x_early = x.clone()
+        plan.iterate(x, full - early)
+        plan.check()
+        out.append(Pair(c, x_early, x.clone(), y, b))
+    return out
+
+
+def sample_batch(pairs: Sequence[Pair], patch, batch: int, rng: np.random.Generator):
+    px, py, pz = patch
+    xs, ts = [], []
+    for _ in range(batch):
+        p = pairs[int(rng.integers(len(pairs)))]
+        g = p.cfg.geom
+        x0 = int(rng.integers(0, g.nx - px + 1))
+        y0 = int(rng.integers(0, g.ny - py + 1))
+        z0 = int(rng.integers(0, g.nz - pz + 1))
+        sl = (slice(z0, z0 + pz), slice(y0, y0 + py), slice(x0, x0 + px))
+        xs.append(p.x_early.view(g.nz, g.ny, g.nx)[sl])
+        ts.append(p.x_full.view(g.nz, g.ny, g.nx)[sl])
+    return (torch.stack(xs).contiguous().view(-1), torch.stack(ts).contiguous().view(-1),
+            (px, py, pz, batch))
+
+
+def train(cnn: WarmStartCNN, pairs: Sequence[Pair], cfg: TrainConfig, log_every: int = 100):
+    """Adam with a cosine-decayed learning rate; returns [(step, loss), ...]."""
+    rng = np.random.default_rng(cfg.seed + 7)
+    hist = []
+    for s in range(cfg.steps):
+        lr = cfg.lr * 0.5 * (1.0 + np.cos(np.pi * s / cfg.steps))
+        xb, tb, dims = sample_batch(pairs, cfg.patch, cfg.batch, rng)
+        loss = cnn.train_step(xb, tb, dims, max(lr, 1e-6))
+        if s % log_every == 0 or s == cfg.steps - 1:
+            hist.append((s, float(loss.item())))
+    cnn.check()
+    return hist
+
+
+def _rmse(a: torch.Tensor, b: torch.Tensor) -> float:
+    return float(torch.sqrt(torch.mean((a.double() - b.double()) ** 2)).item())
+
+
+def warm_start_volume(cnn: WarmStartCNN, x_early: torch.Tensor, g) -> torch.Tensor:
+    """x_warm for a whole volume (one patch of the full size)."""
+    return cnn.forward(x_early, (g.nx, g.ny, g.nz, 1))
+
+
+def evaluate(cnn: WarmStartCNN, pair: Pair, after: int, early: int = 2,
+             rmse_tol: float = 1e-4, max_iters: int = 60) -> dict:
+    """Warm start vs plain OSTR on one case, judged on the FP64 objective at
+    equal total subset-iterations and on RMSE against the target x_full.
+
+    Wall times are measured with the plan set up (scan resident on the GPU),
+    from x = 0: plain OSTR counts iterations to reach RMSE <= rmse_tol; the
+    warm start counts early iterations + inference + iterations after it.
+    """
+    c = pair.cfg
+    g = c.geom
+    plan = OSTR(g, subset_num=c.subset_num, beta=c.beta, delta=c.delta, potential=c.potential)
+    plan.setup(c.angles, pair.y, pair.b)
+    M = c.subset_num
+    ref = pair.x_full
+    # equal-work comparison
+    xp = torch.zeros(g.n_voxels, device="cuda")
+    plan.iterate(xp, early + after)
+    xe = torch.zeros(g.n_voxels, device="cuda")
+    plan.iterate(xe, early)
+    xw = warm_start_volume(cnn, xe, g)
+    plan.iterate(xw, after)
+    plan.check()
+    obj_plain = plan.total_objective(xp)
+    obj_warm = plan.total_objective(xw)
+    obj_ref = plan.total_objective(ref)
+    accept = obj_warm <= obj_plain
+    out = dict(case=c.name, subsets=M, early=early, after=after,
+               objective_plain=obj_plain, objective_warm=obj_warm, objective_full=obj_ref,
+               rmse_plain=_rmse(xp, ref), rmse_warm=_rmse(xw, ref),
+               max_abs_plain=float((xp - ref).abs().max().item()),
+               max_abs_warm=float((xw - ref).abs().max().item()), accepted=bool(accept))
+    # time to RMSE <= tol: plain
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x = torch.zeros(g.n_voxels, device="cuda")
+    it_plain = None
+    for k in range(1, max_iters + 1):
+        plan.iterate(x, 1)
+        if _rmse(x, ref) <= rmse_tol:
+            it_plain = k
+            break
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    x = torch.zeros(g.n_voxels, device="cuda")
+    plan.iterate(x, early)
+    x = warm_start_volume(cnn, x, g)
+    it_warm = None
+    for k in range(1, max_iters + 1):
+        plan.iterate(x, 1)
+        if _rmse(x, ref) <= rmse_tol:
+            it_warm = k
+            break
+    torch.cuda.synchronize()
+    t_warm = time.perf_counter() - t0
+    out.update(rmse_tol=rmse_tol, iters_to_tol_plain=it_plain, seconds_to_tol_plain=t_plain,
+               iters_to_tol_warm=None if it_warm is None else early + it_warm,
+               seconds_to_tol_warm=t_warm)
+    return out
+
+
+def warm_reconstruct(cnn: WarmStartCNN, geom, prj, blank, *, angles, subset_num: int,
+                     iter_num: int, beta: float, delta: float, potential: str = "hyperbola",
+                     early: int = 2, scat=None) -> Tuple[torch.Tensor, dict]:
+    """OSTR with the learned warm start and plain OSTR as fallback and judge.
+
+    Runs `early` iterations, the network, then `iter_num - early` iterations;
+    the same number of plain iterations is run from the early iterate, and the
+    result with the lower FP64 objective is returned with a report."""
+    plan = OSTR(geom, subset_num=subset_num, beta=beta, delta=delta, potential=potential,
+                has_scatter=scat is not None)
+    plan.setup(angles, prj, blank, scat)
+    x = torch.zeros(geom.n_voxels, device=plan.ws.device)
+    plan.iterate(x, early)
+    xw = warm_start_volume(cnn, x, geom)
+    rest = max(iter_num - early, 0)
+    plan.iterate(xw, rest)
+    plan.iterate(x, rest)
+    plan.check()
+    ow, op = plan.total_objective(xw), plan.total_objective(x)
+    keep = ow <= op
+    return (xw if keep else x), dict(objective_warm=ow, objective_plain=op, accepted=keep)
+
+
+def run(cfg: TrainConfig, out_params: Optional[str] = None, n_time: int = 4,
+        log=print) -> dict:
+    """The whole recipe: data, training, held-out evaluation.  Returns a report."""
+    t0 = time.perf_counter()
+    tr_cfgs = case_configs(cfg.n_train, cfg.seed, cfg.crop)
+    va_cfgs = case_configs(cfg.n_val, cfg.seed + cfg.n_train, cfg.crop)
+    vols = phantoms(tr_cfgs + va_cfgs, cfg.workers)
+    t1 = time.perf_counter()
+    pairs = make_pairs(tr_cfgs, vols[:cfg.n_train], cfg.early_iters, cfg.full_iters)
+    val = make_pairs(va_cfgs, vols[cfg.n_train:], cfg.early_iters, cfg.full_iters)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    log(f"data: {len(pairs)} train + {len(val)} held-out pairs; phantoms {t1 - t0:.1f} s, "
+        f"OSTR pairs {t2 - t1:.1f} s")
+    cnn = WarmStartCNN(init_params(cfg.seed, last_scale=cfg.last_scale))
+    hist = train(cnn, pairs, cfg)
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    log(f"train: {cfg.steps} steps in {t3 - t2:.1f} s, loss {hist[0][1]:.3e} -> {hist[-1][1]:.3e}")
+    evals = []
+    for k, p in enumerate(val):
+        e = evaluate(cnn, p, cfg.after_iters, cfg.early_iters,
+                     max_iters=cfg.full_iters if k < n_time else 0)
+        evals.append(e)
+    t4 = time.perf_counter()
+    acc = [e["accepted"] for e in evals]
+    rep = {
+        "config": dataclasses.asdict(cfg),
+        "params": int(cnn.params.numel()),
+        "loss_history": hist,
+        "seconds": {"phantoms": t1 - t0, "ostr_pairs": t2 - t1, "train": t3 - t2,
+                    "eval": t4 - t3},
+        "held_out": evals,
+        "accept_rate": float(np.mean(acc)) if acc else None,
+        "mean_objective_gain": float(np.mean([(e["objective_plain"] - e["objective_warm"])
+                                              / abs(e["objective_plain"]) for e in evals])),
+        "mean_rmse_plain": float(np.mean([e["rmse_plain"] for e in evals])),
+        "mean_rmse_warm": float(np.mean([e["rmse_warm"] for e in evals])),
+    }
+    if out_params:
+        np.savez_compressed(out_params, params=cnn.state(), scale=cnn.scale,
+                            early_iters=cfg.early_iters)
+    return rep
+
+
+def load(path: str) -> WarmStartCNN:
+    z = np.load(path)
+    return WarmStartCNN(z["params"], scale=float(z["scale"]))
+
+
+def main(argv=None) -> int:
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="train and evaluate the OSTR warm-start CNN")
+    ap.add_argument("--n-train", type=int, default=512)
+    ap.add_argument("--n-val", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--workers", type=int, default=8)
+    ap.add_argument("--n-time", type=int, default=4)
+    ap.add_argument("--out", default=None, help="write the trained parameters (.npz)")
+    ap.add_argument("--report", default=None, help="write the JSON report")
+    a = ap.parse_args(argv)
+    from . import native as _n
+
+    _n.load()
+    cfg = TrainConfig(n_train=a.n_train, n_val=a.n_val, steps=a.steps, batch=a.batch, lr=a.lr,
+                      workers=a.workers)
+    rep = run(cfg, a.out, n_time=a.n_time)
+    txt = json.dumps(rep, indent=1, default=float)
+    if a.report:
+        with open(a.report, "w") as f:
+            f.write(txt)
+    summary = {k: rep[k] for k in ("accept_rate", "mean_objective_gain", "mean_rmse_plain",
+                                   "mean_rmse_warm", "seconds")}
+    print(json.dumps(summary, default=float))
+    return 0
+
+
+if __name__ == "__main__":
+    import sys
+
+    sys.exit(main())
