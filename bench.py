@@ -52,6 +52,8 @@ def parse():
                     help="also time N batched reconstructions (persistent launches)")
     ap.add_argument("--batch-steps", type=int, default=25)
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-warm", action="store_true",
+                    help="skip the learned warm-start comparison")
     return ap.parse_args()
 
 
@@ -287,6 +289,8 @@ def run_ours(args):
                                "kind": "port",
                                "sample": f"{len(times)} sub-iterations of the clinical workload "
                                          f"(FP32 restatement, OpenMP), {model}"}
+    if not args.no_warm:
+        out["warm_start"] = warm_bench(cfg, plan, rank)
     if args.batch:
         out["batch"] = batch_bench(args, rank)
     if ws > 1:
@@ -360,6 +364,73 @@ def batch_bench(args, rank):
             "workload": "batch: thickness U(30,80), in-plane U(512,1024)xU(256,512) @0.14mm, "
                         "9/15/25 views over +-U(7.5,25) deg, I0 U(3e3,2e4), gland U(10,50)%, "
                         "hyperbola, 50 iterations"}
+
+
+def warm_bench(cfg, plan, rank, tol=1e-4, early=2):
+    """Time to RMSE <= tol (1/mm) against the 50-iteration volume: plain OSTR
+    vs the learned warm start (2 iterations, CNN, then iterations), both from
+    the scan already resident; plus the CNN's own throughput on this volume."""
+    import torch
+
+    from newrecon_gb300 import warmstart
+
+    path = os.path.join(HERE, "newrecon_gb300", "data", "warmstart_params.npz")
+    if not os.path.isfile(path):
+        return {"unavailable": "no trained parameters"}
+    cnn = warmstart.load(path)
+    g = cfg.geom
+    ref = torch.zeros(g.n_voxels, device="cuda")
+    plan.iterate(ref, cfg.iter_num)
+    stream = torch.cuda.current_stream()
+
+    def rmse(a):
+        return float(torch.sqrt(torch.mean((a.double() - ref.double()) ** 2)).item())
+
+    dims = (g.nx, g.ny, g.nz, 1)
+    x = torch.zeros(g.n_voxels, device="cuda")
+    plan.iterate(x, early)
+    cnn.forward(x, dims)  # warm-up (workspace, weight packing)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    xw = cnn.forward(x, dims)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    cnn.check()
+    cnn_ms = e0.elapsed_time(e1)
+    flops = g.n_voxels * 2 * 27 * (1 * 32 + 4 * 32 * 32 + 32 * 1)
+    # equal-work objective check (3 iterations after the warm start vs plain)
+    xp = x.clone()
+    plan.iterate(xp, 3)
+    plan.iterate(xw, 3)
+    obj_p, obj_w = plan.total_objective(xp), plan.total_objective(xw)
+
+    def to_tol(start_warm):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        y = torch.zeros(g.n_voxels, device="cuda")
+        its = 0
+        if start_warm:
+            plan.iterate(y, early)
+            y = cnn.forward(y, dims)
+            its = early
+        for _ in range(cfg.iter_num + 5):
+            if rmse(y) <= tol:
+                break
+            plan.iterate(y, 1)
+            its += 1
+        torch.cuda.synchronize()
+        return its, time.perf_counter() - t0, rmse(y)
+
+    ip, tp, rp = to_tol(False)
+    iw, tw, rw = to_tol(True)
+    return {"tol_per_mm": tol, "reference": f"{cfg.iter_num}-iteration plain OSTR",
+            "plain": {"iterations": ip, "seconds": tp, "rmse": rp},
+            "warm": {"iterations": iw, "seconds": tw, "rmse": rw},
+            "speedup": tp / tw if tw > 0 else None,
+            "objective_after_5_iters": {"plain": obj_p, "warm": obj_w,
+                                        "warm_accepted": obj_w <= obj_p},
+            "cnn_ms": cnn_ms, "cnn_tflops": flops / (cnn_ms / 1e3) / 1e12,
+            "cnn_flops": flops}
 
 
 def ctypes_ptr(t):
