@@ -320,6 +320,105 @@ nr_status nr_ostr_check(void* workspace, size_t ws_bytes, int32_t* flags,
 nr_status nr_penalty_fp64_static(const nr_geom* g, const float* x, int32_t potential,
                                  float delta, double* out, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * SART / OS-SART family on the same projectors.
+ * Reference-shaped operators first (drop-in for the SART launch wrappers),
+ * then the device-resident OS-SART loop (the reference's Recon_Method 3 is an
+ * empty placeholder, Tomo_OSTR_gold.cpp:1523-1525).
+ * ------------------------------------------------------------------------- */
+
+/* prj_est[(a-a0)][i][j] = Siddon line integral of x (times cos(theta) when
+ * use_cos) and normprj[(a-a0)][i][j] = the ray's in-volume chord, from one
+ * walk, views index[a], a in [a0,a1).  Rays that miss the volume leave both
+ * untouched.  Replaces fprojectCB_1R_GPU_SART (use_cos = 0,
+ * Tomo_OSTR.cu:2278-2304; kernel :1177) and fprojectCB_1R_GPU_SART_cos
+ * (use_cos = 1, :2306-2332; kernel :1245). */
+nr_status nr_fp_sart(const nr_geom* g, const float* x, float* prj_est, float* normprj,
+                     const float* angles, const int32_t* index, int32_t a0, int32_t a1,
+                     int32_t use_cos, void* stream);
+
+/* diff[k] = (prj[k] - prj_est[k]) / normprj[k] where normprj[k] != 0, else 0,
+ * for k < n (n = (a1-a0)*BINSx*BINSy for the reference's view range).
+ * Replaces SART_prj_diff (Tomo_OSTR.cu:2537-2558; kernel :2145). */
+nr_status nr_sart_prj_diff(float* diff, const float* prj, const float* prj_est,
+                           const float* normprj, int64_t n, void* stream);
+
+/* OS-SART update of x in place from the [view][i][j] difference of views
+ * index[a], a in [a0,a1): per voxel, u = sum of the depth-weighted bilinear
+ * back projection, s = the same of a detector of ones (the sensitivity);
+ * x = max(0, x + lambda (u + beta prior) / s), both terms 0 where s = 0.
+ * prior == NULL replaces bprojectCB_4B_GPU_SART (Tomo_OSTR.cu:2460-2495;
+ * kernel :1737); otherwise bprojectCB_4B_GPU_SART_R (:2497-2535; kernel
+ * :1938).  Note the sign: the reference ADDS beta * prior, and prior (below)
+ * is the penalty gradient, so a smoothing penalty takes beta < 0. */
+nr_status nr_bp_ossart(const nr_geom* g, float* x, const float* diff, const float* prior,
+                       const int32_t* index, const float* angles, int32_t a0, int32_t a1,
+                       float lambda, float beta, void* stream);
+
+/* prior += sum over the 26 neighbours of (x_j - x_k) / sqrt(1 + ((x_j - x_k)/delta)^2)
+ * / dist_k, dist_k the plain neighbour distance (no z ratio); out-of-volume
+ * neighbours count as t = 0.  delta == 0 returns NR_ERR_BAD_ARGUMENT (the
+ * reference exits).  Replaces prior_GPU_SART (Tomo_OSTR.cu:2249-2276;
+ * G_Huber_prior :258-325). */
+nr_status nr_prior_sart(const nr_geom* g, float* prior, const float* x, float delta,
+                        void* stream);
+
+/* SART input from a transmission scan: line[k] = log(blank[k] / (prj[k] - scat[k]))
+ * where prj - scat > 0 and blank > 0, else 0; scat may be NULL.  The log
+ * transform of the reference's MATLAB examples (ReconDBT/gen_dbtproj_example.m:113);
+ * the CUDA code takes line integrals as given. */
+nr_status nr_sart_line_integrals(float* line, const float* prj, const float* blank,
+                                 const float* scat, int64_t n, void* stream);
+
+typedef struct nr_sart_params {
+    int32_t subset_num;        /* M; must divide n_angles, n_angles/M <= 32      */
+    int32_t use_cos;           /* 1: the _cos projector, 0: plain line integrals */
+    int32_t regularized;       /* 1: prior_GPU_SART + backprj_OSSART_R           */
+    int32_t fp_batch;          /* Siddon steps per gather round: 2, 4, 8 (0 = 4) */
+    int32_t upd_planes;        /* z planes per update block: 8, 16, 32 (0 = 16) */
+    float lambda;              /* relaxation                                     */
+    float beta;                /* prior weight (regularized only; see the sign note above) */
+    float delta;               /* hyperbola scale, != 0 (regularized only)      */
+} nr_sart_params;
+
+/* Bytes of workspace the OS-SART loop needs. */
+nr_status nr_sart_workspace_size(const nr_geom* g, const nr_sart_params* p, size_t* bytes);
+
+/* Load the line integrals ([view][i][j], ORIGINAL view order) into the
+ * workspace in subset order and trace every ray's chord (normprj) once. */
+nr_status nr_sart_setup(const nr_geom* g, const nr_sart_params* p, const float* angles,
+                        const float* line, void* workspace, size_t ws_bytes, void* stream);
+
+/* n_iters iterations (M sub-iterations each, subset-major view order as the
+ * OSTR driver, Tomo_OSTR_gold.cpp:628-642) on x in place.  Per sub-iteration:
+ * diff = (p - FP_SART(x)) / normprj (0 where normprj = 0) over the subset, then
+ * the OS-SART update above with the prior of the current x.  The status word
+ * (NaN/Inf) is read with nr_ostr_check on this workspace. */
+nr_status nr_sart_iterate(const nr_geom* g, const nr_sart_params* p, float* x,
+                          int32_t n_iters, void* workspace, size_t ws_bytes, void* stream);
+
+/* One sub-iteration for subset a (0 <= a < M), x in place. */
+nr_status nr_sart_subiter(const nr_geom* g, const nr_sart_params* p, float* x,
+                          int32_t subset, void* workspace, size_t ws_bytes, void* stream);
+
+/* nr_sart_iterate captured once into a CUDA graph on `stream` (x and the
+ * workspace are bound into it); launch and destroy it with
+ * nr_ostr_graph_launch / nr_ostr_graph_destroy. */
+nr_status nr_sart_graph_create(const nr_geom* g, const nr_sart_params* p, float* x,
+                               int32_t n_iters, void* workspace, size_t ws_bytes,
+                               void* stream, void** graph);
+
+/* Workspace sections a caller may read (device pointer + byte size). */
+enum {
+    NR_SART_WS_LINE = 0,   /* float[A][BINSy][BINSx]: line integrals, subset order   */
+    NR_SART_WS_NORM = 1,   /* float[A][BINSy][BINSx]: chord per ray, subset order    */
+    NR_SART_WS_DIFF = 2,   /* float[Vs][BINSy][BINSx]: last subset's difference      */
+    NR_SART_WS_INDEX = 3   /* int32[A]: subset-major view order                      */
+};
+nr_status nr_sart_workspace_section(const nr_geom* g, const nr_sart_params* p,
+                                    int32_t section, void* workspace, size_t ws_bytes,
+                                    void** ptr, size_t* bytes);
+
 /* Library version string. */
 const char* nr_version(void);
 

@@ -1,6 +1,7 @@
 // elementwise.cu -- the reference's per-bin / per-voxel host helpers, on the
 // device (compute_yry, compute_gamma_yry, compute_h, update_est, the subset
-// scaling, regroup_prj and x_y_flip of Tomo_OSTR_gold.cpp:93-295).
+// scaling, regroup_prj and x_y_flip of Tomo_OSTR_gold.cpp:93-295), plus the
+// SART projection difference (Tomo_OSTR.cu:2145-2183) and log transform.
 #include "common.cuh"
 
 namespace nr {
@@ -44,6 +45,32 @@ __global__ void update_est_kernel(float* __restrict__ est, const float* __restri
          i += (int64_t)gridDim.x * blockDim.x) {
         const float v = est[i] - __fdiv_rn(capL[i] + beta * RD[i], d[i] + 2.f * beta * RDD[i]);
         est[i] = v < 0.f ? 0.f : v;
+    }
+}
+
+// SART_prj_diff_kernel, Tomo_OSTR.cu:2145-2183: (prj - est) / normprj where
+// normprj != 0, else 0.
+__global__ void prj_diff_kernel(float* __restrict__ diff, const float* __restrict__ prj,
+                                const float* __restrict__ est, const float* __restrict__ norm,
+                                int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float nv = norm[i];
+        diff[i] = nv != 0.f ? __fdiv_rn(prj[i] - est[i], nv) : 0.f;
+    }
+}
+
+// Line integrals of a transmission scan for SART: log(blank / (prj - scat))
+// where both are positive, else 0 (the log transform g = log I0 - log I of
+// the reference's MATLAB examples, ReconDBT/gen_dbtproj_example.m:113).
+__global__ void line_kernel(float* __restrict__ line, const float* __restrict__ prj,
+                           const float* __restrict__ blank, const float* __restrict__ scat,
+                           int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const float nu = prj[i] - (scat ? scat[i] : 0.f);
+        const float b = blank[i];
+        line[i] = (nu > 0.f && b > 0.f) ? logf(__fdiv_rn(b, nu)) : 0.f;
     }
 }
 
@@ -109,6 +136,22 @@ NR_API nr_status nr_compute_yry(float* yry, const float* prj, const float* scat,
     if (!yry || !prj || n < 0) return NR_ERR_BAD_ARGUMENT;
     if (n == 0) return NR_OK;
     yry_kernel<<<ew_blocks(n), 256, 0, as_stream(stream)>>>(yry, prj, scat, n);
+    return launch_status();
+}
+
+NR_API nr_status nr_sart_prj_diff(float* diff, const float* prj, const float* prj_est,
+                                  const float* normprj, int64_t n, void* stream) {
+    if (!diff || !prj || !prj_est || !normprj || n < 0) return NR_ERR_BAD_ARGUMENT;
+    if (n == 0) return NR_OK;
+    prj_diff_kernel<<<ew_blocks(n), 256, 0, as_stream(stream)>>>(diff, prj, prj_est, normprj, n);
+    return launch_status();
+}
+
+NR_API nr_status nr_sart_line_integrals(float* line, const float* prj, const float* blank,
+                                        const float* scat, int64_t n, void* stream) {
+    if (!line || !prj || !blank || n < 0) return NR_ERR_BAD_ARGUMENT;
+    if (n == 0) return NR_OK;
+    line_kernel<<<ew_blocks(n), 256, 0, as_stream(stream)>>>(line, prj, blank, scat, n);
     return launch_status();
 }
 

@@ -34,6 +34,33 @@ __global__ void __launch_bounds__(128) fp_kernel(const __grid_constant__ Geo G,
     }
 }
 
+// SART projector: est = line integral (times cos theta when COS) and norm =
+// in-volume chord of the same walk; missed rays leave both untouched
+// (ray_trace_gpu_manyangles_direct_notexturememory{,_cos},
+// Tomo_OSTR.cu:1177-1311).
+template <bool COS>
+__global__ void __launch_bounds__(128) fp_sart_kernel(const __grid_constant__ Geo G,
+                                                      const float* __restrict__ vol,
+                                                      float* __restrict__ est,
+                                                      float* __restrict__ norm,
+                                                      const float* __restrict__ angles,
+                                                      const int32_t* __restrict__ index, int a0) {
+    __shared__ ViewSrc src;
+    const nr_geom& g = G.g;
+    const int a = a0 + blockIdx.z;
+    if (threadIdx.x == 0 && threadIdx.y == 0) src = view_source(g, angles[index[a]]);
+    __syncthreads();
+    const int i = blockIdx.x * 32 + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.nbx || j >= g.nby) return;
+    float v[2];
+    if (trace<3>(G, vol, src.x0, src.y0, src.z0, bin_x(g, i), bin_y(g, j), -g.detectorR, v)) {
+        const int64_t o = (int64_t)blockIdx.z * g.nbx * g.nby + bin_off<false>(g, i, j);
+        est[o] = COS ? v[0] * src.ct : v[0];
+        norm[o] = v[1];
+    }
+}
+
 // Fused forward projection + h, one block per 32 x 4 bins of one subset view;
 // K Siddon steps per gather round.
 template <int K>
@@ -118,6 +145,23 @@ NR_API nr_status nr_fp_gamma(const nr_geom* g, float* gamma, const float* angles
     else
         fp_kernel<1, false><<<grd, blk, 0, as_stream(stream)>>>(make_geo(*g), nullptr, gamma,
                                                                 angles, index, a0);
+    return launch_status();
+}
+
+NR_API nr_status nr_fp_sart(const nr_geom* g, const float* x, float* prj_est, float* normprj,
+                            const float* angles, const int32_t* index, int32_t a0, int32_t a1,
+                            int32_t use_cos, void* stream) {
+    nr_status st = check_views(g, angles, index, a0, a1);
+    if (st != NR_OK) return st;
+    if (!x || !prj_est || !normprj || prj_est == normprj) return NR_ERR_BAD_ARGUMENT;
+    if (a1 == a0) return NR_OK;
+    dim3 blk(32, 4), grd(cdiv(g->nbx, 32), cdiv(g->nby, 4), a1 - a0);
+    if (use_cos)
+        fp_sart_kernel<true><<<grd, blk, 0, as_stream(stream)>>>(make_geo(*g), x, prj_est, normprj,
+                                                                 angles, index, a0);
+    else
+        fp_sart_kernel<false><<<grd, blk, 0, as_stream(stream)>>>(make_geo(*g), x, prj_est,
+                                                                  normprj, angles, index, a0);
     return launch_status();
 }
 

@@ -141,6 +141,18 @@ __global__ void clear_status_kernel(int* s) {
     if (threadIdx.x < 64) s[threadIdx.x] = 0;
 }
 
+// The two set-up launches the OS-SART driver (sart.cu) shares.
+nr_status launch_subset_index(int32_t* idx, const float* angles_in, float* angles_out, int A,
+                              int M, cudaStream_t s) {
+    index_kernel<<<1, 256, 0, s>>>(idx, angles_in, angles_out, A, M);
+    return launch_status();
+}
+
+nr_status launch_clear_status(int* status, cudaStream_t s) {
+    clear_status_kernel<<<1, 64, 0, s>>>(status);
+    return launch_status();
+}
+
 // Section pointers of a set-up workspace, for the batched path (batch.cu).
 nr_status ostr_sections(const nr_geom* g, const nr_ostr_params* p, void* ws, size_t bytes,
                         float** xtmp, float** h, const float** d, const float** y,

@@ -101,6 +101,25 @@ __global__ void __launch_bounds__(128) prior_kernel(const __grid_constant__ Geo 
     RD[v] = RD[v] + rd;
 }
 
+// The SART prior gradient: prior += sum_k t/sqrt(1+(t/delta)^2) / dist_k with
+// plain neighbour distances (G_Huber_prior, Tomo_OSTR.cu:258-325; W built
+// with z ratio 1).  The RDD sums of prior_sums are dead here and drop out.
+__global__ void __launch_bounds__(128) prior_grad_kernel(const __grid_constant__ Geo G,
+                                                         const __grid_constant__ PriorW W,
+                                                         float* __restrict__ prior,
+                                                         const float* __restrict__ x,
+                                                         float delta) {
+    const nr_geom& g = G.g;
+    const int ix = blockIdx.x * 32 + threadIdx.x;
+    const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    const int iz = blockIdx.z;
+    if (ix >= g.nx || iy >= g.ny) return;
+    const int64_t v = ((int64_t)iz * g.ny + iy) * g.nx + ix;
+    float rdd, rd;
+    prior_sums<NR_POT_HYPERBOLA>(g, W, x, ix, iy, iz, x[v], delta, 1.f / delta, &rdd, &rd);
+    prior[v] = prior[v] + rd;
+}
+
 template <int POT>
 static nr_status launch_prior_t(const nr_geom& g, float* RDD, float* RD, const float* x,
                                 float delta, float zxy, cudaStream_t st) {
@@ -184,4 +203,16 @@ NR_API nr_status nr_prior(const nr_geom* g, float* RDD, float* RD, const float* 
     if (g->nz > 65535) return NR_ERR_BAD_GEOMETRY;
     return launch_prior(*g, potential, RDD, RD, x, potential == NR_POT_Q2 ? 1.f : delta,
                         z_xy_ratio, as_stream(stream));
+}
+
+NR_API nr_status nr_prior_sart(const nr_geom* g, float* prior, const float* x, float delta,
+                               void* stream) {
+    if (!geom_ok(g)) return NR_ERR_BAD_GEOMETRY;
+    if (!prior || !x || prior == x) return NR_ERR_BAD_ARGUMENT;
+    if (delta == 0.f || !(delta == delta)) return NR_ERR_BAD_ARGUMENT;  // Tomo_OSTR.cu:2260-2263
+    if (g->nz > 65535) return NR_ERR_BAD_GEOMETRY;
+    dim3 blk(32, 4), grd(cdiv(g->nx, 32), cdiv(g->ny, 4), g->nz);
+    prior_grad_kernel<<<grd, blk, 0, as_stream(stream)>>>(make_geo(*g), make_weights(1.f), prior,
+                                                          x, delta);
+    return launch_status();
 }

@@ -59,7 +59,9 @@ __device__ __forceinline__ Axis axis_setup(float e, float d, float L, int n, flo
 }
 
 // Traces the ray (x0,y0,z0) -> (x1,y1,z1).  MODE 0: sum_j len_j * vol_j;
-// MODE 1: in-volume chord length; MODE 2: full length |src - bin|.
+// MODE 1: in-volume chord length; MODE 2: full length |src - bin|; MODE 3:
+// out[0] = the MODE 0 sum and out[1] = the chord, from one walk (the sum and
+// sum_norm of rayTrace3D_GPU_direct_notexturememory, Tomo_OSTR.cu:327-610).
 // Returns false when the ray misses the volume (the reference's status -1).
 //
 // MODE 0 walks in batches of K steps: the voxel indices and chord lengths of
@@ -115,6 +117,7 @@ __device__ __forceinline__ bool trace(const Geo& G, const float* __restrict__ vo
         *out = smax;
         return true;
     }
+    if (MODE == 3) out[1] = smax;
     const int sx = ax.dir, sy = ay.dir * g.nx, sz = az.dir * g.nx * g.ny;
     int idx = (az.idx * g.ny + ay.idx) * g.nx + ax.idx;
     float tx = ax.first, ty = ay.first, tz = az.first;

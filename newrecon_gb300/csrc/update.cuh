@@ -118,6 +118,11 @@ __device__ __forceinline__ void prior_all(std::integer_sequence<int, Ks...>,
     *rd = b0 + b1;
 }
 
+// Kinds of fused update (template argument KIND of update_tile).
+constexpr int UPD_OSTR = 0;     // OSTR step above
+constexpr int UPD_SART = 1;     // OS-SART, backprj_OSSART_gpu_manyviews (Tomo_OSTR.cu:1737-1936)
+constexpr int UPD_SART_R = 2;   // OS-SART with the hyperbola prior, backprj_OSSART_R (:1938-2143)
+
 // Shared memory of one update tile: the 3-plane ring and the subset's sources.
 struct UpdSmem {
     float tile[3][UPLANE];
@@ -131,7 +136,15 @@ struct UpdSmem {
 // shared-memory load at a fixed offset.  The global loads of plane z+2 are
 // issued before plane z is computed (register prefetch), so they overlap the
 // arithmetic.  Writes x_out; flags non-finite values.
-template <int POT, int ZC = UZC>
+//
+// KIND = UPD_SART / UPD_SART_R turn the same tile into the OS-SART update:
+// h is the normalised projection difference of the subset, the back
+// projection also sums the interpolation weights (the sensitivity), and
+//     x' = max(0, x + lambda (sum_u + beta RD) / sum_sens)   (0 where sum_sens = 0)
+// with lambda passed in M, RD the hyperbola gradient of x with unit
+// neighbour distances (G_Huber_prior, Tomo_OSTR.cu:258-325; W built with
+// z ratio 1) for UPD_SART_R, and d unused.
+template <int POT, int ZC = UZC, int KIND = UPD_OSTR>
 __device__ __forceinline__ void update_tile(
     const Geo& G, const PriorW5& W, const float* __restrict__ x, float* __restrict__ x_out,
     const float* __restrict__ d, const float* __restrict__ h, const float* __restrict__ angles,
@@ -194,12 +207,12 @@ __device__ __forceinline__ void update_tile(
         if (z + 1 < ze) fetch(z + 2, n0, n1);
         if (active) {
             const int64_t v = (int64_t)z * plane + (int64_t)iy * g.nx + ix;
-            const float dv = __ldg(d + v);
+            const float dv = KIND == UPD_OSTR ? __ldg(d + v) : 0.f;
             const float xc = pc[r * USW + c];
             const float z1 = vox_z(g, z);
             // M * SBP(h): the arithmetic of bp.cu's sbp_term on the [j][i]
             // layout, with reciprocal multiplies in place of divisions.
-            float capL = 0.f;
+            float capL = 0.f, sens = 0.f;
             for (int t = 0; t < nv; t++) {
                 const ViewSrc vs = sv[t];
                 const float ddx = vs.x0 - x1, ddy = vs.y0 - y1, ddz = vs.z0 - z1;
@@ -222,23 +235,50 @@ __device__ __forceinline__ void update_tile(
                 const bool j0 = (jlb < g.nby) && (jlb >= 0);
                 const bool j1 = (jlb < g.nby - 1) && (jlb >= -1);
                 float d1 = 0.f, d2 = 0.f;
+                float s1 = 0.f, s2 = 0.f;  // sensitivity taps (OS-SART only)
                 const int64_t r0 = (int64_t)jlb * g.nbx, r1 = r0 + g.nbx;
-                if (i0 && j0) d1 = (1.f - fracI) * __ldg(p + r0 + ilb);
-                if (i1 && j0) d1 = d1 + fracI * __ldg(p + r0 + ilb + 1);
-                if (i0 && j1) d2 = (1.f - fracI) * __ldg(p + r1 + ilb);
-                if (i1 && j1) d2 = d2 + fracI * __ldg(p + r1 + ilb + 1);
+                if (i0 && j0) {
+                    d1 = (1.f - fracI) * __ldg(p + r0 + ilb);
+                    s1 = 1.f - fracI;
+                }
+                if (i1 && j0) {
+                    d1 = d1 + fracI * __ldg(p + r0 + ilb + 1);
+                    s1 = s1 + fracI;
+                }
+                if (i0 && j1) {
+                    d2 = (1.f - fracI) * __ldg(p + r1 + ilb);
+                    s2 = 1.f - fracI;
+                }
+                if (i1 && j1) {
+                    d2 = d2 + fracI * __ldg(p + r1 + ilb + 1);
+                    s2 = s2 + fracI;
+                }
                 capL = capL + ((1.f - fracJ) * d1 + fracJ * d2) * g.vz * dw;
+                if (KIND != UPD_OSTR) sens = sens + ((1.f - fracJ) * s1 + fracJ * s2) * g.vz * dw;
             }
-            capL = M * capL;
-            float rdd, rd;
+            float rdd = 0.f, rd = 0.f;
             const int base = r * USW + c;
-            if (edge_xy || z == 0 || z == g.nz - 1)
-                prior_all<POT, true>(std::make_integer_sequence<int, 27>{}, pb, pc, pa, base, xc, W,
-                                     delta, inv_delta, &rdd, &rd);
-            else
-                prior_all<POT, false>(std::make_integer_sequence<int, 27>{}, pb, pc, pa, base, xc, W,
-                                      delta, inv_delta, &rdd, &rd);
-            const float xn = xc - __fdividef(capL + beta * rd, dv + 2.f * beta * rdd);
+            if (KIND != UPD_SART) {
+                if (edge_xy || z == 0 || z == g.nz - 1)
+                    prior_all<POT, true>(std::make_integer_sequence<int, 27>{}, pb, pc, pa, base,
+                                         xc, W, delta, inv_delta, &rdd, &rd);
+                else
+                    prior_all<POT, false>(std::make_integer_sequence<int, 27>{}, pb, pc, pa, base,
+                                          xc, W, delta, inv_delta, &rdd, &rd);
+            }
+            float xn;
+            if (KIND == UPD_OSTR) {
+                capL = M * capL;
+                xn = xc - __fdividef(capL + beta * rd, dv + 2.f * beta * rdd);
+            } else {
+                // Tomo_OSTR.cu:2193-2205: u/sens and beta*prior/sens, 0 without sensitivity
+                float ut = 0.f, bt = 0.f;
+                if (sens != 0.f) {
+                    ut = __fdiv_rn(capL, sens);
+                    if (KIND == UPD_SART_R) bt = __fdiv_rn(beta * rd, sens);
+                }
+                xn = xc + M * (ut + bt);
+            }
             if (!(fabsf(xn) < __int_as_float(0x7f800000))) atomicOr(status, NR_FLAG_NONFINITE);
             x_out[v] = xn < 0.f ? 0.f : xn;
         }

@@ -89,6 +89,14 @@ def read_string(path: str, label: str) -> str:
     return _find(_tokens(path), label, 1, path)[0]
 
 
+def read_optional(path: str, label: str, kind: str, default):
+    """An optional parameter: default when the label is absent, else as read_int /
+    read_float (a malformed value still raises)."""
+    if label not in _tokens(path):
+        return default
+    return read_int(path, label) if kind == "int" else read_float(path, label)
+
+
 @dataclasses.dataclass
 class DatConfig:
     """Every parameter ``main`` reads (Tomo_OSTR.cu:2578-2650)."""
@@ -111,6 +119,12 @@ class DatConfig:
     output_recon_folder: str
     output_recon_name: str
     launch: dict  # the reference's launch-shape parameters (read, not needed here)
+    # OS-SART (Recon_Method 3), optional labels with no reference counterpart:
+    # SART_lambda (relaxation, default 1), SART_use_cos (default 1) and
+    # SART_beta (prior weight, default 0 = no prior; the prior uses Delta)
+    sart_lambda: float = 1.0
+    sart_use_cos: int = 1
+    sart_beta: float = 0.0
 
 
 def load(path: str) -> DatConfig:
@@ -137,7 +151,10 @@ def load(path: str) -> DatConfig:
                     projection_name=rs("projection_name"), scatter_folder=rs("scatter_folder"),
                     scatter_name=rs("scatter_name"), blank_folder=rs("blank_folder"),
                     blank_name=rs("blank_name"), output_recon_folder=rs("output_recon_folder"),
-                    output_recon_name=rs("output_recon_name"), launch=launch)
+                    output_recon_name=rs("output_recon_name"), launch=launch,
+                    sart_lambda=read_optional(path, "SART_lambda", "float", 1.0),
+                    sart_use_cos=read_optional(path, "SART_use_cos", "int", 1),
+                    sart_beta=read_optional(path, "SART_beta", "float", 0.0))
     if cfg.subset_num <= 0 or g.n_angles % cfg.subset_num != 0:
         # Tomo_OSTR.cu:2627-2630
         raise DatFileError("Error!! subset_number is not a divisor of angular_samples.")
@@ -163,7 +180,8 @@ def write(path: str, cfg: DatConfig) -> None:
              ("projection_name", cfg.projection_name), ("scatter_folder", cfg.scatter_folder),
              ("scatter_name", cfg.scatter_name), ("blank_folder", cfg.blank_folder),
              ("blank_name", cfg.blank_name), ("output_recon_folder", cfg.output_recon_folder),
-             ("output_recon_name", cfg.output_recon_name)]
+             ("output_recon_name", cfg.output_recon_name), ("SART_lambda", cfg.sart_lambda),
+             ("SART_use_cos", cfg.sart_use_cos), ("SART_beta", cfg.sart_beta)]
     with open(path, "w") as f:
         for k, v in rows:
             f.write(f"{k}\t{v!r}\n" if isinstance(v, float) else f"{k}\t{v}\n")

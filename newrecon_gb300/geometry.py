@@ -47,6 +47,17 @@ class NrOstrParams(ctypes.Structure):
     ]
 
 
+class NrSartParams(ctypes.Structure):
+    """ctypes image of ``nr_sart_params`` (include/nrgb300.h)."""
+
+    _fields_ = [
+        ("subset_num", ctypes.c_int32), ("use_cos", ctypes.c_int32),
+        ("regularized", ctypes.c_int32), ("fp_batch", ctypes.c_int32),
+        ("upd_planes", ctypes.c_int32), ("lam", ctypes.c_float),
+        ("beta", ctypes.c_float), ("delta", ctypes.c_float),
+    ]
+
+
 class NrBatchCase(ctypes.Structure):
     """ctypes image of ``nr_batch_case`` (include/nrgb300.h)."""
 

@@ -10,7 +10,7 @@ import os
 import threading
 from typing import Optional
 
-from .geometry import NrGeom, NrOstrParams
+from .geometry import NrGeom, NrOstrParams, NrSartParams
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libnrgb300.so")
 
@@ -32,6 +32,7 @@ _I64 = ctypes.c_int64
 _F = ctypes.c_float
 _GP = ctypes.POINTER(NrGeom)
 _PP = ctypes.POINTER(NrOstrParams)
+_SP = ctypes.POINTER(NrSartParams)
 SIGNATURES = {
     "nr_validate_geometry": (_I32, [_GP, _I32]),
     "nr_fp_ostr": (_I32, [_GP, _P, _P, _P, _P, _I32, _I32, _P]),
@@ -74,6 +75,20 @@ SIGNATURES = {
     "nr_cnn_check": (_I32, [_P, ctypes.POINTER(_I32), _P]),
     "nr_ostr_check": (_I32, [_P, ctypes.c_size_t, ctypes.POINTER(_I32), _P]),
     "nr_penalty_fp64_static": (_I32, [_GP, _P, _I32, _F, _P, _P]),
+    "nr_fp_sart": (_I32, [_GP, _P, _P, _P, _P, _P, _I32, _I32, _I32, _P]),
+    "nr_sart_prj_diff": (_I32, [_P, _P, _P, _P, _I64, _P]),
+    "nr_bp_ossart": (_I32, [_GP, _P, _P, _P, _P, _P, _I32, _I32, _F, _F, _P]),
+    "nr_prior_sart": (_I32, [_GP, _P, _P, _F, _P]),
+    "nr_sart_line_integrals": (_I32, [_P, _P, _P, _P, _I64, _P]),
+    "nr_sart_workspace_size": (_I32, [_GP, _SP, ctypes.POINTER(ctypes.c_size_t)]),
+    "nr_sart_setup": (_I32, [_GP, _SP, _P, _P, _P, ctypes.c_size_t, _P]),
+    "nr_sart_iterate": (_I32, [_GP, _SP, _P, _I32, _P, ctypes.c_size_t, _P]),
+    "nr_sart_subiter": (_I32, [_GP, _SP, _P, _I32, _P, ctypes.c_size_t, _P]),
+    "nr_sart_graph_create": (_I32, [_GP, _SP, _P, _I32, _P, ctypes.c_size_t, _P,
+                                    ctypes.POINTER(ctypes.c_void_p)]),
+    "nr_sart_workspace_section": (_I32, [_GP, _SP, _I32, _P, ctypes.c_size_t,
+                                         ctypes.POINTER(ctypes.c_void_p),
+                                         ctypes.POINTER(ctypes.c_size_t)]),
     "nr_version": (ctypes.c_char_p, []),
 }
 

@@ -2,12 +2,16 @@
 ``Tomo_OSTR <datafile>`` command on the GPU path.
 
 Reads the parameter file and the per-view raw scans (``datfile``), flips them
-to the in-memory layout on the GPU, runs OSTR with ``Recon_Method`` 0 (Q2
-prior) or 1 (Lange prior) -- the two methods ``Reconstruction()`` dispatches
-(``Tomo_OSTR_gold.cpp:1493-1528``) -- from the initial guess as stored when
-it can be read (else 0; ``Tomo_OSTR_gold.cpp:567-589``), and writes the volume every ``Readout_Every_X_Iters``
-iterations.  ``Readout_Every_X_Iters`` <= 0 (a modulo by zero in the
-reference) writes the last iteration only.
+to the in-memory layout on the GPU, runs ``Recon_Method`` 0 (OSTR, Q2 prior)
+or 1 (OSTR, Lange prior) -- the two methods ``Reconstruction()`` dispatches
+(``Tomo_OSTR_gold.cpp:1493-1528``) -- or 3, OS-SART, which the reference
+leaves empty there: the scans become line integrals log(blank/(prj-scatter))
+and the device-resident OS-SART loop runs with the optional labels
+SART_lambda / SART_use_cos / SART_beta (and Delta for the prior).  Every
+method starts from the initial guess as stored when it can be read (else 0;
+``Tomo_OSTR_gold.cpp:567-589``) and writes the volume every
+``Readout_Every_X_Iters`` iterations.  ``Readout_Every_X_Iters`` <= 0 (a
+modulo by zero in the reference) writes the last iteration only.
 """
 from __future__ import annotations
 
@@ -18,17 +22,18 @@ from typing import List
 import numpy as np
 import torch
 
-from . import datfile, native, ostr
+from . import datfile, native, ostr, sart
 
-METHODS = {0: "q2", 1: "lange"}
+METHODS = {0: "q2", 1: "lange", 3: "ossart"}
 
 
 def run(path: str, log=print) -> List[str]:
     """Runs the reconstruction a parameter file describes; returns the files written."""
     cfg = datfile.load(path)
     if cfg.recon_method not in METHODS:
-        # Tomo_OSTR_gold.cpp:1521-1524: methods 2 and 3 are empty placeholders
-        raise datfile.DatFileError(f"Recon_Method {cfg.recon_method}: only 0 (Q2) and 1 (Lange)")
+        # Tomo_OSTR_gold.cpp:1519-1520: method 2 (convex OSEM) is an empty placeholder
+        raise datfile.DatFileError(
+            f"Recon_Method {cfg.recon_method}: only 0 (OSTR Q2), 1 (OSTR Lange), 3 (OS-SART)")
     g = cfg.geom
     g.validate(cfg.subset_num)
     t0 = time.perf_counter()
@@ -43,9 +48,15 @@ def run(path: str, log=print) -> List[str]:
         native.call("nr_x_y_flip", ostr._p(flipped), ostr._p(t), g.nbx, g.nby, g.n_angles,
                     ostr._stream())
         raw[key] = flipped
-    plan = ostr.OSTR(g, subset_num=cfg.subset_num, beta=cfg.beta, delta=cfg.delta,
-                     potential=METHODS[cfg.recon_method], has_scatter=True)
-    plan.setup(angles, raw["prj"], raw["blank"], raw["scat"])
+    if cfg.recon_method == 3:
+        plan = sart.OSSART(g, subset_num=cfg.subset_num, lam=cfg.sart_lambda,
+                           use_cos=bool(cfg.sart_use_cos), regularized=cfg.sart_beta != 0,
+                           beta=cfg.sart_beta, delta=cfg.delta)
+        plan.setup(angles, sart.line_integrals(raw["prj"], raw["blank"], raw["scat"]))
+    else:
+        plan = ostr.OSTR(g, subset_num=cfg.subset_num, beta=cfg.beta, delta=cfg.delta,
+                         potential=METHODS[cfg.recon_method], has_scatter=True)
+        plan.setup(angles, raw["prj"], raw["blank"], raw["scat"])
     x0 = datfile.read_volume(cfg.ini_guess, g.n_voxels)
     x = (torch.zeros(g.n_voxels, device="cuda") if x0 is None
          else torch.from_numpy(x0).cuda())

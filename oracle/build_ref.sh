@@ -4,14 +4,17 @@
 # they lie (nothing is copied into this repository):
 #   Tomo_OSTR.cu       18-116  host globals and __constant__ geometry
 #                     118-325  G_Q2_prior, G_Fessler_prior, G_Huber_prior
+#                     327-610  Siddon device function of the SART projector
 #                     612-1173 Siddon device functions (OSTR, normprj)
+#                    1177-1311 SART projector kernels (plain and _cos)
 #                    1313-1449 OSTR_cos and normprj kernels
 #                    1553-1735 backprj_gpu_manyviews_SBP
+#                    1737-2183 backprj_OSSART{,_R}_gpu_manyviews, SART_prj_diff_kernel
 #   Tomo_OSTR_gold.cpp 22-1528 I/O, compute_yry/h, regroup, update_est,
 #                              both OSTR drivers, import_param, Reconstruction
-# The rest of Tomo_OSTR.cu (SART/4R kernels with undefined symbols, launch
+# The rest of Tomo_OSTR.cu (the 4R kernels with undefined symbols, launch
 # wrappers with <<< >>>, main) is left out; ref/ref_launch.inc stands in for the
-# five launch wrappers the driver calls.  Tomo_OSTR.h / readdata.h /
+# launch wrappers.  Tomo_OSTR.h / readdata.h /
 # helper_cuda.h are absent from the reference, so their includes (the first
 # lines of each file) are skipped.
 set -euo pipefail
@@ -25,7 +28,8 @@ fi
 mkdir -p "$OUT"
 {
     echo '#include "ref_shim.h"'
-    sed -n '18,116p;118,325p;612,1173p;1313,1449p;1553,1735p' "$REF/Tomo_OSTR.cu"
+    sed -n '18,116p;118,325p;327,610p;612,1173p;1177,1311p;1313,1449p;1553,1735p;1737,2183p' \
+        "$REF/Tomo_OSTR.cu"
     cat "$HERE/ref/ref_launch.inc"
     sed -n '22,1528p' "$REF/Tomo_OSTR_gold.cpp"
     cat "$HERE/ref/ref_api.inc"

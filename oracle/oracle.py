@@ -18,7 +18,7 @@ from typing import Optional
 
 import numpy as np
 
-from newrecon_gb300.geometry import Geometry, NrOstrParams, POTENTIALS, GAMMA_MODES
+from newrecon_gb300.geometry import Geometry, NrOstrParams, NrSartParams, POTENTIALS, GAMMA_MODES
 
 from .build import ORACLE_SO, REF_SO
 
@@ -174,6 +174,69 @@ class Oracle:
                             _ptr(None if scat_sub is None else self._arr(scat_sub)),
                             _ptr(self._arr(d)), _ptr(x))
 
+    # --- SART family -------------------------------------------------------
+    def fp_sart(self, g: Geometry, x, angles, index, a0: int, a1: int, use_cos: bool,
+                est=None, norm=None):
+        """(est, norm) of the SART projector; missed rays keep est/norm's values."""
+        x = self._arr(x).ravel()
+        n = (a1 - a0) * g.n_bins
+        est = np.zeros(n, self.dtype) if est is None else est
+        norm = np.zeros(n, self.dtype) if norm is None else norm
+        gc = g.to_c()
+        self._fn("fp_sart")(ctypes.byref(gc), _ptr(x), _ptr(est), _ptr(norm),
+                            _ptr(np.ascontiguousarray(angles, np.float32)),
+                            _ptr(np.ascontiguousarray(index, np.int32)),
+                            ctypes.c_int(a0), ctypes.c_int(a1), ctypes.c_int(int(bool(use_cos))))
+        return est, norm
+
+    def sart_prj_diff(self, prj, est, norm) -> np.ndarray:
+        prj, est, norm = self._arr(prj).ravel(), self._arr(est).ravel(), self._arr(norm).ravel()
+        out = np.empty_like(prj)
+        self._fn("sart_prj_diff")(_ptr(out), _ptr(prj), _ptr(est), _ptr(norm),
+                                  ctypes.c_int64(prj.size))
+        return out
+
+    def bp_ossart(self, g: Geometry, x, diff, index, angles, a0: int, a1: int, lam: float,
+                  prior=None, beta: float = 0.0) -> np.ndarray:
+        """OS-SART update of a copy of x."""
+        x = self._arr(x).ravel().copy()
+        gc = g.to_c()
+        self._fn("bp_ossart")(ctypes.byref(gc), _ptr(x), _ptr(self._arr(diff).ravel()),
+                              _ptr(None if prior is None else self._arr(prior).ravel()),
+                              _ptr(np.ascontiguousarray(index, np.int32)),
+                              _ptr(np.ascontiguousarray(angles, np.float32)),
+                              ctypes.c_int(a0), ctypes.c_int(a1), ctypes.c_double(lam),
+                              ctypes.c_double(beta))
+        return x
+
+    def prior_sart(self, g: Geometry, x, delta: float, prior=None) -> np.ndarray:
+        prior = np.zeros(g.n_voxels, self.dtype) if prior is None else prior
+        gc = g.to_c()
+        self._fn("prior_sart")(ctypes.byref(gc), _ptr(prior), _ptr(self._arr(x).ravel()),
+                               ctypes.c_double(delta))
+        return prior
+
+    def line_integrals(self, prj, blank, scat=None) -> np.ndarray:
+        prj, blank = self._arr(prj).ravel(), self._arr(blank).ravel()
+        scat = None if scat is None else self._arr(scat).ravel()
+        out = np.empty_like(prj)
+        self._fn("line_integrals")(_ptr(out), _ptr(prj), _ptr(blank), _ptr(scat),
+                                   ctypes.c_int64(prj.size))
+        return out
+
+    def ossart(self, g: Geometry, angles, line, *, subset_num: int, iter_num: int, lam: float,
+               use_cos: bool = True, regularized: bool = False, beta: float = 0.0,
+               delta: float = 1.0, x0=None) -> np.ndarray:
+        """The OS-SART loop (nr_sart_iterate's semantics)."""
+        p = NrSartParams(subset_num, int(bool(use_cos)), int(bool(regularized)), 0, 0, lam, beta,
+                         delta)
+        gc = g.to_c()
+        x = np.zeros(g.n_voxels, self.dtype) if x0 is None else self._arr(x0).ravel().copy()
+        self._fn("ossart")(ctypes.byref(gc), ctypes.byref(p),
+                           _ptr(np.ascontiguousarray(angles, np.float32)),
+                           _ptr(self._arr(line).ravel()), _ptr(x), ctypes.c_int(iter_num))
+        return x
+
     def objective(self, g: Geometry, angles, prj, blank, x, *, potential, delta, scat=None):
         """FP64 objective parts (data, penalty); total = data + beta * penalty."""
         p = NrOstrParams(1, POTENTIALS[potential] if isinstance(potential, str) else int(potential),
@@ -253,6 +316,63 @@ class Reference:
         out = np.zeros(self.g.n_voxels, np.float32)
         self.lib.ref_prior_hyperbola_grad(_ptr(out), _ptr(self._f(x)), ctypes.c_float(delta))
         return out
+
+    def fp_sart(self, x, angles, index, a0, a1, use_cos, est=None, norm=None):
+        g = self.g
+        n = (a1 - a0) * g.n_bins
+        est = np.zeros(n, np.float32) if est is None else self._f(est)
+        norm = np.zeros(n, np.float32) if norm is None else self._f(norm)
+        self.lib.ref_fp_sart(_ptr(self._f(x)), _ptr(est), _ptr(norm), _ptr(self._f(angles)),
+                             _ptr(np.ascontiguousarray(index, np.int32)), ctypes.c_int(a0),
+                             ctypes.c_int(a1), ctypes.c_int(int(bool(use_cos))))
+        return est, norm
+
+    def sart_prj_diff(self, prj, est, norm, index, a0, a1):
+        out = np.zeros(np.size(prj), np.float32)
+        self.lib.ref_sart_prj_diff(_ptr(out), _ptr(self._f(prj)), _ptr(self._f(est)),
+                                   _ptr(self._f(norm)),
+                                   _ptr(np.ascontiguousarray(index, np.int32)),
+                                   ctypes.c_int(a0), ctypes.c_int(a1))
+        return out
+
+    def bp_ossart(self, x, diff, index, angles, a0, a1, lam, prior=None, beta=0.0):
+        x = self._f(x)
+        self.lib.ref_bp_ossart(_ptr(x), _ptr(self._f(diff)),
+                               _ptr(None if prior is None else self._f(prior)),
+                               _ptr(np.ascontiguousarray(index, np.int32)), _ptr(self._f(angles)),
+                               ctypes.c_int(a0), ctypes.c_int(a1), ctypes.c_float(lam),
+                               ctypes.c_float(beta))
+        return x
+
+    def prior_sart(self, x, delta):
+        out = np.zeros(self.g.n_voxels, np.float32)
+        self.lib.ref_prior_sart(_ptr(out), _ptr(self._f(x)), ctypes.c_float(delta))
+        return out
+
+    def ossart(self, angles, line, *, subset_num, iter_num, lam, use_cos=True,
+               regularized=False, beta=0.0, delta=1.0, x0=None):
+        """OS-SART composed from the reference's own SART launch wrappers.
+
+        The reference has no OS-SART driver (Recon_Method 3 is empty), so this
+        loop is the composition the kernels imply, in the OSTR driver's subset
+        order: per subset, est/norm zeroed, fprojectCB_1R_GPU_SART[_cos],
+        SART_prj_diff, [prior zeroed + prior_GPU_SART], bprojectCB_4B_GPU_SART[_R].
+        """
+        g = self.g
+        A, M = g.n_angles, subset_num
+        Vs, B = A // M, g.n_bins
+        idx = np.arange(A, dtype=np.int32)
+        ridx = np.concatenate([idx[i::M] for i in range(M)]).astype(np.int32)
+        lr = np.asarray(line, np.float32).reshape(A, B)[ridx]
+        x = np.zeros(g.n_voxels, np.float32) if x0 is None else self._f(x0)
+        for _ in range(iter_num):
+            for a in range(M):
+                a0, a1 = a * Vs, (a + 1) * Vs
+                est, norm = self.fp_sart(x, angles, ridx, a0, a1, use_cos)
+                diff = self.sart_prj_diff(lr[a0:a1].ravel(), est, norm, ridx, a0, a1)
+                prior = self.prior_sart(x, delta) if regularized else None
+                x = self.bp_ossart(x, diff, ridx, angles, a0, a1, lam, prior, beta)
+        return x
 
     def compute_yry(self, prj, scat):
         out = np.zeros(np.size(prj), np.float32)

@@ -210,60 +210,211 @@ void fp_views(const nr_geom& g, const R* vol, R* prj, const float* angles,
     }
 }
 
-// Voxel-driven bilinear back projection, accumulated into vol.
-// Restates backprj_gpu_manyviews_SBP, Tomo_OSTR.cu:1553-1734 (tap edge rules
-// :1684-1715, depth weight :1634, Vsize_z*depth_weight scaling :1718).
+// One view's depth-weighted bilinear back projection term for voxel centre
+// (x1,y1,z1) from source (x0,y0,z0), reading the [i][j] view p.  Restates the
+// per-view body of backprj_gpu_manyviews_SBP, Tomo_OSTR.cu:1553-1734 (tap
+// edge rules :1684-1715, depth weight :1634, Vsize_z*depth_weight scaling
+// :1718); *sens gets the same interpolation of a detector of ones, the
+// sensitivity of backprj_OSSART_gpu_manyviews (Tomo_OSTR.cu:1838-1882).
+// Returns false (and contributes nothing) when z1 == z0.
+template <class R>
+inline bool bp_term(const nr_geom& g, R x0, R y0, R z0, R x1, R y1, R z1, const R* p,
+                    R* u_out, R* sens_out) {
+    typedef RT<R> M;
+    const int NBX = g.nbx, NBY = g.nby;
+    const R detR = (R)g.detectorR;
+    const R depth_weight = (x0 * x0 + y0 * y0 + z0 * z0) /
+        ((x0 - x1) * (x0 - x1) + (y0 - y1) * (y0 - y1) + (z0 - z1) * (z0 - z1));
+    if (z1 == z0) return false;
+    const R t = (-detR - z0) / (z1 - z0);
+    const R x2 = x0 + (x1 - x0) * t;
+    const R y2 = y0 + (y1 - y0) * t;
+    const R imb = (x2 - (R)g.x_d0) / (R)g.bx;
+    const R jmb = (y2 - (R)g.y_d0) / (R)g.by;
+    int ilb = (int)M::floor_(imb);
+    if ((double)imb < ilb + 0.5) ilb = ilb - 1;
+    int jlb = (int)M::floor_(jmb);
+    if ((double)jmb < jlb + 0.5) jlb = jlb - 1;
+    const R fracI = (R)((double)imb - (ilb + 0.5));
+    const R fracJ = (R)((double)jmb - (jlb + 0.5));
+    R d1 = 0, d2 = 0, s1 = 0, s2 = 0;
+    if (ilb < NBX && ilb >= 0 && jlb < NBY && jlb >= 0) {
+        d1 = (1 - fracI) * p[(size_t)ilb * NBY + jlb];
+        s1 = (1 - fracI);
+    }
+    if (ilb < NBX - 1 && ilb >= -1 && jlb < NBY && jlb >= 0) {
+        d1 = d1 + fracI * p[(size_t)(ilb + 1) * NBY + jlb];
+        s1 = s1 + fracI;
+    }
+    if (ilb < NBX && ilb >= 0 && jlb < NBY - 1 && jlb >= -1) {
+        d2 = (1 - fracI) * p[(size_t)ilb * NBY + jlb + 1];
+        s2 = (1 - fracI);
+    }
+    if (ilb < NBX - 1 && ilb >= -1 && jlb < NBY - 1 && jlb >= -1) {
+        d2 = d2 + fracI * p[(size_t)(ilb + 1) * NBY + jlb + 1];
+        s2 = s2 + fracI;
+    }
+    R u_term = (1 - fracJ) * d1 + fracJ * d2;
+    *u_out = u_term * (R)g.vz * depth_weight;
+    if (sens_out) {
+        R u_sens = (1 - fracJ) * s1 + fracJ * s2;
+        *sens_out = u_sens * (R)g.vz * depth_weight;
+    }
+    return true;
+}
+
+// Source of view angle theta and voxel centre (ix, iy, iz), as the back
+// projectors form them (Tomo_OSTR.cu:1613-1626).
+template <class R>
+inline void bp_geometry(const nr_geom& g, float theta_f, int ix, int iy, int iz, R* x0, R* y0,
+                        R* z0, R* x1, R* y1, R* z1) {
+    typedef RT<R> M;
+    const R theta = (R)theta_f;
+    const R st = M::sin_(theta), ct = M::cos_(theta);
+    *x0 = (R)g.sourceR * st;
+    *z0 = (R)g.sourceR * ct;
+    *y0 = (R)g.sourceY;
+    *x1 = (R)((ix + 0.5) * (double)g.vx + (double)g.x_p0);
+    *y1 = (R)((iy + 0.5) * (double)g.vy + (double)g.y_p0);
+    *z1 = (R)((iz + 0.5) * (double)g.vz + (double)g.z_p0);
+}
+
+// Voxel-driven bilinear back projection, accumulated into vol
+// (backprj_gpu_manyviews_SBP, Tomo_OSTR.cu:1553-1734).
 template <class R>
 void bp_sbp(const nr_geom& g, R* vol, const R* prj, const int32_t* index,
             const float* angles, int a0, int a1) {
-    typedef RT<R> M;
-    const int NX = g.nx, NY = g.ny, NZ = g.nz, NBX = g.nbx, NBY = g.nby;
-    const R detR = (R)g.detectorR;
+    const int NX = g.nx, NY = g.ny, NZ = g.nz;
+    const size_t B = (size_t)g.nbx * g.nby;
 #pragma omp parallel for collapse(2) schedule(static)
     for (int iz = 0; iz < NZ; iz++) {
         for (int iy = 0; iy < NY; iy++) {
             for (int ix = 0; ix < NX; ix++) {
                 R total_sum = 0;
                 for (int a = a0; a < a1; a++) {
-                    const int s = index[a];
-                    const R theta = (R)angles[s];
-                    const R st = M::sin_(theta), ct = M::cos_(theta);
-                    const R x0 = (R)g.sourceR * st, z0 = (R)g.sourceR * ct, y0 = (R)g.sourceY;
-                    const R x1 = (R)((ix + 0.5) * (double)g.vx + (double)g.x_p0);
-                    const R y1 = (R)((iy + 0.5) * (double)g.vy + (double)g.y_p0);
-                    const R z1 = (R)((iz + 0.5) * (double)g.vz + (double)g.z_p0);
-                    const R depth_weight = (x0 * x0 + y0 * y0 + z0 * z0) /
-                        ((x0 - x1) * (x0 - x1) + (y0 - y1) * (y0 - y1) + (z0 - z1) * (z0 - z1));
-                    if (z1 == z0) continue;
-                    const R t = (-detR - z0) / (z1 - z0);
-                    const R x2 = x0 + (x1 - x0) * t;
-                    const R y2 = y0 + (y1 - y0) * t;
-                    const R imb = (x2 - (R)g.x_d0) / (R)g.bx;
-                    const R jmb = (y2 - (R)g.y_d0) / (R)g.by;
-                    int ilb = (int)M::floor_(imb);
-                    if ((double)imb < ilb + 0.5) ilb = ilb - 1;
-                    int jlb = (int)M::floor_(jmb);
-                    if ((double)jmb < jlb + 0.5) jlb = jlb - 1;
-                    const R fracI = (R)((double)imb - (ilb + 0.5));
-                    const R fracJ = (R)((double)jmb - (jlb + 0.5));
-                    const R* p = prj + (size_t)(a - a0) * NBX * NBY;
-                    R d1 = 0, d2 = 0;
-                    if (ilb < NBX && ilb >= 0 && jlb < NBY && jlb >= 0)
-                        d1 = (1 - fracI) * p[(size_t)ilb * NBY + jlb];
-                    if (ilb < NBX - 1 && ilb >= -1 && jlb < NBY && jlb >= 0)
-                        d1 = d1 + fracI * p[(size_t)(ilb + 1) * NBY + jlb];
-                    if (ilb < NBX && ilb >= 0 && jlb < NBY - 1 && jlb >= -1)
-                        d2 = (1 - fracI) * p[(size_t)ilb * NBY + jlb + 1];
-                    if (ilb < NBX - 1 && ilb >= -1 && jlb < NBY - 1 && jlb >= -1)
-                        d2 = d2 + fracI * p[(size_t)(ilb + 1) * NBY + jlb + 1];
-                    R u_term = (1 - fracJ) * d1 + fracJ * d2;
-                    u_term = u_term * (R)g.vz * depth_weight;
-                    total_sum = total_sum + u_term;
+                    R x0, y0, z0, x1, y1, z1, u;
+                    bp_geometry<R>(g, angles[index[a]], ix, iy, iz, &x0, &y0, &z0, &x1, &y1, &z1);
+                    if (bp_term<R>(g, x0, y0, z0, x1, y1, z1, prj + (size_t)(a - a0) * B, &u,
+                                   nullptr))
+                        total_sum = total_sum + u;
                 }
                 size_t v = ((size_t)iz * NY + iy) * NX + ix;
                 vol[v] = vol[v] + total_sum;
             }
         }
+    }
+}
+
+// OS-SART update in place: x += lambda (u/s + beta prior/s), both 0 where
+// s = 0, then clamp at 0.  prior == nullptr restates
+// backprj_OSSART_gpu_manyviews (Tomo_OSTR.cu:1737-1936), otherwise
+// backprj_OSSART_R_gpu_manyviews (:1938-2143).
+template <class R>
+void bp_ossart(const nr_geom& g, R* vol, const R* prj, const R* prior, const int32_t* index,
+               const float* angles, int a0, int a1, R lambda, R beta) {
+    const int NX = g.nx, NY = g.ny, NZ = g.nz;
+    const size_t B = (size_t)g.nbx * g.nby;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int iz = 0; iz < NZ; iz++) {
+        for (int iy = 0; iy < NY; iy++) {
+            for (int ix = 0; ix < NX; ix++) {
+                R total_sum = 0, total_sens = 0;
+                for (int a = a0; a < a1; a++) {
+                    R x0, y0, z0, x1, y1, z1, u, sn;
+                    bp_geometry<R>(g, angles[index[a]], ix, iy, iz, &x0, &y0, &z0, &x1, &y1, &z1);
+                    if (bp_term<R>(g, x0, y0, z0, x1, y1, z1, prj + (size_t)(a - a0) * B, &u,
+                                   &sn)) {
+                        total_sum = total_sum + u;
+                        total_sens = total_sens + sn;
+                    }
+                }
+                const size_t v = ((size_t)iz * NY + iy) * NX + ix;
+                R u_term = 0, beta_term = 0;
+                if (total_sens != 0) {
+                    u_term = total_sum / total_sens;
+                    if (prior) beta_term = (beta * prior[v]) / total_sens;
+                }
+                R nv = vol[v] + lambda * (u_term + beta_term);
+                vol[v] = nv < 0 ? (R)0 : nv;
+            }
+        }
+    }
+}
+
+// SART projector: est = line integral (times cos theta with use_cos), norm =
+// in-volume chord (the sum_norm of the same walk), missed rays untouched.
+// Restates ray_trace_gpu_manyangles_direct_notexturememory{,_cos},
+// Tomo_OSTR.cu:1177-1311, with rayTrace3D_GPU_direct_notexturememory
+// (:327-610), whose sum and sum_norm are the mode 0 and mode 1 walks above.
+template <class R>
+void fp_sart(const nr_geom& g, const R* vol, R* est, R* norm, const float* angles,
+             const int32_t* index, int a0, int a1, int use_cos) {
+    typedef RT<R> M;
+    const int NBX = g.nbx, NBY = g.nby;
+    for (int a = a0; a < a1; a++) {
+        const R theta = (R)angles[index[a]];
+        const R st = M::sin_(theta), ct = M::cos_(theta);
+        const R x0 = (R)g.sourceR * st, z0 = (R)g.sourceR * ct, y0 = (R)g.sourceY;
+        const size_t o0 = (size_t)(a - a0) * NBX * NBY;
+#pragma omp parallel for schedule(dynamic, 4)
+        for (int i = 0; i < NBX; i++) {
+            for (int j = 0; j < NBY; j++) {
+                R x1, y1, z1, sum, sn;
+                bin_center<R>(g, i, j, &x1, &y1, &z1);
+                if (ray_trace<R>(g, vol, x0, y0, z0, x1, y1, z1, 0, &sum)) {
+                    ray_trace<R>(g, vol, x0, y0, z0, x1, y1, z1, 1, &sn);
+                    est[o0 + (size_t)i * NBY + j] = use_cos ? sum * ct : sum;
+                    norm[o0 + (size_t)i * NBY + j] = sn;
+                }
+            }
+        }
+    }
+}
+
+// SART_prj_diff_kernel, Tomo_OSTR.cu:2145-2183.
+template <class R>
+void sart_prj_diff(R* diff, const R* prj, const R* est, const R* norm, int64_t n) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) diff[i] = norm[i] != 0 ? (prj[i] - est[i]) / norm[i] : (R)0;
+}
+
+// G_Huber_prior, Tomo_OSTR.cu:258-325: prior += sum over the 26 neighbours of
+// (1/distance) diff / sqrt(1 + (diff/delta)^2), plain distances, centre
+// distance 1 (its diff is 0), out-of-volume neighbour = the voxel itself.
+// The float instantiation keeps the reference's mixed float/double rounding.
+template <class R>
+void prior_sart(const nr_geom& g, R* prior, const R* x, R delta) {
+    const int NX = g.nx, NY = g.ny, NZ = g.nz;
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int iz = 0; iz < NZ; iz++)
+        for (int iy = 0; iy < NY; iy++)
+            for (int ix = 0; ix < NX; ix++) {
+                const size_t v = ((size_t)iz * NY + iy) * NX + ix;
+                R acc = prior[v];
+                for (int kz = iz - 1; kz < iz + 2; kz++)
+                    for (int ky = iy - 1; ky < iy + 2; ky++)
+                        for (int kx = ix - 1; kx < ix + 2; kx++) {
+                            const int ddx = kx - ix, ddy = ky - iy, ddz = kz - iz;
+                            R distance = std::sqrt((R)(ddx * ddx + ddy * ddy + ddz * ddz));
+                            if (distance == 0) distance = 1;
+                            size_t nb = v;
+                            if (!(kx < 0 || ky < 0 || kz < 0 || kx > NX - 1 || ky > NY - 1 || kz > NZ - 1))
+                                nb = ((size_t)kz * NY + ky) * NX + kx;
+                            const R diff = x[v] - x[nb];
+                            const R den = (R)std::sqrt(1.0 + (double)((diff / delta) * (diff / delta)));
+                            acc = (R)((double)acc + (1.0 / (double)distance) * (double)diff / (double)den);
+                        }
+                prior[v] = acc;
+            }
+}
+
+// log(blank / (prj - scat)) where both are positive, else 0.
+template <class R>
+void line_integrals(R* line, const R* prj, const R* blank, const R* scat, int64_t n) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+        const R nu = prj[i] - (scat ? scat[i] : (R)0);
+        line[i] = (nu > 0 && blank[i] > 0) ? (R)std::log((double)blank[i] / (double)nu) : (R)0;
     }
 }
 
@@ -446,6 +597,40 @@ void subiter(const nr_geom& g, const nr_ostr_params& p, const float* angles,
     update_est<R>(x, capL.data(), RD.data(), d, RDD.data(), (R)p.beta, N);
 }
 
+// The OS-SART loop of the device-resident path: line integrals ([view][i][j],
+// original order) regrouped to subset order, subset-major index
+// (Tomo_OSTR_gold.cpp:628-642); per iteration and subset: est, norm zeroed
+// (missed rays: difference 0), fp_sart, sart_prj_diff, [prior zeroed +
+// prior_sart], bp_ossart in place.
+template <class R>
+void ossart(const nr_geom& g, const nr_sart_params& p, const float* angles, const R* line_in,
+            R* x, int iters) {
+    const int A = g.n_angles, M = p.subset_num, Vs = A / M;
+    const int64_t B = (int64_t)g.nbx * g.nby, N = (int64_t)g.nx * g.ny * g.nz;
+    std::vector<int32_t> index(A);
+    for (int i = 0; i < A; i++) index[i] = i;
+    reorder_index(index.data(), A, M);
+    std::vector<R> line((size_t)A * B);
+    regroup<R>(line.data(), line_in, A, M, B);
+    std::vector<R> est((size_t)Vs * B), norm((size_t)Vs * B), diff((size_t)Vs * B);
+    std::vector<R> prior(p.regularized ? N : 0);
+    for (int iter = 0; iter < iters; iter++)
+        for (int a = 0; a < M; a++) {
+            const int a0 = a * Vs, a1 = a0 + Vs;
+            std::fill(est.begin(), est.end(), (R)0);
+            std::fill(norm.begin(), norm.end(), (R)0);
+            fp_sart<R>(g, x, est.data(), norm.data(), angles, index.data(), a0, a1, p.use_cos);
+            sart_prj_diff<R>(diff.data(), line.data() + (size_t)a0 * B, est.data(), norm.data(),
+                             (int64_t)Vs * B);
+            if (p.regularized) {
+                std::fill(prior.begin(), prior.end(), (R)0);
+                prior_sart<R>(g, prior.data(), x, (R)p.delta);
+            }
+            bp_ossart<R>(g, x, diff.data(), p.regularized ? prior.data() : nullptr, index.data(),
+                         angles, a0, a1, (R)p.lambda, (R)p.beta);
+        }
+}
+
 }  // namespace
 
 #define ORC_EXPORT extern "C" __attribute__((visibility("default")))
@@ -500,7 +685,39 @@ void subiter(const nr_geom& g, const nr_ostr_params& p, const float* angles,
         reconstruct<R>(*g, *p, angles, prj, blank, scat, x, iters, d_out, gamma_out);   \
     }
 
+#define ORC_INSTANTIATE_SART(R, SUF)                                                    \
+    ORC_EXPORT void orc_fp_sart_##SUF(const nr_geom* g, const R* x, R* est, R* norm,    \
+                                      const float* angles, const int32_t* index,        \
+                                      int a0, int a1, int use_cos) {                    \
+        fp_sart<R>(*g, x, est, norm, angles, index, a0, a1, use_cos);                   \
+    }                                                                                   \
+    ORC_EXPORT void orc_sart_prj_diff_##SUF(R* diff, const R* prj, const R* est,        \
+                                            const R* norm, int64_t n) {                 \
+        sart_prj_diff<R>(diff, prj, est, norm, n);                                      \
+    }                                                                                   \
+    ORC_EXPORT void orc_bp_ossart_##SUF(const nr_geom* g, R* x, const R* diff,          \
+                                        const R* prior, const int32_t* index,           \
+                                        const float* angles, int a0, int a1,            \
+                                        double lambda, double beta) {                   \
+        bp_ossart<R>(*g, x, diff, prior, index, angles, a0, a1, (R)lambda, (R)beta);    \
+    }                                                                                   \
+    ORC_EXPORT void orc_prior_sart_##SUF(const nr_geom* g, R* prior, const R* x,        \
+                                         double delta) {                                \
+        prior_sart<R>(*g, prior, x, (R)delta);                                          \
+    }                                                                                   \
+    ORC_EXPORT void orc_line_integrals_##SUF(R* line, const R* prj, const R* blank,     \
+                                             const R* scat, int64_t n) {                \
+        line_integrals<R>(line, prj, blank, scat, n);                                   \
+    }                                                                                   \
+    ORC_EXPORT void orc_ossart_##SUF(const nr_geom* g, const nr_sart_params* p,         \
+                                     const float* angles, const R* line, R* x,          \
+                                     int iters) {                                       \
+        ossart<R>(*g, *p, angles, line, x, iters);                                      \
+    }
+
 ORC_INSTANTIATE(float, f32)
+ORC_INSTANTIATE_SART(float, f32)
+ORC_INSTANTIATE_SART(double, f64)
 ORC_INSTANTIATE(double, f64)
 
 ORC_EXPORT void orc_reorder_index(int32_t* idx, int n_angles, int M) {

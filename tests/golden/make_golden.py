@@ -5,6 +5,7 @@ bodies of Tomo_OSTR.cu and the gold driver Tomo_OSTR_gold.cpp from the
 reference sources) on seeded inputs and stores inputs + outputs as .npz:
 
     python tests/golden/make_golden.py            # needs the reference sources
+    python tests/golden/make_golden.py --sart     # the SART fixtures only
 
 Fixtures (all float32 unless noted):
 
@@ -19,6 +20,11 @@ Fixtures (all float32 unless noted):
                 per-slice sums plus 8192 seeded voxel samples (the full volume
                 is 3 MB), and FP_cos of the phantom for view 0 sampled the
                 same way.
+``sart_tiny.npz``, ``sart_ragged.npz``
+                the SART family on the tiny and ragged cases: the SART
+                projector (plain and cos), the projection difference, the SART
+                prior, both OS-SART back projections, and OS-SART loops
+                composed from the reference's own launch wrappers.
 """
 from __future__ import annotations
 
@@ -81,7 +87,48 @@ def full_set(name: str, g: Geometry, angles, subset_num, beta, delta, x, y, b, s
     print(f"wrote {name}.npz")
 
 
+def sart_set(name: str, g: Geometry, angles, subset_num, x, y, b, s, lam, beta, delta, iters):
+    """The SART family from the reference's own kernels (Tomo_OSTR.cu:1177-1311,
+    1737-2183 through its launch wrappers), and OS-SART loops composed from
+    them (the reference has no OS-SART driver)."""
+    R = Reference()
+    R.set_geometry(g, subset_num, 0.0, delta)
+    A = g.n_angles
+    idx = np.arange(A, dtype=np.int32)
+    ridx = Oracle(np.float64).reorder_index(A, subset_num)
+    Vs = A // subset_num
+    rng = np.random.default_rng(4321)
+    nu = y.astype(np.float64) - s
+    line = np.where((nu > 0) & (b > 0), np.log(np.maximum(b, 1e-30) / np.maximum(nu, 1e-30)),
+                    0.0).astype(np.float32)
+    out = dict(geom=_geom_arr(g), angles=angles, subset_num=np.int32(subset_num),
+               lam=np.float32(lam), beta=np.float32(beta), delta=np.float32(delta),
+               iters=np.int32(iters), x=x, line=line)
+    out["fp_est"], out["fp_norm"] = R.fp_sart(x, angles, idx, 0, A, False)
+    out["fpc_est"], out["fpc_norm"] = R.fp_sart(x, angles, idx, 0, A, True)
+    e1, n1 = R.fp_sart(x, angles, ridx, Vs, 2 * Vs, True)
+    out["fpc_sub1_est"], out["fpc_sub1_norm"] = e1, n1
+    out["diff_sub1"] = R.sart_prj_diff(line.reshape(A, -1)[ridx[Vs:2 * Vs]].ravel(), e1, n1,
+                                       ridx, Vs, 2 * Vs)
+    out["prior"] = R.prior_sart(x, delta)
+    dif = (rng.normal(size=Vs * g.n_bins) * 0.01).astype(np.float32)
+    out["bp_in"] = dif
+    out["bp_plain"] = R.bp_ossart(x, dif, ridx, angles, Vs, 2 * Vs, lam)
+    out["bp_reg"] = R.bp_ossart(x, dif, ridx, angles, Vs, 2 * Vs, lam, out["prior"], beta)
+    out["ossart"] = R.ossart(angles, line, subset_num=subset_num, iter_num=iters, lam=lam,
+                             use_cos=True)
+    out["ossart_nocos"] = R.ossart(angles, line, subset_num=subset_num, iter_num=iters, lam=lam,
+                                   use_cos=False)
+    out["ossart_reg"] = R.ossart(angles, line, subset_num=subset_num, iter_num=iters, lam=lam,
+                                 use_cos=True, regularized=True, beta=beta, delta=delta)
+    np.savez_compressed(os.path.join(HERE, f"sart_{name}.npz"), **out)
+    print(f"wrote sart_{name}.npz")
+
+
 def main() -> None:
+    if "--sart" in sys.argv:
+        sart_main()
+        return
     # tiny: the phantom, its Poisson scan, no scatter
     cfg = config("tiny")
     g = cfg.geom
@@ -134,6 +181,33 @@ def main() -> None:
         phantom_sum=np.float64(x.astype(np.float64).sum()),
         counts_sum=np.float64(y.astype(np.float64).sum()))
     print("wrote small.npz")
+
+
+def sart_main() -> None:
+    # tiny: the phantom and its Poisson scan
+    cfg = config("tiny")
+    g = cfg.geom
+    x = breast_phantom(g, 0, cfg.n_glandular, cfg.n_calc).ravel()
+    idx = np.arange(g.n_angles, dtype=np.int32)
+    line = Oracle(np.float64).fp_ostr(g, x, cfg.angles, idx, 0, g.n_angles)
+    y = poisson_counts(line, cfg.I0, 0)
+    b = np.full_like(y, cfg.I0)
+    s = np.zeros_like(y)
+    sart_set("tiny", g, cfg.angles, cfg.subset_num, x, y, b, s, 0.8, -0.2, 0.01, 3)
+    # ragged: odd sizes, off-centre detector, scatter, dead bins
+    g = Geometry(nx=33, ny=17, nz=5, vx=0.7, vy=0.7, vz=1.3, x_p0=-11.0, y_p0=-12.5,
+                 z_p0=1.0, nbx=41, nby=23, bx=0.9, by=0.8, x_d0=-19.0, y_d0=-17.0,
+                 detectorR=25.0, sourceR=600.0, sourceY=-3.0, n_angles=4)
+    rng = np.random.default_rng(7)
+    angles = view_angles(4, 20.0)
+    x = (rng.uniform(0.0, 0.1, size=g.n_voxels)).astype(np.float32)
+    x[rng.uniform(size=x.size) < 0.05] = 0.0
+    line = Oracle(np.float64).fp_ostr(g, x, angles, np.arange(4, dtype=np.int32), 0, 4)
+    y = poisson_counts(line, 3000.0, 3)
+    b = rng.uniform(2800.0, 3200.0, size=y.size).astype(np.float32)
+    s = rng.uniform(0.0, 60.0, size=y.size).astype(np.float32)
+    y[rng.uniform(size=y.size) < 0.01] = 0.0
+    sart_set("ragged", g, angles, 2, x, y, b, s, 0.5, -0.2, 0.02, 2)
 
 
 if __name__ == "__main__":

@@ -64,6 +64,31 @@ def test_datafile_command_matches_gold_driver(tmp_path, name, method, key):
     assert (out >= 0).all()
 
 
+@pytest.mark.parametrize("name", ["tiny", "ragged"])
+def test_datafile_ossart_matches_reference_kernels(tmp_path, name):
+    """Recon_Method 3 runs OS-SART on the log of the scans; against the OS-SART
+    loop composed from the reference's SART kernels on the same line integrals."""
+    from newrecon_gb300 import native, tomo_ostr
+
+    native.load()
+    z = dict(np.load(os.path.join(HERE, "golden", f"{name}.npz")))
+    zs = np.load(os.path.join(HERE, "golden", f"sart_{name}.npz"))
+    z["iters"] = zs["iters"]
+    z["delta"] = zs["delta"]
+    cfg, path = _write_case(tmp_path, z, 3, io_iter=0)
+    cfg.sart_lambda = float(zs["lam"])
+    cfg.sart_beta = float(zs["beta"])
+    from newrecon_gb300 import datfile
+
+    datfile.write(path, cfg)
+    written = tomo_ostr.run(path, log=lambda *_: None)
+    assert written == [str(tmp_path) + f"/rec_{int(zs['iters']) - 1}"]
+    out = np.fromfile(written[-1], dtype=np.float32)
+    r = rel_rmse(out, zs["ossart_reg"])
+    print(f"{name}/OS-SART vs reference kernels: rel RMSE {r:.2e}")
+    assert r < 1e-4
+
+
 def test_initial_guess_and_readout_period(tmp_path):
     """An initial guess file is read; with a period of 2 only every 2nd iteration is written."""
     from newrecon_gb300 import native, ostr, tomo_ostr
