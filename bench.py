@@ -52,6 +52,8 @@ def parse():
                     help="also time N batched reconstructions (persistent launches)")
     ap.add_argument("--batch-steps", type=int, default=25)
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--algo", default="ostr", choices=["ostr", "ossart"],
+                    help="ostr (the headline) or ossart (the SART family on the same workload)")
     ap.add_argument("--no-warm", action="store_true",
                     help="skip the learned warm-start comparison")
     return ap.parse_args()
@@ -539,9 +541,229 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# OS-SART on the same workload (--algo ossart): lambda 0.8, cos projector,
+# hyperbola prior (beta -0.2, the workload's delta).
+
+SART_METRIC = "OS-SART subset-iterations/s"
+SART_KW = dict(lam=0.8, use_cos=True, regularized=True, beta=-0.2)
+
+
+def sart_line(cfg, y, b):
+    import torch
+
+    from newrecon_gb300 import sart
+
+    return sart.line_integrals(torch.from_numpy(y).cuda(), torch.from_numpy(b).cuda())
+
+
+def cpu_port_ossart(cfg, line, n_sub: int, threads: int):
+    """FP32 CPU restatement of the OS-SART sub-iteration (s per sub-iteration):
+    SART projection, difference, SART prior, OS-SART back projection."""
+    from oracle.oracle import Oracle
+
+    g = cfg.geom
+    O = Oracle(np.float32)
+    O.set_threads(threads)
+    M, A = cfg.subset_num, g.n_angles
+    Vs, B = A // M, g.n_bins
+    ridx = O.reorder_index(A, M)
+    lr = O.regroup(line, A, M)
+    x = np.zeros(g.n_voxels, np.float32)
+    times = []
+    for k in range(n_sub):
+        a = k % M
+        a0, a1 = a * Vs, (a + 1) * Vs
+        t0 = time.perf_counter()
+        est, norm = O.fp_sart(g, x, cfg.angles, ridx, a0, a1, SART_KW["use_cos"])
+        diff = O.sart_prj_diff(lr[a0 * B:a1 * B], est, norm)
+        prior = O.prior_sart(g, x, cfg.delta)
+        x = O.bp_ossart(g, x, diff, ridx, cfg.angles, a0, a1, SART_KW["lam"], prior,
+                        SART_KW["beta"])
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def run_ossart(args):
+    import torch
+    import torch.distributed as dist
+
+    from newrecon_gb300 import native, replicas, sart
+    from newrecon_gb300.geometry import config
+
+    ws, rank, local = replicas.env()
+    if ws > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    native.load()
+    seed = replicas.case_seed(0, rank)
+    cfg = config(args.config, seed=seed)
+    g = cfg.geom
+    x_true, y, b = make_scan_gpu(cfg, seed=seed)
+    line = sart_line(cfg, y, b)
+    M = cfg.subset_num
+    plan = sart.OSSART(g, subset_num=M, delta=cfg.delta, **SART_KW)
+    plan.setup(cfg.angles, line)
+    xa = torch.zeros(g.n_voxels, device="cuda")
+    xb = torch.zeros(g.n_voxels, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step(evs=None):
+        nonlocal xa, xb
+        for a in range(M):
+            if evs is not None:
+                evs[0].record(stream)
+            plan.project(xa, a)
+            if evs is not None:
+                evs[1].record(stream)
+            plan.update(xa, xb, a)
+            if evs is not None:
+                evs[2].record(stream)
+                evs = evs[3:]
+            xa, xb = xb, xa
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    plan.check()
+    events = [torch.cuda.Event(enable_timing=True) for _ in range(3 * M * args.steps)]
+    clocks = Clocks(local)
+    clocks.start()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for s in range(args.steps):
+        step(events[3 * M * s:3 * M * (s + 1)])
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    elapsed = t_start.elapsed_time(t_end) / 1e3
+    elapsed, n_sub = replicas.reduce_timing(elapsed, M * args.steps)
+    plan.check()
+    fp_ms = np.array([events[3 * k].elapsed_time(events[3 * k + 1]) for k in range(M * args.steps)])
+    up_ms = np.array([events[3 * k + 1].elapsed_time(events[3 * k + 2])
+                      for k in range(M * args.steps)])
+    N, B, Vs = g.n_voxels, g.n_bins, g.n_angles // M
+    fp_bytes = 4 * N * Vs + 12 * B * Vs       # x read per view + p, norm read + diff written
+    up_bytes = 8 * N + 4 * B * Vs             # x read + x' written + diff read
+    peak, peak_kind = measured_peaks()
+    kern = {
+        "sart_fp_diff": {"avg_ms": float(fp_ms.mean()), "bytes": fp_bytes,
+                         "gbs": fp_bytes / (fp_ms.mean() / 1e3) / 1e9},
+        "sart_update": {"avg_ms": float(up_ms.mean()), "bytes": up_bytes,
+                        "gbs": up_bytes / (up_ms.mean() / 1e3) / 1e9},
+    }
+    dom = max(kern, key=lambda k: kern[k]["avg_ms"])
+    traffic = None
+    prof_traffic = os.path.join(HERE, "profiles", "dram_traffic.txt")
+    if os.path.isfile(prof_traffic):
+        for ln in open(prof_traffic):
+            parts = ln.split()
+            if len(parts) >= 2 and not ln.startswith("#") and parts[0] == dom:
+                traffic = float(parts[1])
+    workload = ("clinical: 1024x512x60 vox @0.14x0.14x1mm, 1664x832 det @0.14mm, 25 views "
+                "+-25deg, 25 subsets, OS-SART lambda 0.8, cos projector, hyperbola prior "
+                "beta -0.2 d=0.003, line integrals of Poisson(5e3) counts")
+    out = {
+        "metric": SART_METRIC, "value": n_sub / elapsed, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded breast phantom, Poisson counts, log transform)",
+        "config": {"workload": workload, "step": "1 OS-SART iteration = 25 sub-iterations",
+                   "parallelism": f"replicas x{ws}",
+                   "l2": "inputs larger than L2 (x, x': 2 x 126 MB; p, norm: 2 x 138 MB)"},
+        "gpu_launches": 2 * M * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": kern[dom]["gbs"], "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": kern[dom]["gbs"] / peak, "traffic": traffic, "kernels": kern},
+    }
+    if clk is not None:
+        out["clocks"] = clk
+    if not args.no_e2e:
+        iters = args.e2e_iters or cfg.iter_num
+        l_h = line.cpu().pin_memory()
+        a_h = torch.from_numpy(cfg.angles).pin_memory()
+        kw = dict(angles=a_h, subset_num=M, iter_num=iters, delta=cfg.delta, **SART_KW)
+        sart.ossart_reconstruct(g, l_h, **kw)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(args.e2e_runs):
+            t0 = time.perf_counter()
+            vol = sart.ossart_reconstruct(g, l_h, **kw)
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        assert vol.device.type == "cpu"
+        out["e2e"] = {"value": iters * M / float(np.mean(ts)), "unit": UNIT,
+                      "h2d_bytes_per_step": int(l_h.numel() * 4 + cfg.angles.nbytes),
+                      "d2h_bytes_per_step": int(g.n_voxels * 4),
+                      "step": f"sart.ossart_reconstruct from pinned host line integrals: upload, "
+                              f"chord setup, {iters} iterations x {M} subsets, volume download",
+                      "seconds_per_call": float(np.mean(ts))}
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        times = cpu_port_ossart(cfg, line.cpu().numpy(), args.cpu_subiters, threads)
+        ncpu, model = cpu_info()
+        out["cpu_baseline"] = {"value": len(times) / sum(times), "unit": UNIT, "cores": threads,
+                               "kind": "port",
+                               "sample": f"{len(times)} OS-SART sub-iterations of the clinical "
+                                         f"workload (FP32 restatement of the reference's SART "
+                                         f"kernels, OpenMP), {model}"}
+    if ws > 1:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def run_reference_ossart(args):
+    from newrecon_gb300 import replicas
+
+    ws, rank, local = replicas.env()
+    if rank != 0:
+        return
+    from newrecon_gb300.geometry import config
+    from newrecon_gb300.phantom import breast_phantom, poisson_counts
+    from oracle import build as obuild
+    from oracle.oracle import Oracle
+
+    if not os.path.isfile(obuild.ORACLE_SO):
+        obuild.build_oracle().wait()
+    cfg = config(args.config, seed=0)
+    g = cfg.geom
+    threads = os.cpu_count() or 1
+    O = Oracle(np.float32)
+    O.set_threads(threads)
+    x = breast_phantom(g, 0, cfg.n_glandular, cfg.n_calc, thickness_mm=cfg.thickness_mm).ravel()
+    idx = np.arange(g.n_angles, dtype=np.int32)
+    y = poisson_counts(O.fp_ostr(g, x, cfg.angles, idx, 0, g.n_angles), cfg.I0, 0)
+    line = O.line_integrals(y, np.full_like(y, cfg.I0))
+    times = cpu_port_ossart(cfg, line, args.warmup + args.steps, threads)[args.warmup:]
+    elapsed = float(sum(times))
+    value = len(times) / elapsed
+    ncpu, model = cpu_info()
+    print(json.dumps({
+        "impl": "reference", "metric": SART_METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded breast phantom, Poisson counts, log transform)",
+        "config": {"workload": "clinical OS-SART (see --algo ossart)",
+                   "step": "1 OS-SART sub-iteration on the host cores", "parallelism": "host"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{len(times)} sub-iterations (FP32 restatement of the "
+                                   f"reference's SART kernels, OpenMP), {model}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.algo == "ossart":
+        run_reference_ossart(args) if args.impl == "reference" else run_ossart(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

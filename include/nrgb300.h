@@ -397,6 +397,15 @@ nr_status nr_sart_setup(const nr_geom* g, const nr_sart_params* p, const float* 
 nr_status nr_sart_iterate(const nr_geom* g, const nr_sart_params* p, float* x,
                           int32_t n_iters, void* workspace, size_t ws_bytes, void* stream);
 
+/* The two halves of sub-iteration `subset`: the fused projection and
+ * difference into the workspace, then x_out = the OS-SART update of x
+ * (x_out != x).  nr_sart_subiter = project + update + copy back. */
+nr_status nr_sart_project(const nr_geom* g, const nr_sart_params* p, const float* x,
+                          int32_t subset, void* workspace, size_t ws_bytes, void* stream);
+nr_status nr_sart_update(const nr_geom* g, const nr_sart_params* p, const float* x,
+                         float* x_out, int32_t subset, void* workspace, size_t ws_bytes,
+                         void* stream);
+
 /* One sub-iteration for subset a (0 <= a < M), x in place. */
 nr_status nr_sart_subiter(const nr_geom* g, const nr_sart_params* p, float* x,
                           int32_t subset, void* workspace, size_t ws_bytes, void* stream);

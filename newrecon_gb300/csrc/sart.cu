@@ -215,15 +215,26 @@ nr_status launch_sart_update_z(const nr_geom& g, const nr_sart_params& p, const 
     }
 }
 
+nr_status sart_project(const nr_geom& g, const nr_sart_params& p, const float* x, int subset,
+                       const SartWS& w, cudaStream_t s) {
+    const int Vs = g.n_angles / p.subset_num, a0 = subset * Vs;
+    return p.use_cos ? launch_fp_diff_c<true>(g, p.fp_batch, x, w, a0, Vs, s)
+                     : launch_fp_diff_c<false>(g, p.fp_batch, x, w, a0, Vs, s);
+}
+
+nr_status sart_update(const nr_geom& g, const nr_sart_params& p, const float* x, float* x_out,
+                      int subset, const SartWS& w, cudaStream_t s) {
+    const int Vs = g.n_angles / p.subset_num, a0 = subset * Vs;
+    return p.regularized ? launch_sart_update_z<UPD_SART_R>(g, p, x, x_out, w, a0, Vs, s)
+                         : launch_sart_update_z<UPD_SART>(g, p, x, x_out, w, a0, Vs, s);
+}
+
 // One sub-iteration: x -> x_out (x_out != x).
 nr_status sart_step(const nr_geom& g, const nr_sart_params& p, const float* x, float* x_out,
                     int subset, const SartWS& w, cudaStream_t s) {
-    const int Vs = g.n_angles / p.subset_num, a0 = subset * Vs;
-    nr_status st = p.use_cos ? launch_fp_diff_c<true>(g, p.fp_batch, x, w, a0, Vs, s)
-                             : launch_fp_diff_c<false>(g, p.fp_batch, x, w, a0, Vs, s);
+    nr_status st = sart_project(g, p, x, subset, w, s);
     if (st != NR_OK) return st;
-    return p.regularized ? launch_sart_update_z<UPD_SART_R>(g, p, x, x_out, w, a0, Vs, s)
-                         : launch_sart_update_z<UPD_SART>(g, p, x, x_out, w, a0, Vs, s);
+    return sart_update(g, p, x, x_out, subset, w, s);
 }
 
 nr_status sart_enqueue(const nr_geom& g, const nr_sart_params& p, float* x, int n_iters,
@@ -276,6 +287,26 @@ NR_API nr_status nr_sart_setup(const nr_geom* g, const nr_sart_params* p, const 
     dim3 blk(32, 4), grd(cdiv(g->nbx, 32), cdiv(g->nby, 4), A);
     sart_norm_kernel<<<grd, blk, 0, s>>>(make_geo(*g), w.norm, w.angles, w.index);
     return launch_status();
+}
+
+NR_API nr_status nr_sart_project(const nr_geom* g, const nr_sart_params* p, const float* x,
+                                 int32_t subset, void* workspace, size_t ws_bytes, void* stream) {
+    SartLayout L;
+    nr_status st = sart_check_ws(g, p, workspace, ws_bytes, &L);
+    if (st != NR_OK) return st;
+    if (!x || subset < 0 || subset >= p->subset_num) return NR_ERR_BAD_ARGUMENT;
+    return sart_project(*g, *p, x, subset, sart_carve(workspace, L), as_stream(stream));
+}
+
+NR_API nr_status nr_sart_update(const nr_geom* g, const nr_sart_params* p, const float* x,
+                                float* x_out, int32_t subset, void* workspace, size_t ws_bytes,
+                                void* stream) {
+    SartLayout L;
+    nr_status st = sart_check_ws(g, p, workspace, ws_bytes, &L);
+    if (st != NR_OK) return st;
+    if (!x || !x_out || x == x_out || subset < 0 || subset >= p->subset_num)
+        return NR_ERR_BAD_ARGUMENT;
+    return sart_update(*g, *p, x, x_out, subset, sart_carve(workspace, L), as_stream(stream));
 }
 
 NR_API nr_status nr_sart_subiter(const nr_geom* g, const nr_sart_params* p, float* x,

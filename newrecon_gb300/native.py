@@ -84,6 +84,8 @@ SIGNATURES = {
     "nr_sart_setup": (_I32, [_GP, _SP, _P, _P, _P, ctypes.c_size_t, _P]),
     "nr_sart_iterate": (_I32, [_GP, _SP, _P, _I32, _P, ctypes.c_size_t, _P]),
     "nr_sart_subiter": (_I32, [_GP, _SP, _P, _I32, _P, ctypes.c_size_t, _P]),
+    "nr_sart_project": (_I32, [_GP, _SP, _P, _I32, _P, ctypes.c_size_t, _P]),
+    "nr_sart_update": (_I32, [_GP, _SP, _P, _P, _I32, _P, ctypes.c_size_t, _P]),
     "nr_sart_graph_create": (_I32, [_GP, _SP, _P, _I32, _P, ctypes.c_size_t, _P,
                                     ctypes.POINTER(ctypes.c_void_p)]),
     "nr_sart_workspace_section": (_I32, [_GP, _SP, _I32, _P, ctypes.c_size_t,

@@ -155,6 +155,18 @@ class OSSART:
                     int(n_iters), ws, n, _stream())
         return x
 
+    def project(self, x: torch.Tensor, subset: int) -> None:
+        """First half of a sub-iteration: the subset's normalised difference."""
+        ws, n = self._ws()
+        native.call("nr_sart_project", ctypes.byref(self.gc), ctypes.byref(self.params), _p(x),
+                    int(subset), ws, n, _stream())
+
+    def update(self, x: torch.Tensor, x_out: torch.Tensor, subset: int) -> None:
+        """Second half: x_out = the OS-SART update of x (x_out is not x)."""
+        ws, n = self._ws()
+        native.call("nr_sart_update", ctypes.byref(self.gc), ctypes.byref(self.params), _p(x),
+                    _p(x_out), int(subset), ws, n, _stream())
+
     def subiter(self, x: torch.Tensor, subset: int) -> torch.Tensor:
         ws, n = self._ws()
         native.call("nr_sart_subiter", ctypes.byref(self.gc), ctypes.byref(self.params), _p(x),

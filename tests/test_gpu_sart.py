@@ -274,9 +274,17 @@ def test_graph_and_subiter_match_iterate(sart):
     gr.launch()
     torch.cuda.synchronize()
     gr.close()
+    x4 = torch.zeros(g.n_voxels, device="cuda")
+    x5 = torch.empty_like(x4)
+    for _ in range(2):
+        for a in range(M):
+            plan.project(x4, a)
+            plan.update(x4, x5, a)
+            x4, x5 = x5, x4
     assert plan.check() == 0
     assert torch.equal(x1, x2)
     assert torch.equal(x1, x3)
+    assert torch.equal(x1, x4)
 
 
 def test_bad_parameters_and_nonfinite(sart):
