@@ -337,6 +337,28 @@ nr_status nr_fp_sart(const nr_geom* g, const float* x, float* prj_est, float* no
                      const float* angles, const int32_t* index, int32_t a0, int32_t a1,
                      int32_t use_cos, void* stream);
 
+/* Detector layouts a projector can write. */
+enum {
+    NR_LAYOUT_IJ = 0,      /* [view][i][j], j fastest: the 1R projectors' layout           */
+    NR_LAYOUT_JI = 1       /* [view][j][i], i fastest: the scanner files' layout            */
+};
+
+/* 2 x 2 super-sampled projection: per bin, the mean of the line integrals of
+ * the four sub-rays through the sub-bin centres x_d0 + (2i+a+0.5) Bsize_x/2,
+ * y_d0 + (2j+b+0.5) Bsize_y/2 (a, b in {0, 1}), sub-rays that miss the volume
+ * counting 0, summed in the order (((s00 + s10) + s01) + s11) / 4, times
+ * cos(theta) when use_cos.  prj gets every bin of views index[a], a in
+ * [a0,a1), in `layout`; sub, if not NULL, gets the sub-ray sums
+ * [view][2 BINSy][2 BINSx] (missed sub-rays untouched).  Replaces
+ * fprojectCB1_4R_GPU_SART (Tomo_OSTR.cu:2398-2433; kernels :1453, :1517),
+ * fixed: the reference does not compile (nBatchBINSx_4R / PRJ_*_4R are
+ * undefined) and its merge never assigns the fourth sub-ray's index
+ * (:1545-1547).  Its drop-in is use_cos = 0, layout = NR_LAYOUT_JI (the layout
+ * its merge writes); the sub-ray buffer it needs is optional here. */
+nr_status nr_fp_4r(const nr_geom* g, const float* x, float* prj, float* sub,
+                   const float* angles, const int32_t* index, int32_t a0, int32_t a1,
+                   int32_t use_cos, int32_t layout, void* stream);
+
 /* diff[k] = (prj[k] - prj_est[k]) / normprj[k] where normprj[k] != 0, else 0,
  * for k < n (n = (a1-a0)*BINSx*BINSy for the reference's view range).
  * Replaces SART_prj_diff (Tomo_OSTR.cu:2537-2558; kernel :2145). */
@@ -379,6 +401,8 @@ typedef struct nr_sart_params {
     float lambda;              /* relaxation                                     */
     float beta;                /* prior weight (regularized only; see the sign note above) */
     float delta;               /* hyperbola scale, != 0 (regularized only)      */
+    int32_t supersample;       /* 1: the 2 x 2 sub-ray projector of nr_fp_4r (and its
+                                  mean chord as normprj); 0: one ray per bin      */
 } nr_sart_params;
 
 /* Bytes of workspace the OS-SART loop needs. */
@@ -427,6 +451,36 @@ enum {
 nr_status nr_sart_workspace_section(const nr_geom* g, const nr_sart_params* p,
                                     int32_t section, void* workspace, size_t ws_bytes,
                                     void** ptr, size_t* bytes);
+
+/* ---------------------------------------------------------------------------
+ * Dual-energy weighted subtraction (syncrecon.m:1-41): post-processing of a
+ * high-energy (he) and a low-energy (le) reconstruction on the device.
+ * ------------------------------------------------------------------------- */
+
+/* For each of n_weights (1..16) weights w_k (host array of doubles):
+ * d[k][i] = float(double(he[i]) - double(le[i]) * w_k), i < n, rounded in
+ * double exactly as MATLAB's `d = he - le*weight` on the float32 volumes it
+ * reads (syncrecon.m:28).  mask_level >= 0 first zeroes he and le where
+ * he <= mask_level (the imbinarize(he, graythresh(he)) mask of :7-8, applied
+ * in its commented-out :21-22); mask_level < 0 uses no mask.  If hist is not
+ * NULL it gets hist[k][b] = the number of i in [hist_begin, hist_begin +
+ * hist_len) whose double d_k falls in 8-bit bin b = round(255 d) saturated to
+ * [0, 255] (the histogram MATLAB's entropy(d(:,:,slice)) counts, :34).
+ * he, le and d 16-byte aligned; d holds n_weights * n floats. */
+nr_status nr_de_subtract(const float* he, const float* le, const double* weights,
+                         int32_t n_weights, int64_t n, double mask_level, float* d,
+                         int64_t hist_begin, int64_t hist_len, int32_t* hist, void* stream);
+
+/* hist[b] = the number of x[i] (i < n) in 8-bit bin b, as above (the
+ * histogram of graythresh, syncrecon.m:7).  hist: 256 int32 on the device. */
+nr_status nr_hist8(const float* x, int64_t n, int32_t* hist, void* stream);
+
+/* Host functions on a 256-bin histogram in HOST memory (no GPU work):
+ * Shannon entropy in bits of `count` values (MATLAB's entropy), and Otsu's
+ * threshold as a level in [0, 1] (graythresh: bin of maximal between-class
+ * variance, the mean index of ties, / 255; 0 when the maximum is not finite). */
+nr_status nr_hist_entropy(const int32_t* hist, int64_t count, double* entropy);
+nr_status nr_otsu_level(const int32_t* hist, double* level);
 
 /* Library version string. */
 const char* nr_version(void);

@@ -1,0 +1,202 @@
+// dual_energy.cu -- weighted dual-energy subtraction of two reconstructions.
+//
+// syncrecon.m (the reference's post-processing of a high- and a low-energy
+// OSTR volume) forms, for every weight w of a list, d = he - le * w and writes
+// d as float32; it prints the entropy of one slice of each d, and computes an
+// Otsu threshold of he (graythresh) whose mask it applies in commented-out
+// lines.  MATLAB reads the float32 files as double, so d is
+//     float(double(he) - double(le) * w)        (two roundings in double)
+// which the kernel reproduces bit for bit with separate double multiply and
+// subtract (no contraction to an FMA).  The K outputs of one voxel are
+// written from one read of he and le; the stream is HBM bound on the K
+// writes, with the double arithmetic on the FP64 pipe beside it.
+//
+// Image-statistics helpers (the 8-bit conversion of MATLAB's entropy and
+// graythresh): a value v maps to bin round(255 v) (half away from zero),
+// saturated to [0, 255], NaN to 0.
+#include <cmath>
+
+#include "common.cuh"
+
+namespace nr {
+
+constexpr int DE_MAX_WEIGHTS = 16;
+
+struct DeWeights {
+    double w[DE_MAX_WEIGHTS];
+    int k;
+    int masked;        // 1: he and le multiplied by (he > level) first
+    double level;
+};
+
+__device__ __forceinline__ int im8_bin(double v) {
+    if (!(v == v)) return 0;
+    const double r = round(255.0 * v);   // CUDA round(): half away from zero
+    return r <= 0.0 ? 0 : (r >= 255.0 ? 255 : (int)r);
+}
+
+__device__ __forceinline__ double de_value(double h, double l, double w) {
+    return __dadd_rn(h, -__dmul_rn(l, w));
+}
+
+// d[k][i] = float(he[i] - le[i] * w_k), four voxels per thread per step.
+__global__ void __launch_bounds__(256) de_subtract_kernel(const float* __restrict__ he,
+                                                          const float* __restrict__ le,
+                                                          float* __restrict__ d, int64_t n,
+                                                          const __grid_constant__ DeWeights W) {
+    const int64_t n4 = n / 4;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4; q += stride) {
+        const float4 h4 = __ldg(reinterpret_cast<const float4*>(he) + q);
+        const float4 l4 = __ldg(reinterpret_cast<const float4*>(le) + q);
+        double h[4] = {h4.x, h4.y, h4.z, h4.w};
+        double l[4] = {l4.x, l4.y, l4.z, l4.w};
+        if (W.masked)
+            for (int t = 0; t < 4; t++)
+                if (!(h[t] > W.level)) h[t] = l[t] = 0.0;
+        for (int k = 0; k < W.k; k++) {
+            float4 o;
+            o.x = __double2float_rn(de_value(h[0], l[0], W.w[k]));
+            o.y = __double2float_rn(de_value(h[1], l[1], W.w[k]));
+            o.z = __double2float_rn(de_value(h[2], l[2], W.w[k]));
+            o.w = __double2float_rn(de_value(h[3], l[3], W.w[k]));
+            __stcs(reinterpret_cast<float4*>(d + (int64_t)k * n) + q, o);
+        }
+    }
+    // the n % 4 tail
+    for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        double h = he[i], l = le[i];
+        if (W.masked && !(h > W.level)) h = l = 0.0;
+        for (int k = 0; k < W.k; k++)
+            d[(int64_t)k * n + i] = __double2float_rn(de_value(h, l, W.w[k]));
+    }
+}
+
+// hist[k][b] += voxels of [begin, begin + len) whose double d_k falls in bin
+// b; the double value (before rounding to float) as MATLAB's entropy sees it.
+__global__ void __launch_bounds__(256) de_hist_kernel(const float* __restrict__ he,
+                                                      const float* __restrict__ le,
+                                                      int64_t begin, int64_t len,
+                                                      int* __restrict__ hist,
+                                                      const __grid_constant__ DeWeights W) {
+    __shared__ int sh[DE_MAX_WEIGHTS * 256];
+    for (int t = threadIdx.x; t < W.k * 256; t += blockDim.x) sh[t] = 0;
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double h = he[begin + i], l = le[begin + i];
+        if (W.masked && !(h > W.level)) h = l = 0.0;
+        for (int k = 0; k < W.k; k++) atomicAdd(&sh[k * 256 + im8_bin(de_value(h, l, W.w[k]))], 1);
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < W.k * 256; t += blockDim.x)
+        if (sh[t]) atomicAdd(&hist[t], sh[t]);
+}
+
+// hist[b] += voxels of x in bin b (graythresh's 8-bit histogram).
+__global__ void __launch_bounds__(256) hist8_kernel(const float* __restrict__ x, int64_t n,
+                                                    int* __restrict__ hist) {
+    __shared__ int sh[256];
+    sh[threadIdx.x] = 0;
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&sh[im8_bin((double)x[i])], 1);
+    __syncthreads();
+    if (sh[threadIdx.x]) atomicAdd(&hist[threadIdx.x], sh[threadIdx.x]);
+}
+
+static unsigned de_blocks(int64_t work) {
+    int64_t b = (work + 255) / 256;
+    return (unsigned)(b > 152 * 16 ? 152 * 16 : (b < 1 ? 1 : b));
+}
+
+}  // namespace nr
+
+using namespace nr;
+
+NR_API nr_status nr_de_subtract(const float* he, const float* le, const double* weights,
+                                int32_t n_weights, int64_t n, double mask_level, float* d,
+                                int64_t hist_begin, int64_t hist_len, int32_t* hist,
+                                void* stream) {
+    if (!he || !le || !weights || !d || n < 0) return NR_ERR_BAD_ARGUMENT;
+    if (n_weights < 1 || n_weights > DE_MAX_WEIGHTS) return NR_ERR_BAD_ARGUMENT;
+    if (hist && (hist_begin < 0 || hist_len < 0 || hist_begin + hist_len > n))
+        return NR_ERR_BAD_ARGUMENT;
+    if (((uintptr_t)he | (uintptr_t)le | (uintptr_t)d) & 15) return NR_ERR_BAD_ARGUMENT;
+    DeWeights W;
+    for (int k = 0; k < n_weights; k++) W.w[k] = weights[k];
+    for (int k = n_weights; k < DE_MAX_WEIGHTS; k++) W.w[k] = 0.0;
+    W.k = n_weights;
+    W.masked = mask_level >= 0.0;
+    W.level = mask_level;
+    cudaStream_t s = as_stream(stream);
+    if (n > 0)
+        de_subtract_kernel<<<de_blocks(n / 4 + 1), 256, 0, s>>>(he, le, d, n, W);
+    if (hist) {
+        if (cudaMemsetAsync(hist, 0, (size_t)n_weights * 256 * sizeof(int32_t), s) != cudaSuccess)
+            return NR_ERR_CUDA;
+        if (hist_len > 0)
+            de_hist_kernel<<<de_blocks(hist_len), 256, 0, s>>>(he, le, hist_begin, hist_len,
+                                                               hist, W);
+    }
+    return launch_status();
+}
+
+NR_API nr_status nr_hist8(const float* x, int64_t n, int32_t* hist, void* stream) {
+    if (!x || !hist || n < 0) return NR_ERR_BAD_ARGUMENT;
+    cudaStream_t s = as_stream(stream);
+    if (cudaMemsetAsync(hist, 0, 256 * sizeof(int32_t), s) != cudaSuccess) return NR_ERR_CUDA;
+    if (n > 0) hist8_kernel<<<de_blocks(n), 256, 0, s>>>(x, n, hist);
+    return launch_status();
+}
+
+// Host: Shannon entropy (bits) of a 256-bin histogram of `count` values,
+// -sum p log2 p over the non-empty bins, p = hist / count.
+NR_API nr_status nr_hist_entropy(const int32_t* hist, int64_t count, double* entropy) {
+    if (!hist || !entropy || count <= 0) return NR_ERR_BAD_ARGUMENT;
+    double e = 0.0;
+    for (int b = 0; b < 256; b++) {
+        if (hist[b] <= 0) continue;
+        const double p = (double)hist[b] / (double)count;
+        e -= p * std::log2(p);
+    }
+    *entropy = e;
+    return NR_OK;
+}
+
+// Host: Otsu's threshold (Otsu 1979) of a 256-bin histogram: the bin k that
+// maximises the between-class variance (mu_T w(k) - mu(k))^2 / (w(k)(1 - w(k))),
+// w and mu the cumulative class probability and first moment; with several
+// maxima the mean of their indices; returned as k / 255 (0 when the maximum is
+// not finite, e.g. one occupied bin).
+NR_API nr_status nr_otsu_level(const int32_t* hist, double* level) {
+    if (!hist || !level) return NR_ERR_BAD_ARGUMENT;
+    double total = 0.0;
+    for (int b = 0; b < 256; b++) total += hist[b] > 0 ? (double)hist[b] : 0.0;
+    if (!(total > 0.0)) return NR_ERR_BAD_ARGUMENT;
+    double sb[256], w = 0.0, mu = 0.0, mu_t = 0.0;
+    for (int b = 0; b < 256; b++) mu_t += (hist[b] > 0 ? hist[b] / total : 0.0) * (b + 1);
+    double best = -1.0;
+    for (int b = 0; b < 256; b++) {
+        const double p = hist[b] > 0 ? hist[b] / total : 0.0;
+        w += p;
+        mu += p * (b + 1);
+        const double num = mu_t * w - mu;
+        sb[b] = num * num / (w * (1.0 - w));
+        if (sb[b] > best) best = sb[b];   // NaN/inf never win: compared below
+    }
+    if (!(best >= 0.0) || !(best < INFINITY)) {
+        *level = 0.0;
+        return NR_OK;
+    }
+    double sum = 0.0;
+    int cnt = 0;
+    for (int b = 0; b < 256; b++)
+        if (sb[b] == best) {
+            sum += b + 1;
+            cnt++;
+        }
+    *level = (sum / cnt - 1.0) / 255.0;
+    return NR_OK;
+}

@@ -61,6 +61,53 @@ __global__ void __launch_bounds__(128) fp_sart_kernel(const __grid_constant__ Ge
     }
 }
 
+// 2 x 2 super-sampled projection: the fixed fprojectCB1_4R_GPU_SART
+// (Tomo_OSTR.cu:1453-1550, 2398-2433).  One thread per sub-ray: sub-bin
+// (is, js) of the 2 BINSx x 2 BINSy sub-detector, centre
+// x_d0 + (is + 0.5) Bsize_x / 2 (:1491-1492); a block is 32 x 8 sub-rays =
+// 16 x 4 bins of one view.  Bin (i, j) gets (((s00 + s10) + s01) + s11) / 4,
+// s_ab the sub-ray (2i+a, 2j+b) with missed sub-rays 0 -- the merge of
+// :1517-1550 as intended (there the fourth index is never assigned and the
+// sub-ray buffer is read as the caller left it) -- times cos theta when COS.
+// out: JI ? [view][j][i] (the reference merge's layout) : [view][i][j].
+// sub, when given: [view][2 BINSy][2 BINSx] sub-ray sums (missed untouched).
+template <bool COS, bool JI>
+__global__ void __launch_bounds__(256) fp_4r_kernel(const __grid_constant__ Geo G,
+                                                    const float* __restrict__ vol,
+                                                    float* __restrict__ out,
+                                                    float* __restrict__ sub,
+                                                    const float* __restrict__ angles,
+                                                    const int32_t* __restrict__ index, int a0) {
+    __shared__ ViewSrc src;
+    __shared__ float tile[8][33];
+    const nr_geom& g = G.g;
+    const int a = a0 + blockIdx.z;
+    if (threadIdx.x == 0 && threadIdx.y == 0) src = view_source(g, angles[index[a]]);
+    __syncthreads();
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int is = blockIdx.x * 32 + tx, js = blockIdx.y * 8 + ty;
+    const int nbx2 = 2 * g.nbx, nby2 = 2 * g.nby;
+    const bool on = is < nbx2 && js < nby2;
+    float v = 0.f;
+    if (on) {
+        const float x1 = __fmaf_rn((float)is + 0.5f, 0.5f * g.bx, g.x_d0);
+        const float y1 = __fmaf_rn((float)js + 0.5f, 0.5f * g.by, g.y_d0);
+        float sm;
+        if (trace<0>(G, vol, src.x0, src.y0, src.z0, x1, y1, -g.detectorR, &sm)) {
+            v = sm;
+            if (sub) sub[((int64_t)blockIdx.z * nby2 + js) * nbx2 + is] = sm;
+        }
+    }
+    tile[ty][tx] = v;
+    __syncthreads();
+    if (on && ((tx | ty) & 1) == 0) {
+        float m = (((tile[ty][tx] + tile[ty][tx + 1]) + tile[ty + 1][tx]) + tile[ty + 1][tx + 1]) *
+                  0.25f;
+        if (COS) m = m * src.ct;
+        out[(int64_t)blockIdx.z * g.nbx * g.nby + bin_off<JI>(g, is >> 1, js >> 1)] = m;
+    }
+}
+
 // Fused forward projection + h, one block per 32 x 4 bins of one subset view;
 // K Siddon steps per gather round.
 template <int K>
@@ -162,6 +209,32 @@ NR_API nr_status nr_fp_sart(const nr_geom* g, const float* x, float* prj_est, fl
     else
         fp_sart_kernel<false><<<grd, blk, 0, as_stream(stream)>>>(make_geo(*g), x, prj_est,
                                                                   normprj, angles, index, a0);
+    return launch_status();
+}
+
+NR_API nr_status nr_fp_4r(const nr_geom* g, const float* x, float* prj, float* sub,
+                          const float* angles, const int32_t* index, int32_t a0, int32_t a1,
+                          int32_t use_cos, int32_t layout, void* stream) {
+    nr_status st = check_views(g, angles, index, a0, a1);
+    if (st != NR_OK) return st;
+    if (!x || !prj || prj == sub || (layout != NR_LAYOUT_IJ && layout != NR_LAYOUT_JI))
+        return NR_ERR_BAD_ARGUMENT;
+    if ((int64_t)4 * g->nbx * g->nby * (a1 - a0) >= (int64_t)1 << 31) return NR_ERR_BAD_GEOMETRY;
+    if (a1 == a0) return NR_OK;
+    dim3 blk(32, 8), grd(cdiv(2 * (int64_t)g->nbx, 32), cdiv(2 * (int64_t)g->nby, 8), a1 - a0);
+    const Geo G = make_geo(*g);
+    cudaStream_t s = as_stream(stream);
+    if (use_cos) {
+        if (layout == NR_LAYOUT_JI)
+            fp_4r_kernel<true, true><<<grd, blk, 0, s>>>(G, x, prj, sub, angles, index, a0);
+        else
+            fp_4r_kernel<true, false><<<grd, blk, 0, s>>>(G, x, prj, sub, angles, index, a0);
+    } else {
+        if (layout == NR_LAYOUT_JI)
+            fp_4r_kernel<false, true><<<grd, blk, 0, s>>>(G, x, prj, sub, angles, index, a0);
+        else
+            fp_4r_kernel<false, false><<<grd, blk, 0, s>>>(G, x, prj, sub, angles, index, a0);
+    }
     return launch_status();
 }
 

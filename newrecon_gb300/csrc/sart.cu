@@ -11,7 +11,10 @@
 // Two launches per sub-iteration:
 //   sart_fp_diff_kernel  one thread per subset bin: Siddon sum, the
 //                        difference against the stored line integral, divided
-//                        by the ray's chord (0 where the chord is 0)
+//                        by the ray's chord (0 where the chord is 0); with
+//                        supersample, sart_fp_diff_4r_kernel does the same on
+//                        the mean of 2 x 2 sub-rays per bin (nr_fp_4r's
+//                        projector) against their mean chord
 //   sart_update_kernel   the fused update tile of update.cuh in its OS-SART
 //                        kinds: sensitivity-normalised back projection, the
 //                        hyperbola prior from the 3-plane ring, the step and
@@ -100,6 +103,7 @@ nr_status sart_check_params(const nr_geom* g, const nr_sart_params* p) {
         return NR_ERR_BAD_ARGUMENT;
     if (p->upd_planes != 0 && p->upd_planes != 8 && p->upd_planes != 16 && p->upd_planes != 32)
         return NR_ERR_BAD_ARGUMENT;
+    if (p->supersample != 0 && p->supersample != 1) return NR_ERR_BAD_ARGUMENT;
     if (g->ny > 65535 || g->nz > 65535 || g->n_angles > 65535) return NR_ERR_BAD_GEOMETRY;
     return NR_OK;
 }
@@ -162,6 +166,72 @@ __global__ void __launch_bounds__(128) sart_fp_diff_kernel(
     diff[(int64_t)blockIdx.z * B + off] = out;
 }
 
+// The 2 x 2 super-sampled forms (supersample = 1; the projector of nr_fp_4r):
+// one thread per sub-ray, 32 x 8 sub-rays = 16 x 4 bins per block, the four
+// sub-rays of a bin merged in shared memory in the order of nr_fp_4r.
+// MODE 1 traces chords (set-up), MODE 0 line integrals.
+template <int MODE>
+__device__ __forceinline__ bool sub_ray_merge(const Geo& G, const float* __restrict__ vol,
+                                              const ViewSrc& src, float (*tile)[33], float* m,
+                                              int* i, int* j) {
+    const nr_geom& g = G.g;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int is = blockIdx.x * 32 + tx, js = blockIdx.y * 8 + ty;
+    const bool on = is < 2 * g.nbx && js < 2 * g.nby;
+    float v = 0.f;
+    if (on) {
+        const float x1 = __fmaf_rn((float)is + 0.5f, 0.5f * g.bx, g.x_d0);
+        const float y1 = __fmaf_rn((float)js + 0.5f, 0.5f * g.by, g.y_d0);
+        float t;
+        if (trace<MODE>(G, vol, src.x0, src.y0, src.z0, x1, y1, -g.detectorR, &t)) v = t;
+    }
+    tile[ty][tx] = v;
+    __syncthreads();
+    if (!on || ((tx | ty) & 1) != 0) return false;
+    *m = (((tile[ty][tx] + tile[ty][tx + 1]) + tile[ty + 1][tx]) + tile[ty + 1][tx + 1]) * 0.25f;
+    *i = is >> 1;
+    *j = js >> 1;
+    return true;
+}
+
+__global__ void __launch_bounds__(256) sart_norm_4r_kernel(const __grid_constant__ Geo G,
+                                                           float* __restrict__ norm,
+                                                           const float* __restrict__ angles,
+                                                           const int32_t* __restrict__ index) {
+    __shared__ ViewSrc src;
+    __shared__ float tile[8][33];
+    const nr_geom& g = G.g;
+    const int a = blockIdx.z;
+    if (threadIdx.x == 0 && threadIdx.y == 0) src = view_source(g, angles[index[a]]);
+    __syncthreads();
+    float m;
+    int i, j;
+    if (sub_ray_merge<1>(G, nullptr, src, tile, &m, &i, &j))
+        norm[(int64_t)a * g.nbx * g.nby + bin_off<true>(g, i, j)] = m;
+}
+
+template <bool COS>
+__global__ void __launch_bounds__(256) sart_fp_diff_4r_kernel(
+    const __grid_constant__ Geo G, const float* __restrict__ vol, float* __restrict__ diff,
+    const float* __restrict__ angles, const int32_t* __restrict__ index, int a0,
+    const float* __restrict__ p, const float* __restrict__ norm) {
+    __shared__ ViewSrc src;
+    __shared__ float tile[8][33];
+    const nr_geom& g = G.g;
+    const int a = a0 + blockIdx.z;
+    if (threadIdx.x == 0 && threadIdx.y == 0) src = view_source(g, angles[index[a]]);
+    __syncthreads();
+    float m;
+    int i, j;
+    if (!sub_ray_merge<0>(G, vol, src, tile, &m, &i, &j)) return;
+    const int64_t B = (int64_t)g.nbx * g.nby;
+    const int64_t off = bin_off<true>(g, i, j);
+    const float nv = norm[(int64_t)a * B + off];
+    const float est = COS ? m * src.ct : m;
+    diff[(int64_t)blockIdx.z * B + off] = nv != 0.f ? __fdiv_rn(p[(int64_t)a * B + off] - est, nv)
+                                                    : 0.f;
+}
+
 template <int KIND, int ZC>
 __global__ void __launch_bounds__(256) sart_update_kernel(
     const __grid_constant__ Geo G, const __grid_constant__ PriorW5 W,
@@ -178,9 +248,15 @@ namespace {
 
 template <bool COS>
 nr_status launch_fp_diff_c(const nr_geom& g, int k, const float* x, const SartWS& w, int a0,
-                           int nv, cudaStream_t s) {
-    dim3 blk(32, 4), grd(cdiv(g.nbx, 32), cdiv(g.nby, 4), nv);
+                           int nv, bool ss, cudaStream_t s) {
     const Geo G = make_geo(g);
+    if (ss) {
+        dim3 blk(32, 8), grd(cdiv(2 * (int64_t)g.nbx, 32), cdiv(2 * (int64_t)g.nby, 8), nv);
+        sart_fp_diff_4r_kernel<COS><<<grd, blk, 0, s>>>(G, x, w.diff, w.angles, w.index, a0, w.p,
+                                                         w.norm);
+        return launch_status();
+    }
+    dim3 blk(32, 4), grd(cdiv(g.nbx, 32), cdiv(g.nby, 4), nv);
     if (k == 2)
         sart_fp_diff_kernel<2, COS><<<grd, blk, 0, s>>>(G, x, w.diff, w.angles, w.index, a0, w.p,
                                                         w.norm);
@@ -218,8 +294,8 @@ nr_status launch_sart_update_z(const nr_geom& g, const nr_sart_params& p, const 
 nr_status sart_project(const nr_geom& g, const nr_sart_params& p, const float* x, int subset,
                        const SartWS& w, cudaStream_t s) {
     const int Vs = g.n_angles / p.subset_num, a0 = subset * Vs;
-    return p.use_cos ? launch_fp_diff_c<true>(g, p.fp_batch, x, w, a0, Vs, s)
-                     : launch_fp_diff_c<false>(g, p.fp_batch, x, w, a0, Vs, s);
+    return p.use_cos ? launch_fp_diff_c<true>(g, p.fp_batch, x, w, a0, Vs, p.supersample, s)
+                     : launch_fp_diff_c<false>(g, p.fp_batch, x, w, a0, Vs, p.supersample, s);
 }
 
 nr_status sart_update(const nr_geom& g, const nr_sart_params& p, const float* x, float* x_out,
@@ -284,8 +360,13 @@ NR_API nr_status nr_sart_setup(const nr_geom* g, const nr_sart_params* p, const 
     if ((st = launch_subset_index(w.index, angles, w.angles, A, M, s)) != NR_OK) return st;
     // [view][i][j] original order -> [view][j][i] subset order.
     if ((st = launch_transpose(w.p, line, g->nbx, g->nby, A, M, Vs, s)) != NR_OK) return st;
-    dim3 blk(32, 4), grd(cdiv(g->nbx, 32), cdiv(g->nby, 4), A);
-    sart_norm_kernel<<<grd, blk, 0, s>>>(make_geo(*g), w.norm, w.angles, w.index);
+    if (p->supersample) {
+        dim3 blk(32, 8), grd(cdiv(2 * (int64_t)g->nbx, 32), cdiv(2 * (int64_t)g->nby, 8), A);
+        sart_norm_4r_kernel<<<grd, blk, 0, s>>>(make_geo(*g), w.norm, w.angles, w.index);
+    } else {
+        dim3 blk(32, 4), grd(cdiv(g->nbx, 32), cdiv(g->nby, 4), A);
+        sart_norm_kernel<<<grd, blk, 0, s>>>(make_geo(*g), w.norm, w.angles, w.index);
+    }
     return launch_status();
 }
 

@@ -55,6 +55,7 @@ class NrSartParams(ctypes.Structure):
         ("regularized", ctypes.c_int32), ("fp_batch", ctypes.c_int32),
         ("upd_planes", ctypes.c_int32), ("lam", ctypes.c_float),
         ("beta", ctypes.c_float), ("delta", ctypes.c_float),
+        ("supersample", ctypes.c_int32),
     ]
 
 

@@ -76,6 +76,7 @@ SIGNATURES = {
     "nr_ostr_check": (_I32, [_P, ctypes.c_size_t, ctypes.POINTER(_I32), _P]),
     "nr_penalty_fp64_static": (_I32, [_GP, _P, _I32, _F, _P, _P]),
     "nr_fp_sart": (_I32, [_GP, _P, _P, _P, _P, _P, _I32, _I32, _I32, _P]),
+    "nr_fp_4r": (_I32, [_GP, _P, _P, _P, _P, _P, _I32, _I32, _I32, _I32, _P]),
     "nr_sart_prj_diff": (_I32, [_P, _P, _P, _P, _I64, _P]),
     "nr_bp_ossart": (_I32, [_GP, _P, _P, _P, _P, _P, _I32, _I32, _F, _F, _P]),
     "nr_prior_sart": (_I32, [_GP, _P, _P, _F, _P]),
@@ -91,6 +92,10 @@ SIGNATURES = {
     "nr_sart_workspace_section": (_I32, [_GP, _SP, _I32, _P, ctypes.c_size_t,
                                          ctypes.POINTER(ctypes.c_void_p),
                                          ctypes.POINTER(ctypes.c_size_t)]),
+    "nr_de_subtract": (_I32, [_P, _P, _P, _I32, _I64, ctypes.c_double, _P, _I64, _I64, _P, _P]),
+    "nr_hist8": (_I32, [_P, _I64, _P, _P]),
+    "nr_hist_entropy": (_I32, [_P, _I64, ctypes.POINTER(ctypes.c_double)]),
+    "nr_otsu_level": (_I32, [_P, ctypes.POINTER(ctypes.c_double)]),
     "nr_version": (ctypes.c_char_p, []),
 }
 

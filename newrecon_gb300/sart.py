@@ -6,6 +6,8 @@ names and arguments, reading the geometry from the module-level names of
 
 * ``fprojectCB_1R_GPU_SART`` / ``fprojectCB_1R_GPU_SART_cos``: line integral
   (times cos theta) and the ray's in-volume chord; missed rays untouched;
+* ``fprojectCB1_4R_GPU_SART``: the 2 x 2 super-sampled projector, fixed
+  (the reference's does not compile and never sets its fourth sub-ray index);
 * ``SART_prj_diff``: (prj - est) / normprj, 0 where normprj is 0;
 * ``bprojectCB_4B_GPU_SART`` / ``bprojectCB_4B_GPU_SART_R``: the in-place
   OS-SART update x = max(0, x + lambda (u [+ beta prior]) / sensitivity);
@@ -50,6 +52,38 @@ def fprojectCB_1R_GPU_SART_cos(estbuf, prj_est, d_normprj, d_angles, d_index, an
                                angleEnd):
     """As fprojectCB_1R_GPU_SART with prj_est times cos(theta) (Tomo_OSTR.cu:2306)."""
     _fp_sart(estbuf, prj_est, d_normprj, d_angles, d_index, angleStart, angleEnd, 1)
+
+
+def fprojectCB1_4R_GPU_SART(d_objbuf, d_prjbuf, d_4R_prjbuf, d_angles, d_index, angleStart,
+                            angleEnd):
+    """d_prjbuf = mean of the 2 x 2 sub-ray line integrals per bin, [view][j][i] as the
+    reference's merge writes it; d_4R_prjbuf (may be None) gets the sub-ray sums
+    [view][2 BINSy][2 BINSx].  The fixed Tomo_OSTR.cu:2398 (see nr_fp_4r)."""
+    gp, g = _geom_c()
+    x = _in(d_objbuf)
+    out = _Out(d_prjbuf)
+    sub = None if d_4R_prjbuf is None else _Out(d_4R_prjbuf)
+    ang = _in(d_angles)
+    idx = _in(d_index, torch.int32)
+    native.call("nr_fp_4r", gp, _p(x), out.ptr(), None if sub is None else sub.ptr(), _p(ang),
+                _p(idx), int(angleStart), int(angleEnd), 0, 1, _stream())
+    out.done()
+    if sub is not None:
+        sub.done()
+
+
+def fproject_4R(estbuf, prj_est, d_angles, d_index, angleStart, angleEnd, use_cos=False,
+                layout="ij"):
+    """The 4R projector in either layout ("ij": [view][i][j] like the 1R projectors,
+    "ji": [view][j][i]) and optionally times cos(theta)."""
+    gp, g = _geom_c()
+    x = _in(estbuf)
+    out = _Out(prj_est)
+    ang = _in(d_angles)
+    idx = _in(d_index, torch.int32)
+    native.call("nr_fp_4r", gp, _p(x), out.ptr(), None, _p(ang), _p(idx), int(angleStart),
+                int(angleEnd), int(bool(use_cos)), {"ij": 0, "ji": 1}[layout], _stream())
+    out.done()
 
 
 def SART_prj_diff(diff_line, prjbuf, prj_est, normprj, d_index, angleStart, angleEnd):
@@ -123,12 +157,12 @@ class OSSART:
 
     def __init__(self, geom: Geometry, *, subset_num: int, lam: float, use_cos: bool = True,
                  regularized: bool = False, beta: float = 0.0, delta: float = 1.0,
-                 fp_batch: int = 0, upd_planes: int = 0):
+                 fp_batch: int = 0, upd_planes: int = 0, supersample: bool = False):
         geom.validate(subset_num)
         self.geom = geom
         self.params = NrSartParams(int(subset_num), int(bool(use_cos)), int(bool(regularized)),
                                    int(fp_batch), int(upd_planes), float(lam), float(beta),
-                                   float(delta))
+                                   float(delta), int(bool(supersample)))
         self.gc = geom.to_c()
         size = ctypes.c_size_t(0)
         native.call("nr_sart_workspace_size", ctypes.byref(self.gc), ctypes.byref(self.params),
@@ -228,14 +262,15 @@ class SartGraph:
 
 def ossart_reconstruct(geom: Geometry, line, *, angles, subset_num: int, iter_num: int,
                        lam: float, use_cos: bool = True, regularized: bool = False,
-                       beta: float = 0.0, delta: float = 1.0, x0=None):
+                       beta: float = 0.0, delta: float = 1.0, supersample: bool = False,
+                       x0=None):
     """OS-SART: line integrals [view][i][j] (original order) in, attenuation out.
 
     Returns the volume [z][y][x]; numpy when line was a host array, else a
     CUDA tensor.
     """
     plan = OSSART(geom, subset_num=subset_num, lam=lam, use_cos=use_cos,
-                  regularized=regularized, beta=beta, delta=delta)
+                  regularized=regularized, beta=beta, delta=delta, supersample=supersample)
     plan.setup(angles, line)
     if x0 is None:
         x = torch.zeros(geom.n_voxels, dtype=torch.float32, device=plan.ws.device)

@@ -8,12 +8,15 @@
 #                     612-1173 Siddon device functions (OSTR, normprj)
 #                    1177-1311 SART projector kernels (plain and _cos)
 #                    1313-1449 OSTR_cos and normprj kernels
+#                    1453-1515 the 4R sub-ray kernel (its undefined batch counts
+#                              come from ref/ref_shim.h; the merge kernel
+#                              :1517-1550 reads an unassigned index and is left out)
 #                    1553-1735 backprj_gpu_manyviews_SBP
 #                    1737-2183 backprj_OSSART{,_R}_gpu_manyviews, SART_prj_diff_kernel
 #   Tomo_OSTR_gold.cpp 22-1528 I/O, compute_yry/h, regroup, update_est,
 #                              both OSTR drivers, import_param, Reconstruction
-# The rest of Tomo_OSTR.cu (the 4R kernels with undefined symbols, launch
-# wrappers with <<< >>>, main) is left out; ref/ref_launch.inc stands in for the
+# The rest of Tomo_OSTR.cu (the 4R merge kernel, launch wrappers with
+# <<< >>>, main) is left out; ref/ref_launch.inc stands in for the
 # launch wrappers.  Tomo_OSTR.h / readdata.h /
 # helper_cuda.h are absent from the reference, so their includes (the first
 # lines of each file) are skipped.
@@ -28,7 +31,7 @@ fi
 mkdir -p "$OUT"
 {
     echo '#include "ref_shim.h"'
-    sed -n '18,116p;118,325p;327,610p;612,1173p;1177,1311p;1313,1449p;1553,1735p;1737,2183p' \
+    sed -n '18,116p;118,325p;327,610p;612,1173p;1177,1311p;1313,1449p;1453,1515p;1553,1735p;1737,2183p' \
         "$REF/Tomo_OSTR.cu"
     cat "$HERE/ref/ref_launch.inc"
     sed -n '22,1528p' "$REF/Tomo_OSTR_gold.cpp"

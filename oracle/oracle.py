@@ -189,6 +189,19 @@ class Oracle:
                             ctypes.c_int(a0), ctypes.c_int(a1), ctypes.c_int(int(bool(use_cos))))
         return est, norm
 
+    def fp_4r(self, g: Geometry, x, angles, index, a0: int, a1: int, use_cos: bool = False,
+              layout: str = "ji", sub=None) -> np.ndarray:
+        """The fixed 2 x 2 super-sampled projector; sub (optional) gets the sub-ray sums."""
+        x = self._arr(x).ravel()
+        out = np.zeros((a1 - a0) * g.n_bins, self.dtype)
+        gc = g.to_c()
+        self._fn("fp_4r")(ctypes.byref(gc), _ptr(x), _ptr(out), _ptr(sub),
+                          _ptr(np.ascontiguousarray(angles, np.float32)),
+                          _ptr(np.ascontiguousarray(index, np.int32)), ctypes.c_int(a0),
+                          ctypes.c_int(a1), ctypes.c_int(int(bool(use_cos))),
+                          ctypes.c_int({"ij": 0, "ji": 1}[layout]))
+        return out
+
     def sart_prj_diff(self, prj, est, norm) -> np.ndarray:
         prj, est, norm = self._arr(prj).ravel(), self._arr(est).ravel(), self._arr(norm).ravel()
         out = np.empty_like(prj)
@@ -226,10 +239,10 @@ class Oracle:
 
     def ossart(self, g: Geometry, angles, line, *, subset_num: int, iter_num: int, lam: float,
                use_cos: bool = True, regularized: bool = False, beta: float = 0.0,
-               delta: float = 1.0, x0=None) -> np.ndarray:
+               delta: float = 1.0, supersample: bool = False, x0=None) -> np.ndarray:
         """The OS-SART loop (nr_sart_iterate's semantics)."""
         p = NrSartParams(subset_num, int(bool(use_cos)), int(bool(regularized)), 0, 0, lam, beta,
-                         delta)
+                         delta, int(bool(supersample)))
         gc = g.to_c()
         x = np.zeros(g.n_voxels, self.dtype) if x0 is None else self._arr(x0).ravel().copy()
         self._fn("ossart")(ctypes.byref(gc), ctypes.byref(p),
@@ -326,6 +339,15 @@ class Reference:
                              _ptr(np.ascontiguousarray(index, np.int32)), ctypes.c_int(a0),
                              ctypes.c_int(a1), ctypes.c_int(int(bool(use_cos))))
         return est, norm
+
+    def fp_4r_subrays(self, x, angles, index, a0, a1):
+        """The reference's 4R sub-ray kernel: [view][2 BINSy][2 BINSx], zero-initialised."""
+        g = self.g
+        sub = np.zeros((a1 - a0) * 4 * g.n_bins, np.float32)
+        self.lib.ref_fp_4r_subrays(_ptr(self._f(x)), _ptr(sub), _ptr(self._f(angles)),
+                                   _ptr(np.ascontiguousarray(index, np.int32)),
+                                   ctypes.c_int(a0), ctypes.c_int(a1))
+        return sub
 
     def sart_prj_diff(self, prj, est, norm, index, a0, a1):
         out = np.zeros(np.size(prj), np.float32)

@@ -371,6 +371,47 @@ void fp_sart(const nr_geom& g, const R* vol, R* est, R* norm, const float* angle
     }
 }
 
+// 2 x 2 super-sampled projection, the fixed fprojectCB1_4R_GPU_SART: the
+// sub-ray kernel ray_trace_4R_gpu_manyangles_direct_notexturememory
+// (Tomo_OSTR.cu:1453-1515: sub-bin centre x_d0 + (i+0.5)/2*Bsize_x in double,
+// plain line integral, sub layout [view][2 BINSy][2 BINSx], missed untouched)
+// and the merge merge_4R_to_1R_global (:1517-1550) as intended: the four
+// sub-rays (2i,2j), (2i+1,2j), (2i,2j+1), (2i+1,2j+1) summed in that order,
+// / 4, with missed sub-rays 0 (a zeroed sub-ray buffer).  The merged value is
+// multiplied by cos theta with use_cos; layout 0 writes [view][i][j], 1
+// [view][j][i] (the merge's).
+template <class R>
+void fp_4r(const nr_geom& g, const R* vol, R* prj, R* sub, const float* angles,
+           const int32_t* index, int a0, int a1, int use_cos, int layout) {
+    typedef RT<R> M;
+    const int NBX = g.nbx, NBY = g.nby, NBX2 = 2 * NBX, NBY2 = 2 * NBY;
+    std::vector<R> s4((size_t)NBX2 * NBY2);
+    for (int a = a0; a < a1; a++) {
+        const R theta = (R)angles[index[a]];
+        const R st = M::sin_(theta), ct = M::cos_(theta);
+        const R x0 = (R)g.sourceR * st, z0 = (R)g.sourceR * ct, y0 = (R)g.sourceY;
+#pragma omp parallel for schedule(dynamic, 4)
+        for (int js = 0; js < NBY2; js++)
+            for (int is = 0; is < NBX2; is++) {
+                const R x1 = (R)((double)g.x_d0 + (is + 0.5) / 2 * (double)g.bx);
+                const R y1 = (R)((double)g.y_d0 + (js + 0.5) / 2 * (double)g.by);
+                R v;
+                const bool hit = ray_trace<R>(g, vol, x0, y0, z0, x1, y1, -(R)g.detectorR, 0, &v);
+                s4[(size_t)js * NBX2 + is] = hit ? v : (R)0;
+                if (hit && sub) sub[((size_t)(a - a0) * NBY2 + js) * NBX2 + is] = v;
+            }
+        for (int j = 0; j < NBY; j++)
+            for (int i = 0; i < NBX; i++) {
+                const R* r0 = &s4[(size_t)(2 * j) * NBX2 + 2 * i];
+                const R* r1 = r0 + NBX2;
+                R m = (((r0[0] + r0[1]) + r1[0]) + r1[1]) / 4;
+                if (use_cos) m = m * ct;
+                const size_t o = layout ? (size_t)j * NBX + i : (size_t)i * NBY + j;
+                prj[(size_t)(a - a0) * NBX * NBY + o] = m;
+            }
+    }
+}
+
 // SART_prj_diff_kernel, Tomo_OSTR.cu:2145-2183.
 template <class R>
 void sart_prj_diff(R* diff, const R* prj, const R* est, const R* norm, int64_t n) {
@@ -597,6 +638,36 @@ void subiter(const nr_geom& g, const nr_ostr_params& p, const float* angles,
     update_est<R>(x, capL.data(), RD.data(), d, RDD.data(), (R)p.beta, N);
 }
 
+// Mean in-volume chord of the 2 x 2 sub-rays of each bin ([view][i][j]), merged
+// in the order of fp_4r, missed sub-rays 0: the normprj of the super-sampled
+// OS-SART loop.
+template <class R>
+void fp_4r_chord(const nr_geom& g, R* norm, const float* angles, const int32_t* index, int a0,
+                 int a1) {
+    typedef RT<R> M;
+    const int NBX = g.nbx, NBY = g.nby;
+    for (int a = a0; a < a1; a++) {
+        const R theta = (R)angles[index[a]];
+        const R st = M::sin_(theta), ct = M::cos_(theta);
+        const R x0 = (R)g.sourceR * st, z0 = (R)g.sourceR * ct, y0 = (R)g.sourceY;
+#pragma omp parallel for schedule(dynamic, 4)
+        for (int i = 0; i < NBX; i++)
+            for (int j = 0; j < NBY; j++) {
+                R c[4];
+                for (int k = 0; k < 4; k++) {
+                    const int is = 2 * i + (k & 1), js = 2 * j + (k >> 1);
+                    const R x1 = (R)((double)g.x_d0 + (is + 0.5) / 2 * (double)g.bx);
+                    const R y1 = (R)((double)g.y_d0 + (js + 0.5) / 2 * (double)g.by);
+                    R v;
+                    c[k] = ray_trace<R>(g, (const R*)nullptr, x0, y0, z0, x1, y1,
+                                        -(R)g.detectorR, 1, &v) ? v : (R)0;
+                }
+                norm[(size_t)(a - a0) * NBX * NBY + (size_t)i * NBY + j] =
+                    (((c[0] + c[1]) + c[2]) + c[3]) / 4;
+            }
+    }
+}
+
 // The OS-SART loop of the device-resident path: line integrals ([view][i][j],
 // original order) regrouped to subset order, subset-major index
 // (Tomo_OSTR_gold.cpp:628-642); per iteration and subset: est, norm zeroed
@@ -619,7 +690,14 @@ void ossart(const nr_geom& g, const nr_sart_params& p, const float* angles, cons
             const int a0 = a * Vs, a1 = a0 + Vs;
             std::fill(est.begin(), est.end(), (R)0);
             std::fill(norm.begin(), norm.end(), (R)0);
-            fp_sart<R>(g, x, est.data(), norm.data(), angles, index.data(), a0, a1, p.use_cos);
+            if (p.supersample) {
+                // 2 x 2 sub-rays: the merged projection and the merged chord
+                fp_4r<R>(g, x, est.data(), nullptr, angles, index.data(), a0, a1, p.use_cos, 0);
+                fp_4r_chord<R>(g, norm.data(), angles, index.data(), a0, a1);
+            } else {
+                fp_sart<R>(g, x, est.data(), norm.data(), angles, index.data(), a0, a1,
+                           p.use_cos);
+            }
             sart_prj_diff<R>(diff.data(), line.data() + (size_t)a0 * B, est.data(), norm.data(),
                              (int64_t)Vs * B);
             if (p.regularized) {
@@ -690,6 +768,11 @@ void ossart(const nr_geom& g, const nr_sart_params& p, const float* angles, cons
                                       const float* angles, const int32_t* index,        \
                                       int a0, int a1, int use_cos) {                    \
         fp_sart<R>(*g, x, est, norm, angles, index, a0, a1, use_cos);                   \
+    }                                                                                   \
+    ORC_EXPORT void orc_fp_4r_##SUF(const nr_geom* g, const R* x, R* prj, R* sub,         \
+                                    const float* angles, const int32_t* index, int a0,  \
+                                    int a1, int use_cos, int layout) {                  \
+        fp_4r<R>(*g, x, prj, sub, angles, index, a0, a1, use_cos, layout);              \
     }                                                                                   \
     ORC_EXPORT void orc_sart_prj_diff_##SUF(R* diff, const R* prj, const R* est,        \
                                             const R* norm, int64_t n) {                 \

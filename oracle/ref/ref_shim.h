@@ -44,3 +44,7 @@ static inline int cudaDeviceSynchronize(void) { return 0; }
 // error paths; silence both.
 #define printf(...) ((void)0)
 #define system(x) 0
+
+// The reference's 4R sub-ray kernel (Tomo_OSTR.cu:1453-1515) reads two batch
+// counts that Tomo_OSTR.cu never defines; one batch covers the detector here.
+static int nBatchBINSx_4R = 1, nBatchBINSy_4R = 1;

@@ -23,8 +23,9 @@ Fixtures (all float32 unless noted):
 ``sart_tiny.npz``, ``sart_ragged.npz``
                 the SART family on the tiny and ragged cases: the SART
                 projector (plain and cos), the projection difference, the SART
-                prior, both OS-SART back projections, and OS-SART loops
-                composed from the reference's own launch wrappers.
+                prior, both OS-SART back projections, OS-SART loops
+                composed from the reference's own launch wrappers, and the
+                4R sub-rays of the reference's kernel with their merge.
 """
 from __future__ import annotations
 
@@ -115,6 +116,13 @@ def sart_set(name: str, g: Geometry, angles, subset_num, x, y, b, s, lam, beta, 
     out["bp_in"] = dif
     out["bp_plain"] = R.bp_ossart(x, dif, ridx, angles, Vs, 2 * Vs, lam)
     out["bp_reg"] = R.bp_ossart(x, dif, ridx, angles, Vs, 2 * Vs, lam, out["prior"], beta)
+    # the 4R sub-rays from the reference's kernel; the merge as intended
+    # (Tomo_OSTR.cu:1517-1550 with its fourth index assigned), in float32
+    sub = R.fp_4r_subrays(x, angles, idx, 0, A).reshape(A, 2 * g.nby, 2 * g.nbx)
+    out["fp4r_sub"] = sub.ravel()
+    s00, s10 = sub[:, 0::2, 0::2], sub[:, 0::2, 1::2]
+    s01, s11 = sub[:, 1::2, 0::2], sub[:, 1::2, 1::2]
+    out["fp4r_merged_ji"] = ((((s00 + s10) + s01) + s11) / np.float32(4)).astype(np.float32).ravel()
     out["ossart"] = R.ossart(angles, line, subset_num=subset_num, iter_num=iters, lam=lam,
                              use_cos=True)
     out["ossart_nocos"] = R.ossart(angles, line, subset_num=subset_num, iter_num=iters, lam=lam,

@@ -1,0 +1,106 @@
+"""Dual-energy subtraction on the GPU against the NumPy restatement of
+syncrecon.m (oracle/dual_energy_oracle.py): the subtraction and the 8-bit
+histograms are exact (bit-identical floats, identical counts), the entropies
+and Otsu levels equal to 1e-12."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+from oracle import dual_energy_oracle as de
+from test_oracle_golden import geom_of
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mod():
+    from newrecon_gb300 import dual_energy, native
+
+    native.load()
+    return dual_energy
+
+
+def volumes(shape, seed):
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = shape
+    he = rng.gamma(2.0, 0.02, size=nx * ny * nz).astype(np.float32)
+    le = (he * rng.uniform(1.1, 1.6, size=he.size) + rng.normal(0, 0.003, he.size)).astype(np.float32)
+    return he, le
+
+
+@pytest.mark.parametrize("shape", [(40, 24, 8), (33, 17, 5)], ids=["even", "tail"])
+def test_subtract_and_entropy_exact(mod, shape):
+    he, le = volumes(shape, 1)
+    w = list(mod.DEFAULT_WEIGHTS)
+    z = shape[2] // 2
+    d, ent = mod.subtract(torch.from_numpy(he).cuda(), torch.from_numpy(le).cuda(), w,
+                          slice_shape=shape[:2], entropy_slice=z)
+    ref, ref64 = de.subtract(he, le, w)
+    assert np.array_equal(d.cpu().numpy(), ref)
+    n2 = shape[0] * shape[1]
+    for k in range(len(w)):
+        assert ent[k] == pytest.approx(de.entropy(ref64[k, z * n2:(z + 1) * n2]), abs=1e-12)
+
+
+def test_mask_and_otsu(mod):
+    he, le = volumes((40, 24, 8), 2)
+    he[: he.size // 3] *= 6.0   # a second mode
+    t = mod.otsu_level(he)
+    assert t == de.otsu_level(de.hist8(he))
+    assert 0.0 < t < 1.0
+    d, _ = mod.subtract(he, le, [0.3, 0.6], mask_level=t)
+    ref, _ = de.subtract(he, le, [0.3, 0.6], mask_level=t)
+    assert np.array_equal(d.cpu().numpy(), ref)
+    assert (d.cpu().numpy()[:, he <= t] == 0).all()
+
+
+def test_syncrecon_files(mod, tmp_path):
+    shape = (33, 17, 5)
+    he, le = volumes(shape, 3)
+    he.tofile(tmp_path / "he.raw")
+    le.tofile(tmp_path / "le.raw")
+    got = mod.syncrecon(str(tmp_path / "he.raw"), str(tmp_path / "le.raw"), shape,
+                        str(tmp_path), entropy_slice=2, log=lambda *_: None)
+    ref, ref64 = de.subtract(he, le, mod.DEFAULT_WEIGHTS)
+    n2 = shape[0] * shape[1]
+    for k, w in enumerate(mod.DEFAULT_WEIGHTS):
+        f = tmp_path / f"d_{w:g}.raw"
+        assert f.exists(), f
+        assert np.array_equal(np.fromfile(f, np.float32), ref[k])
+        assert got[k][0] == w
+        assert got[k][1] == pytest.approx(de.entropy(ref64[k, 2 * n2:3 * n2]), abs=1e-12)
+
+
+def test_reconstruct_pair(mod):
+    """Two OSTR reconstructions and their subtraction without leaving the GPU."""
+    z = golden("tiny")
+    g = geom_of(z)
+    he_scan = dict(prj=z["y"], blank=z["b"])
+    le_scan = dict(prj=(z["y"] * 0.8).astype(np.float32), blank=(z["b"] * 0.8).astype(np.float32))
+    xh, xl, d, ent = mod.reconstruct_pair(g, he_scan, le_scan, [0.5, 1.0], angles=z["angles"],
+                                          subset_num=int(z["subset_num"]), iter_num=2,
+                                          beta=float(z["beta"]), delta=float(z["delta"]),
+                                          entropy_slice=3)
+    ref, _ = de.subtract(xh.cpu().numpy(), xl.cpu().numpy(), [0.5, 1.0])
+    assert np.array_equal(d.cpu().numpy(), ref)
+    assert len(ent) == 2 and all(e >= 0 for e in ent)
+
+
+def test_bad_arguments(mod):
+    from newrecon_gb300 import native
+    from newrecon_gb300.native import NrError
+
+    he = torch.zeros(64, device="cuda")
+    w = np.array([0.5])
+    out = torch.empty(64, device="cuda")
+    with pytest.raises(NrError) as e:  # misaligned output
+        native.call("nr_de_subtract", ctypes.c_void_p(he.data_ptr()),
+                    ctypes.c_void_p(he.data_ptr()), w.ctypes.data_as(ctypes.c_void_p), 1, 32,
+                    -1.0, ctypes.c_void_p(out.data_ptr() + 4), 0, 0, None, None)
+    assert e.value.code == 2
+    with pytest.raises(ValueError):
+        mod.subtract(he, he, list(np.linspace(0, 1, 17)))

@@ -65,6 +65,57 @@ def test_fp_sart(sart, name, g, angles, x, use_cos):
         assert maxrel(gn[~miss], rn[~miss]) < TOL
 
 
+@pytest.mark.parametrize("cos,layout", [(False, "ji"), (True, "ij")])
+@pytest.mark.parametrize("name,g,angles,x", CASES, ids=[c[0] for c in CASES])
+def test_fp_4r(sart, name, g, angles, x, cos, layout):
+    from newrecon_gb300 import ostr
+    from oracle.oracle import Oracle
+
+    ostr.set_geometry(g)
+    A = g.n_angles
+    M = _subsets(name, A)
+    ridx = Oracle(np.float64).reorder_index(A, M)
+    Vs = A // M
+    for idx, a0, a1 in ((np.arange(A, dtype=np.int32), 0, A), (ridx, Vs, 2 * Vs)):
+        s = -7.0
+        rsub = np.full(4 * (a1 - a0) * g.n_bins, s)
+        ref = Oracle(np.float64).fp_4r(g, x, angles, idx, a0, a1, cos, layout, sub=rsub)
+        out = torch.full(((a1 - a0) * g.n_bins,), s, device="cuda")
+        if not cos and layout == "ji":
+            sub = torch.full((4 * (a1 - a0) * g.n_bins,), s, device="cuda")
+            sart.fprojectCB1_4R_GPU_SART(dev(x), out, sub, dev(angles), dev(idx, torch.int32),
+                                         a0, a1)
+            gs = sub.cpu().numpy()
+            miss = rsub == s
+            assert np.array_equal(gs == s, miss)
+            assert relrmse(gs[~miss], rsub[~miss]) < RMSE_FP
+            assert maxrel(gs[~miss], rsub[~miss]) < TOL
+        else:
+            sart.fproject_4R(dev(x), out, dev(angles), dev(idx, torch.int32), a0, a1, cos, layout)
+        got = out.cpu().numpy()
+        assert not (got == s).any()  # every bin is written
+        print(f"{name} fp_4r cos={cos} {layout}: rel RMSE {relrmse(got, ref):.2e} "
+              f"max {maxrel(got, ref):.2e}")
+        assert relrmse(got, ref) < RMSE_FP
+        assert maxrel(got, ref) < TOL
+
+
+def test_fp_4r_matches_reference_fixture(sart):
+    from newrecon_gb300 import ostr
+
+    for name in ("tiny", "ragged"):
+        z = golden(f"sart_{name}")
+        g = geom_of(z)
+        ostr.set_geometry(g)
+        A = g.n_angles
+        idx = dev(np.arange(A, dtype=np.int32), torch.int32)
+        out = torch.zeros(A * g.n_bins, device="cuda")
+        sub = torch.zeros(4 * A * g.n_bins, device="cuda")
+        sart.fprojectCB1_4R_GPU_SART(dev(z["x"]), out, sub, dev(z["angles"]), idx, 0, A)
+        assert maxrel(sub.cpu().numpy(), z["fp4r_sub"]) < TOL
+        assert maxrel(out.cpu().numpy(), z["fp4r_merged_ji"]) < TOL
+
+
 @pytest.mark.parametrize("name", ["tiny", "ragged"])
 def test_prj_diff_bitexact(sart, name):
     from newrecon_gb300 import ostr
@@ -197,6 +248,7 @@ VARIANTS = {
     "cos": dict(use_cos=True),
     "plain": dict(use_cos=False),
     "reg": dict(use_cos=True, regularized=True, beta=-0.2, delta=0.01),
+    "4r": dict(use_cos=True, supersample=True),
 }
 
 
