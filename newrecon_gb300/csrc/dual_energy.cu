@@ -39,12 +39,15 @@ __device__ __forceinline__ double de_value(double h, double l, double w) {
     return __dadd_rn(h, -__dmul_rn(l, w));
 }
 
-// d[k][i] = float(he[i] - le[i] * w_k), four voxels per thread per step.
+// d[k][i] = float(he[i] - le[i] * w_k).  VEC (n a multiple of 4, so that every
+// output row d + k n stays 16-byte aligned): four voxels per thread per step
+// with 16-byte loads and stores; otherwise one voxel per step.
+template <bool VEC>
 __global__ void __launch_bounds__(256) de_subtract_kernel(const float* __restrict__ he,
                                                           const float* __restrict__ le,
                                                           float* __restrict__ d, int64_t n,
                                                           const __grid_constant__ DeWeights W) {
-    const int64_t n4 = n / 4;
+    const int64_t n4 = VEC ? n / 4 : 0;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4; q += stride) {
         const float4 h4 = __ldg(reinterpret_cast<const float4*>(he) + q);
@@ -63,7 +66,7 @@ __global__ void __launch_bounds__(256) de_subtract_kernel(const float* __restric
             __stcs(reinterpret_cast<float4*>(d + (int64_t)k * n) + q, o);
         }
     }
-    // the n % 4 tail
+    // everything when !VEC
     for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
         double h = he[i], l = le[i];
         if (W.masked && !(h > W.level)) h = l = 0.0;
@@ -124,6 +127,8 @@ NR_API nr_status nr_de_subtract(const float* he, const float* le, const double* 
     if (hist && (hist_begin < 0 || hist_len < 0 || hist_begin + hist_len > n))
         return NR_ERR_BAD_ARGUMENT;
     if (((uintptr_t)he | (uintptr_t)le | (uintptr_t)d) & 15) return NR_ERR_BAD_ARGUMENT;
+    // float4 path: he, le, d 16-byte aligned (checked) and n % 4 == 0, so each
+    // row d + k n is aligned too; q < n/4 keeps every access below n.
     DeWeights W;
     for (int k = 0; k < n_weights; k++) W.w[k] = weights[k];
     for (int k = n_weights; k < DE_MAX_WEIGHTS; k++) W.w[k] = 0.0;
@@ -131,8 +136,10 @@ NR_API nr_status nr_de_subtract(const float* he, const float* le, const double* 
     W.masked = mask_level >= 0.0;
     W.level = mask_level;
     cudaStream_t s = as_stream(stream);
-    if (n > 0)
-        de_subtract_kernel<<<de_blocks(n / 4 + 1), 256, 0, s>>>(he, le, d, n, W);
+    if (n > 0 && n % 4 == 0)
+        de_subtract_kernel<true><<<de_blocks(n / 4), 256, 0, s>>>(he, le, d, n, W);
+    else if (n > 0)
+        de_subtract_kernel<false><<<de_blocks(n), 256, 0, s>>>(he, le, d, n, W);
     if (hist) {
         if (cudaMemsetAsync(hist, 0, (size_t)n_weights * 256 * sizeof(int32_t), s) != cudaSuccess)
             return NR_ERR_CUDA;
