@@ -123,11 +123,65 @@ constexpr int UPD_OSTR = 0;     // OSTR step above
 constexpr int UPD_SART = 1;     // OS-SART, backprj_OSSART_gpu_manyviews (Tomo_OSTR.cu:1737-1936)
 constexpr int UPD_SART_R = 2;   // OS-SART with the hyperbola prior, backprj_OSSART_R (:1938-2143)
 
-// Shared memory of one update tile: the 3-plane ring and the subset's sources.
+// Shared memory of one update tile: the 3-plane ring, the subset's sources,
+// and the current plane's separable back-projection tables (see bp_tables).
 struct UpdSmem {
     float tile[3][UPLANE];
     ViewSrc sv[UPD_VIEWS_SMEM];
+    float4 tabx[UPD_VIEWS_SMEM][UTX];
+    float4 taby[UPD_VIEWS_SMEM][UTY];
 };
+
+// The back projection of a voxel onto one view's detector is separable: on a
+// plane z, the detector column (ilb, fracI) of a voxel depends only on its x
+// and the row (jlb, fracJ) only on its y (the ray from the source through
+// the voxel centre meets the detector plane at x0 + (x1 - x0) t(z), y0 +
+// (y1 - y0) t(z)).  Per plane and view the block therefore computes 32 column
+// entries and 8 row entries, with the arithmetic of bp.cu's sbp_term (in
+// reciprocal-multiply form), and each voxel combines one of each:
+//   tabx[t][c] = {ilb, fracI, (x0 - x1)^2, tap bits}
+//   taby[t][r] = {jlb * BINSx, fracJ, (y0 - y1)^2 + (z0 - z1)^2, tap bits}
+// Tap bits: x gives i0 | i1<<1 | i0<<2 | i1<<3, y gives j0 | j0<<1 | j1<<2 |
+// j1<<3 (0 when the plane holds the source, Tomo_OSTR.cu:1643), so bit k of
+// their AND says whether tap k = (00, 10, 01, 11) of the bilinear stencil lies
+// on the detector (the rules of :1684-1715).
+__device__ __forceinline__ void bp_tables(const nr_geom& g, const ViewSrc* __restrict__ sv,
+                                          int nv, int x0t, int y0t, float z1, float inv_bx,
+                                          float inv_by, float4 (*tabx)[UTX],
+                                          float4 (*taby)[UTY], int tid) {
+    for (int e = tid; e < nv * (UTX + UTY); e += UTX * UTY) {
+        const int t = e / (UTX + UTY), q = e - t * (UTX + UTY);
+        const ViewSrc vs = sv[t];
+        const bool valid = z1 != vs.z0;
+        const float tt = valid ? __fdividef(-g.detectorR - vs.z0, z1 - vs.z0) : 0.f;
+        if (q < UTX) {
+            const float x1 = vox_x(g, x0t + q);
+            const float ddx = vs.x0 - x1;
+            const float x2 = vs.x0 + (x1 - vs.x0) * tt;
+            const float imb = (x2 - g.x_d0) * inv_bx;
+            int ilb = (int)floorf(imb);
+            if (imb < (float)ilb + 0.5f) ilb -= 1;
+            const float fracI = imb - ((float)ilb + 0.5f);
+            const int i0 = (ilb < g.nbx) && (ilb >= 0);
+            const int i1 = (ilb < g.nbx - 1) && (ilb >= -1);
+            tabx[t][q] = make_float4(__int_as_float(ilb), fracI, ddx * ddx,
+                                     __int_as_float(i0 | (i1 << 1) | (i0 << 2) | (i1 << 3)));
+        } else {
+            const int r = q - UTX;
+            const float y1 = vox_y(g, y0t + r);
+            const float ddy = vs.y0 - y1, ddz = vs.z0 - z1;
+            const float y2 = vs.y0 + (y1 - vs.y0) * tt;
+            const float jmb = (y2 - g.y_d0) * inv_by;
+            int jlb = (int)floorf(jmb);
+            if (jmb < (float)jlb + 0.5f) jlb -= 1;
+            const float fracJ = jmb - ((float)jlb + 0.5f);
+            const int j0 = valid && (jlb < g.nby) && (jlb >= 0);
+            const int j1 = valid && (jlb < g.nby - 1) && (jlb >= -1);
+            taby[t][r] = make_float4(__int_as_float(jlb * g.nbx), fracJ, ddy * ddy + ddz * ddz,
+                                     __int_as_float(j0 | (j0 << 1) | (j1 << 2) | (j1 << 3)));
+        }
+    }
+}
 
 // One sub-iteration's update, fused: SBP of h (subset views, [view][j][i]),
 // the penalty, and the update_est step.  Each block owns a 32 x 8 tile of
@@ -135,7 +189,8 @@ struct UpdSmem {
 // (with halo) in a 3-slot shared-memory ring, so every neighbour read is a
 // shared-memory load at a fixed offset.  The global loads of plane z+2 are
 // issued before plane z is computed (register prefetch), so they overlap the
-// arithmetic.  Writes x_out; flags non-finite values.
+// arithmetic.  The back projection reads the plane's separable tables
+// (bp_tables).  Writes x_out; flags non-finite values.
 //
 // KIND = UPD_SART / UPD_SART_R turn the same tile into the OS-SART update:
 // h is the normalised projection difference of the subset, the back
@@ -155,6 +210,7 @@ __device__ __forceinline__ void update_tile(
     const nr_geom& g = G.g;
     const int tid = threadIdx.y * UTX + threadIdx.x;
     for (int t = tid; t < nv; t += UTX * UTY) sv[t] = view_source(g, angles[index[a0 + t]]);
+    __syncthreads();  // the first plane's tables read sv
     const int x0t = bx * UTX, y0t = by * UTY;
     const int zb = bz * ZC, ze = min(zb + ZC, g.nz);
     const int64_t plane = (int64_t)g.nx * g.ny;
@@ -197,60 +253,48 @@ __device__ __forceinline__ void update_tile(
     const bool edge_xy = x0t == 0 || x0t + UTX >= g.nx || y0t == 0 || y0t + UTY >= g.ny;
     const float inv_delta = 1.f / delta;
     const float inv_bx = 1.f / g.bx, inv_by = 1.f / g.by;
-    const float x1 = vox_x(g, ix), y1 = vox_y(g, iy);
     const int64_t B = (int64_t)g.nbx * g.nby;
     const int r = threadIdx.y + 1, c = threadIdx.x + 1;
     for (int z = zb; z < ze; z++) {
         pa[tid] = n0;
         if (has1) pa[e1] = n1;
+        // This plane's tables: the previous plane's readers have all passed
+        // the barrier at the end of the last iteration.
+        bp_tables(g, sv, nv, x0t, y0t, vox_z(g, z), inv_bx, inv_by, sm.tabx, sm.taby, tid);
         __syncthreads();
         if (z + 1 < ze) fetch(z + 2, n0, n1);
         if (active) {
             const int64_t v = (int64_t)z * plane + (int64_t)iy * g.nx + ix;
             const float dv = KIND == UPD_OSTR ? __ldg(d + v) : 0.f;
             const float xc = pc[r * USW + c];
-            const float z1 = vox_z(g, z);
-            // M * SBP(h): the arithmetic of bp.cu's sbp_term on the [j][i]
-            // layout, with reciprocal multiplies in place of divisions.
+            // M * SBP(h) from the plane's tables: the taps and weights of
+            // bp.cu's sbp_term on the [j][i] layout.
             float capL = 0.f, sens = 0.f;
-            for (int t = 0; t < nv; t++) {
-                const ViewSrc vs = sv[t];
-                const float ddx = vs.x0 - x1, ddy = vs.y0 - y1, ddz = vs.z0 - z1;
-                const float dw = __fdividef(vs.s2, ddx * ddx + ddy * ddy + ddz * ddz);
-                if (z1 == vs.z0) continue;
-                const float tt = __fdividef(-g.detectorR - vs.z0, z1 - vs.z0);
-                const float x2 = vs.x0 + (x1 - vs.x0) * tt;
-                const float y2 = vs.y0 + (y1 - vs.y0) * tt;
-                const float imb = (x2 - g.x_d0) * inv_bx;
-                const float jmb = (y2 - g.y_d0) * inv_by;
-                int ilb = (int)floorf(imb);
-                if (imb < (float)ilb + 0.5f) ilb -= 1;
-                int jlb = (int)floorf(jmb);
-                if (jmb < (float)jlb + 0.5f) jlb -= 1;
-                const float fracI = imb - ((float)ilb + 0.5f);
-                const float fracJ = jmb - ((float)jlb + 0.5f);
-                const float* p = h + (int64_t)t * B;
-                const bool i0 = (ilb < g.nbx) && (ilb >= 0);
-                const bool i1 = (ilb < g.nbx - 1) && (ilb >= -1);
-                const bool j0 = (jlb < g.nby) && (jlb >= 0);
-                const bool j1 = (jlb < g.nby - 1) && (jlb >= -1);
+            const float* p = h;
+            for (int t = 0; t < nv; t++, p += B) {
+                const float4 ex = sm.tabx[t][threadIdx.x];
+                const float4 ey = sm.taby[t][threadIdx.y];
+                const int m = __float_as_int(ex.w) & __float_as_int(ey.w);
+                const float fracI = ex.y, fracJ = ey.y;
+                const float dw = __fdividef(sv[t].s2, ex.z + ey.z);
+                const float* q0 = p + (__float_as_int(ey.x) + __float_as_int(ex.x));
+                const float* q1 = q0 + g.nbx;
                 float d1 = 0.f, d2 = 0.f;
                 float s1 = 0.f, s2 = 0.f;  // sensitivity taps (OS-SART only)
-                const int64_t r0 = (int64_t)jlb * g.nbx, r1 = r0 + g.nbx;
-                if (i0 && j0) {
-                    d1 = (1.f - fracI) * __ldg(p + r0 + ilb);
+                if (m & 1) {
+                    d1 = (1.f - fracI) * __ldg(q0);
                     s1 = 1.f - fracI;
                 }
-                if (i1 && j0) {
-                    d1 = d1 + fracI * __ldg(p + r0 + ilb + 1);
+                if (m & 2) {
+                    d1 = d1 + fracI * __ldg(q0 + 1);
                     s1 = s1 + fracI;
                 }
-                if (i0 && j1) {
-                    d2 = (1.f - fracI) * __ldg(p + r1 + ilb);
+                if (m & 4) {
+                    d2 = (1.f - fracI) * __ldg(q1);
                     s2 = 1.f - fracI;
                 }
-                if (i1 && j1) {
-                    d2 = d2 + fracI * __ldg(p + r1 + ilb + 1);
+                if (m & 8) {
+                    d2 = d2 + fracI * __ldg(q1 + 1);
                     s2 = s2 + fracI;
                 }
                 capL = capL + ((1.f - fracJ) * d1 + fracJ * d2) * g.vz * dw;
