@@ -29,6 +29,7 @@ struct CaseDev {
     const float *d, *y, *b, *r, *angles;
     const int32_t* index;
     int* status;
+    BpTab T;               // the case's back-projection tables
     int fp_tx, fp_ty;      // detector tiles of 32 x 4 bins
     int up_tx, up_ty;      // volume tiles of 32 x 8 columns (z chunks of UZC planes)
     int64_t N;
@@ -101,7 +102,7 @@ __global__ void __launch_bounds__(256, 5) update_batch_kernel(const void* __rest
         const int a0 = (step % (int)cd.M) * cd.Vs;
         const float* cur = (step & 1) ? cd.xtmp : cd.x;
         float* nxt = (step & 1) ? cd.x : cd.xtmp;
-        update_tile<POT>(cd.G, cd.W, cur, nxt, cd.d, cd.h, cd.angles, cd.index, a0, cd.Vs, cd.M,
+        update_tile<POT>(cd.G, cd.W, cur, nxt, cd.d, cd.h, cd.angles, cd.index, cd.T, a0, cd.Vs, cd.M,
                          cd.beta, cd.delta, cd.status, bx, by, bz, sm);
     }
 }
@@ -124,7 +125,7 @@ __global__ void finish_kernel(const void* __restrict__ table) {
 nr_status ostr_sections(const nr_geom* g, const nr_ostr_params* p, void* ws, size_t bytes,
                         float** xtmp, float** h, const float** d, const float** y,
                         const float** b, const float** r, const float** angles,
-                        const int32_t** index, int** status);
+                        const int32_t** index, int** status, BpTab* tab);
 
 static int persistent_blocks(const void* kernel, int threads, size_t smem) {
     int dev = 0, sms = 152, per = 1;
@@ -176,7 +177,7 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
             return NR_ERR_BAD_ARGUMENT;
         }
         st = ostr_sections(&k.g, &k.p, k.workspace, k.ws_bytes, &d.xtmp, &d.h, &d.d, &d.y, &d.b,
-                           &d.r, &d.angles, &d.index, &d.status);
+                           &d.r, &d.angles, &d.index, &d.status, &d.T);
         if (st != NR_OK) {
             delete[] img;
             return st;

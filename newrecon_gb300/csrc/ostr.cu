@@ -11,9 +11,10 @@
 //   d        float[N]                   curvature denominators
 //   xtmp     float[N]                   second volume buffer (ping-pong)
 //   h        float[Vs][BINSy][BINSx]    subset gradient in the detector domain
+//   bpx, bpy float4[A][nz][nx], [A][nz][ny]  back-projection tables (update.cuh)
 //   gc       float[A][BINSy][BINSx]     gamma*yry (setup only)
 //   gr       float[A][BINSy][BINSx]     scatter in original order (setup only; with scatter)
-#include "common.cuh"
+#include "update.cuh"
 
 namespace nr {
 
@@ -26,8 +27,10 @@ nr_status launch_bp(const nr_geom& g, bool ji, float* vol, const float* prj, con
                     const int32_t* index, int a0, int nv, cudaStream_t st);
 nr_status launch_update(const nr_geom& g, int pot, int zc, const float* x, float* x_out,
                         const float* d, const float* h, const float* angles, const int32_t* index,
-                        int a0, int nv, float M, float beta, float delta, int* status,
-                        cudaStream_t st);
+                        const BpTab& T, int a0, int nv, float M, float beta, float delta,
+                        int* status, cudaStream_t st);
+nr_status launch_bp_tables(const nr_geom& g, const float* angles, const int32_t* index,
+                           float4* tx, float4* ty, cudaStream_t st);
 nr_status launch_transpose(float* out, const float* in, int rows, int cols, int nviews, int M,
                            int Vs, cudaStream_t st);
 nr_status launch_objective(const nr_geom& g, int pot, float delta, const float* x,
@@ -37,7 +40,7 @@ nr_status launch_objective(const nr_geom& g, int pot, float delta, const float* 
 int64_t objective_partials(const nr_geom& g);
 
 struct Layout {
-    size_t status, red, index, angles, y, b, r, d, xtmp, h, gc, gr, total;
+    size_t status, red, index, angles, y, b, r, d, xtmp, h, bpx, bpy, gc, gr, total;
     int64_t red_n;
 };
 
@@ -65,6 +68,8 @@ static Layout layout(const nr_geom& g, const nr_ostr_params& p) {
     L.d = take(N * sizeof(float));
     L.xtmp = take(N * sizeof(float));
     L.h = take(Vs * B * sizeof(float));
+    L.bpx = take((size_t)A * g.nz * g.nx * sizeof(float4));
+    L.bpy = take((size_t)A * g.nz * g.ny * sizeof(float4));
     L.gc = take(A * B * sizeof(float));
     L.gr = p.has_scatter ? take(A * B * sizeof(float)) : (size_t)-1;
     L.total = o;
@@ -76,7 +81,9 @@ struct WS {
     double* red;
     int32_t* index;
     float *angles, *y, *b, *r, *d, *xtmp, *h, *gc, *gr;
+    float4 *bpx, *bpy;
     int64_t red_n;
+    BpTab tab() const { return BpTab{bpx, bpy}; }
 };
 
 static WS carve(void* base, const Layout& L) {
@@ -92,6 +99,8 @@ static WS carve(void* base, const Layout& L) {
     w.d = (float*)(c + L.d);
     w.xtmp = (float*)(c + L.xtmp);
     w.h = (float*)(c + L.h);
+    w.bpx = (float4*)(c + L.bpx);
+    w.bpy = (float4*)(c + L.bpy);
     w.gc = (float*)(c + L.gc);
     w.gr = L.gr == (size_t)-1 ? nullptr : (float*)(c + L.gr);
     w.red_n = L.red_n;
@@ -157,7 +166,7 @@ nr_status launch_clear_status(int* status, cudaStream_t s) {
 nr_status ostr_sections(const nr_geom* g, const nr_ostr_params* p, void* ws, size_t bytes,
                         float** xtmp, float** h, const float** d, const float** y,
                         const float** b, const float** r, const float** angles,
-                        const int32_t** index, int** status) {
+                        const int32_t** index, int** status, BpTab* tab) {
     Layout L;
     nr_status st = check_ws(g, p, ws, bytes, &L);
     if (st != NR_OK) return st;
@@ -171,6 +180,7 @@ nr_status ostr_sections(const nr_geom* g, const nr_ostr_params* p, void* ws, siz
     *angles = w.angles;
     *index = w.index;
     *status = w.status;
+    *tab = w.tab();
     return NR_OK;
 }
 
@@ -208,6 +218,7 @@ NR_API nr_status nr_ostr_setup(const nr_geom* g, const nr_ostr_params* p, const 
     clear_status_kernel<<<1, 64, 0, s>>>(w.status);
     index_kernel<<<1, 256, 0, s>>>(w.index, angles, w.angles, A, M);
     if ((st = launch_status()) != NR_OK) return st;
+    if ((st = launch_bp_tables(*g, w.angles, w.index, w.bpx, w.bpy, s)) != NR_OK) return st;
     // [view][i][j] original order -> [view][j][i] subset order.
     if ((st = launch_transpose(w.y, prj, g->nbx, g->nby, A, M, Vs, s)) != NR_OK) return st;
     if ((st = launch_transpose(w.b, blank, g->nbx, g->nby, A, M, Vs, s)) != NR_OK) return st;
@@ -247,7 +258,7 @@ NR_API nr_status nr_ostr_update(const nr_geom* g, const nr_ostr_params* p, const
         return NR_ERR_BAD_ARGUMENT;
     WS w = carve(workspace, L);
     const int M = p->subset_num, Vs = g->n_angles / M;
-    return launch_update(*g, p->potential, p->upd_planes, x, x_out, w.d, w.h, w.angles, w.index, subset * Vs, Vs,
+    return launch_update(*g, p->potential, p->upd_planes, x, x_out, w.d, w.h, w.angles, w.index, w.tab(), subset * Vs, Vs,
                          (float)M, p->beta, p->delta, w.status, as_stream(stream));
 }
 
@@ -285,7 +296,7 @@ NR_API nr_status nr_ostr_subiter(const nr_geom* g, const nr_ostr_params* p, floa
     const int a0 = subset * Vs;
     if ((st = launch_fp_h(*g, p->fp_batch, x, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, s)) != NR_OK)
         return st;
-    if ((st = launch_update(*g, p->potential, p->upd_planes, x, w.xtmp, w.d, w.h, w.angles, w.index, a0, Vs,
+    if ((st = launch_update(*g, p->potential, p->upd_planes, x, w.xtmp, w.d, w.h, w.angles, w.index, w.tab(), a0, Vs,
                             (float)M, p->beta, p->delta, w.status, s)) != NR_OK)
         return st;
     if (cudaMemcpyAsync(x, w.xtmp, N * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
@@ -307,7 +318,7 @@ static nr_status enqueue_iterations(const nr_geom* g, const nr_ostr_params* p, f
             if ((st = launch_fp_h(*g, p->fp_batch, cur, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, s)) !=
                 NR_OK)
                 return st;
-            if ((st = launch_update(*g, p->potential, p->upd_planes, cur, nxt, w.d, w.h, w.angles, w.index, a0, Vs,
+            if ((st = launch_update(*g, p->potential, p->upd_planes, cur, nxt, w.d, w.h, w.angles, w.index, w.tab(), a0, Vs,
                                     (float)M, p->beta, p->delta, w.status, s)) != NR_OK)
                 return st;
             float* t = cur;

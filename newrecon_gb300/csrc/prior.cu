@@ -139,53 +139,89 @@ nr_status launch_prior(const nr_geom& g, int pot, float* RDD, float* RD, const f
     }
 }
 
+// The separable back-projection tables of update.cuh for every view position
+// a (subset order, angles[index[a]]), plane and column / row: grid (.., nz, A).
+__global__ void __launch_bounds__(128) bp_table_kernel(const __grid_constant__ Geo G,
+                                                       const float* __restrict__ angles,
+                                                       const int32_t* __restrict__ index,
+                                                       float4* __restrict__ tx,
+                                                       float4* __restrict__ ty) {
+    __shared__ ViewSrc src;
+    const nr_geom& g = G.g;
+    const int a = blockIdx.z, z = blockIdx.y;
+    if (threadIdx.x == 0) src = view_source(g, angles[index[a]]);
+    __syncthreads();
+    const float z1 = vox_z(g, z);
+    const float tt = bp_tt(g, src, z1);
+    const float inv_bx = 1.f / g.bx, inv_by = 1.f / g.by;
+    const int64_t row = (int64_t)a * g.nz + z;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < g.nx + g.ny;
+         q += gridDim.x * blockDim.x) {
+        if (q < g.nx)
+            tx[row * g.nx + q] = bp_entry_x(g, src, tt, q, inv_bx);
+        else
+            ty[row * g.ny + (q - g.nx)] = bp_entry_y(g, src, z1, tt, q - g.nx, inv_by);
+    }
+}
+
+size_t bp_table_bytes(const nr_geom& g) {
+    return (size_t)g.n_angles * g.nz * (g.nx + g.ny) * sizeof(float4);
+}
+
+nr_status launch_bp_tables(const nr_geom& g, const float* angles, const int32_t* index,
+                           float4* tx, float4* ty, cudaStream_t st) {
+    dim3 grd(cdiv((int64_t)g.nx + g.ny, 128), g.nz, g.n_angles);
+    bp_table_kernel<<<grd, 128, 0, st>>>(make_geo(g), angles, index, tx, ty);
+    return launch_status();
+}
+
 template <int POT, int ZC>
 static nr_status launch_update_t(const nr_geom& g, const float* x, float* x_out, const float* d,
                                  const float* h, const float* angles, const int32_t* index,
-                                 int a0, int nv, float M, float beta, float delta, int* status,
-                                 cudaStream_t st) {
+                                 const BpTab& T, int a0, int nv, float M, float beta,
+                                 float delta, int* status, cudaStream_t st) {
     dim3 blk(UTX, UTY), grd(cdiv(g.nx, UTX), cdiv(g.ny, UTY), cdiv(g.nz, ZC));
     update_kernel<POT, ZC><<<grd, blk, 0, st>>>(make_geo(g), make_w5(g.vz / g.vx, delta), x,
-                                                x_out, d, h, angles, index, a0, nv, M, beta, delta,
-                                                status);
+                                                x_out, d, h, angles, index, T, a0, nv, M, beta,
+                                                delta, status);
     return launch_status();
 }
 
 template <int POT>
 static nr_status launch_update_z(const nr_geom& g, int zc, const float* x, float* x_out,
                                  const float* d, const float* h, const float* angles,
-                                 const int32_t* index, int a0, int nv, float M, float beta,
-                                 float delta, int* status, cudaStream_t st) {
+                                 const int32_t* index, const BpTab& T, int a0, int nv, float M,
+                                 float beta, float delta, int* status, cudaStream_t st) {
     switch (zc) {
     case 8:
-        return launch_update_t<POT, 8>(g, x, x_out, d, h, angles, index, a0, nv, M, beta, delta,
+        return launch_update_t<POT, 8>(g, x, x_out, d, h, angles, index, T, a0, nv, M, beta, delta,
                                        status, st);
     case 32:
-        return launch_update_t<POT, 32>(g, x, x_out, d, h, angles, index, a0, nv, M, beta, delta,
+        return launch_update_t<POT, 32>(g, x, x_out, d, h, angles, index, T, a0, nv, M, beta, delta,
                                         status, st);
     default:
-        return launch_update_t<POT, 16>(g, x, x_out, d, h, angles, index, a0, nv, M, beta, delta,
+        return launch_update_t<POT, 16>(g, x, x_out, d, h, angles, index, T, a0, nv, M, beta, delta,
                                         status, st);
     }
 }
 
 nr_status launch_update(const nr_geom& g, int pot, int zc, const float* x, float* x_out,
                         const float* d, const float* h, const float* angles, const int32_t* index,
-                        int a0, int nv, float M, float beta, float delta, int* status,
-                        cudaStream_t st) {
+                        const BpTab& T, int a0, int nv, float M, float beta, float delta,
+                        int* status, cudaStream_t st) {
     if (nv > UPD_VIEWS_SMEM) return NR_ERR_BAD_ARGUMENT;
     switch (pot) {
     case NR_POT_Q2:
-        return launch_update_z<NR_POT_Q2>(g, zc, x, x_out, d, h, angles, index, a0, nv, M, beta,
+        return launch_update_z<NR_POT_Q2>(g, zc, x, x_out, d, h, angles, index, T, a0, nv, M, beta,
                                           delta, status, st);
     case NR_POT_LANGE:
-        return launch_update_z<NR_POT_LANGE>(g, zc, x, x_out, d, h, angles, index, a0, nv, M, beta,
+        return launch_update_z<NR_POT_LANGE>(g, zc, x, x_out, d, h, angles, index, T, a0, nv, M, beta,
                                              delta, status, st);
     case NR_POT_HYPERBOLA:
-        return launch_update_z<NR_POT_HYPERBOLA>(g, zc, x, x_out, d, h, angles, index, a0, nv, M,
+        return launch_update_z<NR_POT_HYPERBOLA>(g, zc, x, x_out, d, h, angles, index, T, a0, nv, M,
                                                  beta, delta, status, st);
     case NR_POT_HUBER:
-        return launch_update_z<NR_POT_HUBER>(g, zc, x, x_out, d, h, angles, index, a0, nv, M, beta,
+        return launch_update_z<NR_POT_HUBER>(g, zc, x, x_out, d, h, angles, index, T, a0, nv, M, beta,
                                              delta, status, st);
     default: return NR_ERR_BAD_ARGUMENT;
     }

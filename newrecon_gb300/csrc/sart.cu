@@ -31,6 +31,7 @@
 //   norm   float[A][BINSy][BINSx]     chord lengths, same layout
 //   diff   float[Vs][BINSy][BINSx]    the subset's normalised difference
 //   xtmp   float[N]                   second volume buffer (ping-pong)
+//   bpx, bpy float4[A][nz][nx], [A][nz][ny]  back-projection tables (update.cuh)
 #include "project.cuh"
 #include "update.cuh"
 
@@ -41,11 +42,13 @@ nr_status launch_subset_index(int32_t* idx, const float* angles_in, float* angle
 nr_status launch_clear_status(int* status, cudaStream_t s);
 nr_status launch_transpose(float* out, const float* in, int rows, int cols, int nviews, int M,
                            int Vs, cudaStream_t st);
+nr_status launch_bp_tables(const nr_geom& g, const float* angles, const int32_t* index,
+                           float4* tx, float4* ty, cudaStream_t st);
 
 namespace {
 
 struct SartLayout {
-    size_t status, index, angles, p, norm, diff, xtmp, total;
+    size_t status, index, angles, p, norm, diff, xtmp, bpx, bpy, total;
 };
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -68,6 +71,8 @@ SartLayout sart_layout(const nr_geom& g, const nr_sart_params& p) {
     L.norm = take(A * B * sizeof(float));
     L.diff = take(Vs * B * sizeof(float));
     L.xtmp = take(N * sizeof(float));
+    L.bpx = take((size_t)A * g.nz * g.nx * sizeof(float4));
+    L.bpy = take((size_t)A * g.nz * g.ny * sizeof(float4));
     L.total = o;
     return L;
 }
@@ -76,6 +81,7 @@ struct SartWS {
     int* status;
     int32_t* index;
     float *angles, *p, *norm, *diff, *xtmp;
+    float4 *bpx, *bpy;
 };
 
 SartWS sart_carve(void* base, const SartLayout& L) {
@@ -88,6 +94,8 @@ SartWS sart_carve(void* base, const SartLayout& L) {
     w.norm = (float*)(c + L.norm);
     w.diff = (float*)(c + L.diff);
     w.xtmp = (float*)(c + L.xtmp);
+    w.bpx = (float4*)(c + L.bpx);
+    w.bpy = (float4*)(c + L.bpy);
     return w;
 }
 
@@ -236,12 +244,13 @@ template <int KIND, int ZC>
 __global__ void __launch_bounds__(256) sart_update_kernel(
     const __grid_constant__ Geo G, const __grid_constant__ PriorW5 W,
     const float* __restrict__ x, float* __restrict__ x_out, const float* __restrict__ diff,
-    const float* __restrict__ angles, const int32_t* __restrict__ index, int a0, int nv,
-    float lambda, float beta, float delta, int* __restrict__ status) {
+    const float* __restrict__ angles, const int32_t* __restrict__ index,
+    const __grid_constant__ BpTab T, int a0, int nv, float lambda, float beta, float delta,
+    int* __restrict__ status) {
     __shared__ UpdSmem sm;
-    update_tile<NR_POT_HYPERBOLA, ZC, KIND>(G, W, x, x_out, nullptr, diff, angles, index, a0, nv,
-                                            lambda, beta, delta, status, blockIdx.x, blockIdx.y,
-                                            blockIdx.z, sm);
+    update_tile<NR_POT_HYPERBOLA, ZC, KIND>(G, W, x, x_out, nullptr, diff, angles, index, T, a0,
+                                            nv, lambda, beta, delta, status, blockIdx.x,
+                                            blockIdx.y, blockIdx.z, sm);
 }
 
 namespace {
@@ -276,7 +285,8 @@ nr_status launch_sart_update_t(const nr_geom& g, const nr_sart_params& p, const 
     // unit neighbour distances: G_Huber_prior has no z ratio (Tomo_OSTR.cu:303)
     const float delta = p.regularized ? p.delta : 1.f;
     sart_update_kernel<KIND, ZC><<<grd, blk, 0, s>>>(make_geo(g), make_w5(1.f, delta), x, x_out,
-                                                     w.diff, w.angles, w.index, a0, nv, p.lambda,
+                                                     w.diff, w.angles, w.index,
+                                                     BpTab{w.bpx, w.bpy}, a0, nv, p.lambda,
                                                      p.beta, delta, w.status);
     return launch_status();
 }
@@ -358,6 +368,7 @@ NR_API nr_status nr_sart_setup(const nr_geom* g, const nr_sart_params* p, const 
     const int A = g->n_angles, M = p->subset_num, Vs = A / M;
     if ((st = launch_clear_status(w.status, s)) != NR_OK) return st;
     if ((st = launch_subset_index(w.index, angles, w.angles, A, M, s)) != NR_OK) return st;
+    if ((st = launch_bp_tables(*g, w.angles, w.index, w.bpx, w.bpy, s)) != NR_OK) return st;
     // [view][i][j] original order -> [view][j][i] subset order.
     if ((st = launch_transpose(w.p, line, g->nbx, g->nby, A, M, Vs, s)) != NR_OK) return st;
     if (p->supersample) {

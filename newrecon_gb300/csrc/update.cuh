@@ -123,64 +123,65 @@ constexpr int UPD_OSTR = 0;     // OSTR step above
 constexpr int UPD_SART = 1;     // OS-SART, backprj_OSSART_gpu_manyviews (Tomo_OSTR.cu:1737-1936)
 constexpr int UPD_SART_R = 2;   // OS-SART with the hyperbola prior, backprj_OSSART_R (:1938-2143)
 
-// Shared memory of one update tile: the 3-plane ring, the subset's sources,
-// and the current plane's separable back-projection tables (see bp_tables).
+// Shared memory of one update tile: the 3-plane ring and the subset's sources.
 struct UpdSmem {
     float tile[3][UPLANE];
     ViewSrc sv[UPD_VIEWS_SMEM];
-    float4 tabx[UPD_VIEWS_SMEM][UTX];
-    float4 taby[UPD_VIEWS_SMEM][UTY];
 };
 
 // The back projection of a voxel onto one view's detector is separable: on a
 // plane z, the detector column (ilb, fracI) of a voxel depends only on its x
 // and the row (jlb, fracJ) only on its y (the ray from the source through
 // the voxel centre meets the detector plane at x0 + (x1 - x0) t(z), y0 +
-// (y1 - y0) t(z)).  Per plane and view the block therefore computes 32 column
-// entries and 8 row entries, with the arithmetic of bp.cu's sbp_term (in
-// reciprocal-multiply form), and each voxel combines one of each:
-//   tabx[t][c] = {ilb, fracI, (x0 - x1)^2, tap bits}
-//   taby[t][r] = {jlb * BINSx, fracJ, (y0 - y1)^2 + (z0 - z1)^2, tap bits}
+// (y1 - y0) t(z)).  Neither depends on the volume, so they are tabulated once
+// per reconstruction, per view (subset order), plane and column / row, with
+// the arithmetic of bp.cu's sbp_term in reciprocal-multiply form:
+//   x[(a nz + z) nx + i] = {ilb, fracI, (x0 - x1)^2, tap bits}
+//   y[(a nz + z) ny + j] = {jlb * BINSx, fracJ, (y0 - y1)^2 + (z0 - z1)^2, tap bits}
 // Tap bits: x gives i0 | i1<<1 | i0<<2 | i1<<3, y gives j0 | j0<<1 | j1<<2 |
 // j1<<3 (0 when the plane holds the source, Tomo_OSTR.cu:1643), so bit k of
 // their AND says whether tap k = (00, 10, 01, 11) of the bilinear stencil lies
-// on the detector (the rules of :1684-1715).
-__device__ __forceinline__ void bp_tables(const nr_geom& g, const ViewSrc* __restrict__ sv,
-                                          int nv, int x0t, int y0t, float z1, float inv_bx,
-                                          float inv_by, float4 (*tabx)[UTX],
-                                          float4 (*taby)[UTY], int tid) {
-    for (int e = tid; e < nv * (UTX + UTY); e += UTX * UTY) {
-        const int t = e / (UTX + UTY), q = e - t * (UTX + UTY);
-        const ViewSrc vs = sv[t];
-        const bool valid = z1 != vs.z0;
-        const float tt = valid ? __fdividef(-g.detectorR - vs.z0, z1 - vs.z0) : 0.f;
-        if (q < UTX) {
-            const float x1 = vox_x(g, x0t + q);
-            const float ddx = vs.x0 - x1;
-            const float x2 = vs.x0 + (x1 - vs.x0) * tt;
-            const float imb = (x2 - g.x_d0) * inv_bx;
-            int ilb = (int)floorf(imb);
-            if (imb < (float)ilb + 0.5f) ilb -= 1;
-            const float fracI = imb - ((float)ilb + 0.5f);
-            const int i0 = (ilb < g.nbx) && (ilb >= 0);
-            const int i1 = (ilb < g.nbx - 1) && (ilb >= -1);
-            tabx[t][q] = make_float4(__int_as_float(ilb), fracI, ddx * ddx,
-                                     __int_as_float(i0 | (i1 << 1) | (i0 << 2) | (i1 << 3)));
-        } else {
-            const int r = q - UTX;
-            const float y1 = vox_y(g, y0t + r);
-            const float ddy = vs.y0 - y1, ddz = vs.z0 - z1;
-            const float y2 = vs.y0 + (y1 - vs.y0) * tt;
-            const float jmb = (y2 - g.y_d0) * inv_by;
-            int jlb = (int)floorf(jmb);
-            if (jmb < (float)jlb + 0.5f) jlb -= 1;
-            const float fracJ = jmb - ((float)jlb + 0.5f);
-            const int j0 = valid && (jlb < g.nby) && (jlb >= 0);
-            const int j1 = valid && (jlb < g.nby - 1) && (jlb >= -1);
-            taby[t][r] = make_float4(__int_as_float(jlb * g.nbx), fracJ, ddy * ddy + ddz * ddz,
-                                     __int_as_float(j0 | (j0 << 1) | (j1 << 2) | (j1 << 3)));
-        }
-    }
+// on the detector (the rules of :1684-1715).  Each update reads one entry of
+// each per voxel and view (the x entries of a warp are consecutive, its y
+// entry is one broadcast); the tables of a subset stay in L2.
+struct BpTab {
+    const float4* __restrict__ x;
+    const float4* __restrict__ y;
+};
+
+__device__ __forceinline__ float bp_tt(const nr_geom& g, const ViewSrc& vs, float z1) {
+    return z1 != vs.z0 ? __fdividef(-g.detectorR - vs.z0, z1 - vs.z0) : 0.f;
+}
+
+__device__ __forceinline__ float4 bp_entry_x(const nr_geom& g, const ViewSrc& vs, float tt,
+                                             int i, float inv_bx) {
+    const float x1 = vox_x(g, i);
+    const float ddx = vs.x0 - x1;
+    const float x2 = vs.x0 + (x1 - vs.x0) * tt;
+    const float imb = (x2 - g.x_d0) * inv_bx;
+    int ilb = (int)floorf(imb);
+    if (imb < (float)ilb + 0.5f) ilb -= 1;
+    const float fracI = imb - ((float)ilb + 0.5f);
+    const int i0 = (ilb < g.nbx) && (ilb >= 0);
+    const int i1 = (ilb < g.nbx - 1) && (ilb >= -1);
+    return make_float4(__int_as_float(ilb), fracI, ddx * ddx,
+                       __int_as_float(i0 | (i1 << 1) | (i0 << 2) | (i1 << 3)));
+}
+
+__device__ __forceinline__ float4 bp_entry_y(const nr_geom& g, const ViewSrc& vs, float z1,
+                                             float tt, int j, float inv_by) {
+    const bool valid = z1 != vs.z0;
+    const float y1 = vox_y(g, j);
+    const float ddy = vs.y0 - y1, ddz = vs.z0 - z1;
+    const float y2 = vs.y0 + (y1 - vs.y0) * tt;
+    const float jmb = (y2 - g.y_d0) * inv_by;
+    int jlb = (int)floorf(jmb);
+    if (jmb < (float)jlb + 0.5f) jlb -= 1;
+    const float fracJ = jmb - ((float)jlb + 0.5f);
+    const int j0 = valid && (jlb < g.nby) && (jlb >= 0);
+    const int j1 = valid && (jlb < g.nby - 1) && (jlb >= -1);
+    return make_float4(__int_as_float(jlb * g.nbx), fracJ, ddy * ddy + ddz * ddz,
+                       __int_as_float(j0 | (j0 << 1) | (j1 << 2) | (j1 << 3)));
 }
 
 // One sub-iteration's update, fused: SBP of h (subset views, [view][j][i]),
@@ -189,8 +190,8 @@ __device__ __forceinline__ void bp_tables(const nr_geom& g, const ViewSrc* __res
 // (with halo) in a 3-slot shared-memory ring, so every neighbour read is a
 // shared-memory load at a fixed offset.  The global loads of plane z+2 are
 // issued before plane z is computed (register prefetch), so they overlap the
-// arithmetic.  The back projection reads the plane's separable tables
-// (bp_tables).  Writes x_out; flags non-finite values.
+// arithmetic.  The back projection reads the separable tables (BpTab).
+// Writes x_out; flags non-finite values.
 //
 // KIND = UPD_SART / UPD_SART_R turn the same tile into the OS-SART update:
 // h is the normalised projection difference of the subset, the back
@@ -203,14 +204,13 @@ template <int POT, int ZC = UZC, int KIND = UPD_OSTR>
 __device__ __forceinline__ void update_tile(
     const Geo& G, const PriorW5& W, const float* __restrict__ x, float* __restrict__ x_out,
     const float* __restrict__ d, const float* __restrict__ h, const float* __restrict__ angles,
-    const int32_t* __restrict__ index, int a0, int nv, float M, float beta, float delta,
-    int* __restrict__ status, int bx, int by, int bz, UpdSmem& sm) {
+    const int32_t* __restrict__ index, const BpTab& T, int a0, int nv, float M, float beta,
+    float delta, int* __restrict__ status, int bx, int by, int bz, UpdSmem& sm) {
     float (*tile)[UPLANE] = sm.tile;
     ViewSrc* sv = sm.sv;
     const nr_geom& g = G.g;
     const int tid = threadIdx.y * UTX + threadIdx.x;
     for (int t = tid; t < nv; t += UTX * UTY) sv[t] = view_source(g, angles[index[a0 + t]]);
-    __syncthreads();  // the first plane's tables read sv
     const int x0t = bx * UTX, y0t = by * UTY;
     const int zb = bz * ZC, ze = min(zb + ZC, g.nz);
     const int64_t plane = (int64_t)g.nx * g.ny;
@@ -252,15 +252,11 @@ __device__ __forceinline__ void update_tile(
     const bool active = ix < g.nx && iy < g.ny;
     const bool edge_xy = x0t == 0 || x0t + UTX >= g.nx || y0t == 0 || y0t + UTY >= g.ny;
     const float inv_delta = 1.f / delta;
-    const float inv_bx = 1.f / g.bx, inv_by = 1.f / g.by;
     const int64_t B = (int64_t)g.nbx * g.nby;
     const int r = threadIdx.y + 1, c = threadIdx.x + 1;
     for (int z = zb; z < ze; z++) {
         pa[tid] = n0;
         if (has1) pa[e1] = n1;
-        // This plane's tables: the previous plane's readers have all passed
-        // the barrier at the end of the last iteration.
-        bp_tables(g, sv, nv, x0t, y0t, vox_z(g, z), inv_bx, inv_by, sm.tabx, sm.taby, tid);
         __syncthreads();
         if (z + 1 < ze) fetch(z + 2, n0, n1);
         if (active) {
@@ -271,9 +267,12 @@ __device__ __forceinline__ void update_tile(
             // bp.cu's sbp_term on the [j][i] layout.
             float capL = 0.f, sens = 0.f;
             const float* p = h;
-            for (int t = 0; t < nv; t++, p += B) {
-                const float4 ex = sm.tabx[t][threadIdx.x];
-                const float4 ey = sm.taby[t][threadIdx.y];
+            const float4* tx = T.x + ((int64_t)a0 * g.nz + z) * g.nx + ix;
+            const float4* ty = T.y + ((int64_t)a0 * g.nz + z) * g.ny + iy;
+            const int64_t sx = (int64_t)g.nz * g.nx, sy = (int64_t)g.nz * g.ny;
+            for (int t = 0; t < nv; t++, p += B, tx += sx, ty += sy) {
+                const float4 ex = __ldg(tx);
+                const float4 ey = __ldg(ty);
                 const int m = __float_as_int(ex.w) & __float_as_int(ey.w);
                 const float fracI = ex.y, fracJ = ey.y;
                 const float dw = __fdividef(sv[t].s2, ex.z + ey.z);
@@ -340,10 +339,10 @@ __global__ void __launch_bounds__(256) update_kernel(
     const __grid_constant__ Geo G, const __grid_constant__ PriorW5 W,
     const float* __restrict__ x, float* __restrict__ x_out, const float* __restrict__ d,
     const float* __restrict__ h, const float* __restrict__ angles,
-    const int32_t* __restrict__ index, int a0, int nv, float M, float beta, float delta,
-    int* __restrict__ status) {
+    const int32_t* __restrict__ index, const __grid_constant__ BpTab T, int a0, int nv,
+    float M, float beta, float delta, int* __restrict__ status) {
     __shared__ UpdSmem sm;
-    update_tile<POT, ZC>(G, W, x, x_out, d, h, angles, index, a0, nv, M, beta, delta, status,
+    update_tile<POT, ZC>(G, W, x, x_out, d, h, angles, index, T, a0, nv, M, beta, delta, status,
                          blockIdx.x, blockIdx.y, blockIdx.z, sm);
 }
 
