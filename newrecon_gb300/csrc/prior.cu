@@ -181,9 +181,14 @@ static nr_status launch_update_t(const nr_geom& g, const float* x, float* x_out,
                                  const BpTab& T, int a0, int nv, float M, float beta,
                                  float delta, int* status, cudaStream_t st) {
     dim3 blk(UTX, UTY), grd(cdiv(g.nx, UTX), cdiv(g.ny, UTY), cdiv(g.nz, ZC));
-    update_kernel<POT, ZC><<<grd, blk, 0, st>>>(make_geo(g), make_w5(g.vz / g.vx, delta), x,
-                                                x_out, d, h, angles, index, T, a0, nv, M, beta,
-                                                delta, status);
+    const Geo G = make_geo(g);
+    const PriorW5 W = make_w5(g.vz / g.vx, delta);
+    if (nv == 1)
+        update_kernel<POT, ZC, 1><<<grd, blk, 0, st>>>(G, W, x, x_out, d, h, angles, index, T, a0,
+                                                       nv, M, beta, delta, status);
+    else
+        update_kernel<POT, ZC, 0><<<grd, blk, 0, st>>>(G, W, x, x_out, d, h, angles, index, T, a0,
+                                                       nv, M, beta, delta, status);
     return launch_status();
 }
 

@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(256) sart_fp_diff_4r_kernel(
                                                     : 0.f;
 }
 
-template <int KIND, int ZC>
+template <int KIND, int ZC, int NV>
 __global__ void __launch_bounds__(256) sart_update_kernel(
     const __grid_constant__ Geo G, const __grid_constant__ PriorW5 W,
     const float* __restrict__ x, float* __restrict__ x_out, const float* __restrict__ diff,
@@ -248,9 +248,9 @@ __global__ void __launch_bounds__(256) sart_update_kernel(
     const __grid_constant__ BpTab T, int a0, int nv, float lambda, float beta, float delta,
     int* __restrict__ status) {
     __shared__ UpdSmem sm;
-    update_tile<NR_POT_HYPERBOLA, ZC, KIND>(G, W, x, x_out, nullptr, diff, angles, index, T, a0,
-                                            nv, lambda, beta, delta, status, blockIdx.x,
-                                            blockIdx.y, blockIdx.z, sm);
+    update_tile<NR_POT_HYPERBOLA, ZC, KIND, NV>(G, W, x, x_out, nullptr, diff, angles, index, T,
+                                                a0, nv, lambda, beta, delta, status, blockIdx.x,
+                                                blockIdx.y, blockIdx.z, sm);
 }
 
 namespace {
@@ -284,10 +284,17 @@ nr_status launch_sart_update_t(const nr_geom& g, const nr_sart_params& p, const 
     dim3 blk(UTX, UTY), grd(cdiv(g.nx, UTX), cdiv(g.ny, UTY), cdiv(g.nz, ZC));
     // unit neighbour distances: G_Huber_prior has no z ratio (Tomo_OSTR.cu:303)
     const float delta = p.regularized ? p.delta : 1.f;
-    sart_update_kernel<KIND, ZC><<<grd, blk, 0, s>>>(make_geo(g), make_w5(1.f, delta), x, x_out,
-                                                     w.diff, w.angles, w.index,
-                                                     BpTab{w.bpx, w.bpy}, a0, nv, p.lambda,
-                                                     p.beta, delta, w.status);
+    const Geo G = make_geo(g);
+    const PriorW5 W = make_w5(1.f, delta);
+    const BpTab T{w.bpx, w.bpy};
+    if (nv == 1)
+        sart_update_kernel<KIND, ZC, 1><<<grd, blk, 0, s>>>(G, W, x, x_out, w.diff, w.angles,
+                                                            w.index, T, a0, nv, p.lambda, p.beta,
+                                                            delta, w.status);
+    else
+        sart_update_kernel<KIND, ZC, 0><<<grd, blk, 0, s>>>(G, W, x, x_out, w.diff, w.angles,
+                                                            w.index, T, a0, nv, p.lambda, p.beta,
+                                                            delta, w.status);
     return launch_status();
 }
 
