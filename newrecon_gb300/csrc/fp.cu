@@ -109,9 +109,12 @@ __global__ void __launch_bounds__(256) fp_4r_kernel(const __grid_constant__ Geo 
 }
 
 // Fused forward projection + h, one block per 32 x 4 bins of one subset view;
-// K Siddon steps per gather round.
+// K Siddon steps per gather round.  The walk waits on its volume gathers, so
+// residency pays: 12 blocks per SM (40 registers, no spills) run it 5 % faster
+// on the clinical workload than the 10 that 48 registers allow (K = 8 needs
+// more registers and keeps 8).
 template <int K>
-__global__ void __launch_bounds__(128) fp_h_kernel(const __grid_constant__ Geo G,
+__global__ void __launch_bounds__(128, (K >= 8 ? 8 : 12)) fp_h_kernel(const __grid_constant__ Geo G,
                                                    const float* __restrict__ vol,
                                                    float* __restrict__ h,
                                                    const float* __restrict__ angles,

@@ -147,9 +147,10 @@ __global__ void __launch_bounds__(128) sart_norm_kernel(const __grid_constant__ 
     norm[(int64_t)a * g.nbx * g.nby + bin_off<true>(g, i, j)] = v;
 }
 
-// diff = (p - FP(x) [cos]) / norm for the subset views [a0, a0 + gridDim.z).
+// diff = (p - FP(x) [cos]) / norm for the subset views [a0, a0 + gridDim.z);
+// 12 resident blocks per SM, as fp_h_kernel.
 template <int K, bool COS>
-__global__ void __launch_bounds__(128) sart_fp_diff_kernel(
+__global__ void __launch_bounds__(128, (K >= 8 ? 8 : 12)) sart_fp_diff_kernel(
     const __grid_constant__ Geo G, const float* __restrict__ vol, float* __restrict__ diff,
     const float* __restrict__ angles, const int32_t* __restrict__ index, int a0,
     const float* __restrict__ p, const float* __restrict__ norm) {
