@@ -276,7 +276,9 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (x, x', d: 3 x 126 MB; y, b: 2 x 138 MB)"},
         "gpu_launches": 2 * M * args.steps,
         "tuned": None if tuned is None else {"fp_batch": tuned["fp_batch"],
-                                             "upd_planes": tuned["upd_planes"]},
+                                             "fp_stage": tuned.get("fp_stage", 0),
+                                             "upd_planes": tuned["upd_planes"],
+                                             "fp_ms": tuned.get("fp_ms")},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / peak,
                      "traffic": traffic, "kernels": kern},

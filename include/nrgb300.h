@@ -147,7 +147,19 @@ typedef struct nr_ostr_params {
     float delta;               /* potential scale (1/mm), > 0 unless Q2          */
     int32_t fp_batch;          /* Siddon steps per gather round: 2, 4, 8 (0 = 4) */
     int32_t upd_planes;        /* z planes per update block: 8, 16, 32 (0 = 16) */
+    int32_t fp_stage;          /* NR_STAGE_OFF (default): the projection gathers
+                                  the volume through L1/L2; NR_STAGE_TMA: it stages
+                                  the volume slab by slab in shared memory by TMA
+                                  where the volume allows it (IMGSIZx a multiple of
+                                  4, x 16-byte aligned; fp_batch 2 or 4).  Same
+                                  result either way; on the clinical workload the
+                                  staged form is slower (0.255 vs 0.162 ms).     */
 } nr_ostr_params;
+
+enum {
+    NR_STAGE_OFF = 0,
+    NR_STAGE_TMA = 1
+};
 
 /* fp_batch and upd_planes select kernel variants only (every variant gives the
  * same result); the autotuner (newrecon_gb300/autotune.py) picks them per

@@ -5,7 +5,9 @@ computes the same result, bit for bit):
 
 * ``fp_batch`` -- Siddon steps walked per gather round in the forward
   projection (2, 4, 8): more steps keep more volume gathers in flight but use
-  more registers (fewer resident warps);
+  more registers (fewer resident warps); 2 and 4 are also tried with the
+  volume staged slab by slab in shared memory by TMA (``fp_stage``), where
+  the geometry allows it;
 * ``upd_planes`` -- z planes walked per block by the fused update (8, 16, 32):
   deeper slabs amortise the halo planes, shallower ones give more blocks.
 
@@ -24,6 +26,9 @@ from typing import Dict, Optional, Tuple
 import torch
 
 FP_BATCHES = (2, 4, 8)
+# (fp_batch, fp_stage) variants of the projection: direct gathers for every
+# batch, TMA-staged slabs for 2 and 4
+FP_VARIANTS = ((2, 0), (4, 0), (8, 0), (2, 1), (4, 1))
 UPD_PLANES = (8, 16, 32)
 
 
@@ -37,7 +42,7 @@ def signature(plan) -> str:
     p = plan.params
     dev = torch.cuda.get_device_name(plan.ws.device)
     return (f"{dev}|{g.nx}x{g.ny}x{g.nz}|{g.nbx}x{g.nby}|A{g.n_angles}|M{p.subset_num}"
-            f"|pot{p.potential}|scat{p.has_scatter}")
+            f"|pot{p.potential}|scat{p.has_scatter}|v2")
 
 
 def _load() -> Dict[str, dict]:
@@ -85,29 +90,32 @@ def tune(plan, x: Optional[torch.Tensor] = None, reps: int = 3,
         if hit and hit.get("fp_batch") in FP_BATCHES and hit.get("upd_planes") in UPD_PLANES:
             plan.params.fp_batch = int(hit["fp_batch"])
             plan.params.upd_planes = int(hit["upd_planes"])
+            plan.params.fp_stage = int(hit.get("fp_stage", 0))
             return plan.params.fp_batch, plan.params.upd_planes, hit
     if x is None:
         x = torch.zeros(plan.geom.n_voxels, dtype=torch.float32, device=plan.ws.device)
     xo = torch.empty_like(x)
     M = plan.params.subset_num
-    saved = (plan.params.fp_batch, plan.params.upd_planes)
+    saved = (plan.params.fp_batch, plan.params.upd_planes, plan.params.fp_stage)
     fp_ms, up_ms = {}, {}
-    for k in FP_BATCHES:
+    for k, st in FP_VARIANTS:
         plan.params.fp_batch = k
+        plan.params.fp_stage = st
         plan.project(x, 0)  # warm-up
-        fp_ms[k] = _time(lambda: [plan.project(x, a) for a in range(M)], reps)
-    plan.params.fp_batch = saved[0]
+        fp_ms[(k, st)] = _time(lambda: [plan.project(x, a) for a in range(M)], reps)
+    plan.params.fp_batch, plan.params.fp_stage = saved[0], saved[2]
     plan.project(x, 0)  # h of subset 0 for the update timings
     for z in UPD_PLANES:
         plan.params.upd_planes = z
         plan.update(x, xo, 0)
         up_ms[z] = _time(lambda: [plan.update(x, xo, 0) for _ in range(M)], reps)
-    best_k = min(fp_ms, key=fp_ms.get)
+    best_k, best_st = min(fp_ms, key=fp_ms.get)
     best_z = min(up_ms, key=up_ms.get)
     plan.params.fp_batch = best_k
+    plan.params.fp_stage = best_st
     plan.params.upd_planes = best_z
-    rec = {"fp_batch": best_k, "upd_planes": best_z,
-           "fp_ms": {str(k): v for k, v in fp_ms.items()},
+    rec = {"fp_batch": best_k, "fp_stage": best_st, "upd_planes": best_z,
+           "fp_ms": {f"{k}{'-tma' if st else ''}": v for (k, st), v in fp_ms.items()},
            "update_ms": {str(k): v for k, v in up_ms.items()}}
     if use_cache:
         _store(key, rec)

@@ -6,7 +6,10 @@
 // the same few 128-byte lines of one volume row (the volume is x-fastest):
 // the gathers coalesce.  Views of a launch run on gridDim.z.  The walk itself
 // is in siddon.cuh.
+#include <cudaTypedefs.h>
+
 #include "project.cuh"
+#include "slab.cuh"
 
 namespace nr {
 
@@ -124,6 +127,27 @@ __global__ void __launch_bounds__(128, (K >= 8 ? 8 : 12)) fp_h_kernel(const __gr
                                                    const float* __restrict__ r) {
     __shared__ ViewSrc src;
     fp_h_tile<K>(G, vol, h, angles, index, a0, y, b, r, blockIdx.x, blockIdx.y, blockIdx.z, src);
+}
+
+// The same with the volume staged slab by slab through shared memory by TMA
+// (slab.cuh); bit-identical to fp_h_kernel.  Measured on the clinical
+// workload it is slower than the direct gathers (0.255 ms with 4-plane slabs,
+// 0.346 ms with 2-plane slabs, against 0.162 ms): the walk's gathers already
+// hit L1 three times in four and the walk is instruction bound, so the
+// per-slab synchronisation and bookkeeping cost more than the latency they
+// hide.  It is kept as an option (NR_STAGE_TMA).
+template <int K, int SZ>
+__global__ void __launch_bounds__(128, (SZ >= 4 ? 6 : 10)) fp_h_slab_kernel(
+    const __grid_constant__ Geo G, const __grid_constant__ CUtensorMap map,
+    const float* __restrict__ vol, float* __restrict__ h, const float* __restrict__ angles,
+    const int32_t* __restrict__ index, int a0, const float* __restrict__ y,
+    const float* __restrict__ b, const float* __restrict__ r, int* __restrict__ status) {
+    extern __shared__ __align__(128) float sbuf[];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ ViewSrc src;
+    __shared__ SlabBox box[2];
+    fp_h_slab_tile<K, SZ>(G, &map, vol, h, angles, index, a0, y, b, r, status, sbuf, src, box,
+                          bar);
 }
 
 // gamma * yry for every view in one pass (the d precompute's detector term,
@@ -244,11 +268,72 @@ NR_API nr_status nr_fp_4r(const nr_geom* g, const float* x, float* prj, float* s
 // Internal launchers used by the device-resident path (ostr.cu).
 namespace nr {
 
-nr_status launch_fp_h(const nr_geom& g, int k, const float* x, float* h, const float* angles,
-                      const int32_t* index, int a0, int nviews, const float* y, const float* b,
-                      const float* r, cudaStream_t st) {
+// cuTensorMapEncodeTiled from the driver, looked up once.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+        }
+        return (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }();
+    return fn;
+}
+
+#ifndef NR_SLAB_Z
+#define NR_SLAB_Z 4
+#endif
+constexpr int SLAB_Z = NR_SLAB_Z;  // planes per staged slab
+
+// The TMA descriptor of volume x ([z][y][x] float) with the staging box; false
+// when the volume cannot be described (x rows not a multiple of 16 bytes,
+// misaligned base, no driver entry point).
+bool slab_map(const nr_geom& g, const float* x, CUtensorMap* map) {
+    if (g.nx % 4 != 0 || ((uintptr_t)x & 15) != 0) return false;
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.nx * 4, (cuuint64_t)g.nx * g.ny * 4};
+    const cuuint32_t box[3] = {SLAB_FX, SLAB_FY, SLAB_Z};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)x, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// premap: x's descriptor when the caller encoded it already (slab_map), else
+// nullptr (encoded here when staging applies).
+nr_status launch_fp_h(const nr_geom& g, int k, int stage, const float* x, float* h,
+                      const float* angles, const int32_t* index, int a0, int nviews,
+                      const float* y, const float* b, const float* r, int* status,
+                      const CUtensorMap* premap, cudaStream_t st) {
     dim3 blk(32, 4), grd(cdiv(g.nbx, 32), cdiv(g.nby, 4), nviews);
     const Geo G = make_geo(g);
+    CUtensorMap map;
+    bool staged = false;
+    if (stage == NR_STAGE_TMA && k != 8) {
+        if (premap) {
+            map = *premap;
+            staged = true;
+        } else {
+            staged = slab_map(g, x, &map);
+        }
+    }
+    if (staged) {
+        const size_t smem = 2 * SlabCfg<SLAB_Z>::BYTES;
+        if (k == 2)
+            fp_h_slab_kernel<2, SLAB_Z><<<grd, blk, smem, st>>>(G, map, x, h, angles, index, a0,
+                                                                y, b, r, status);
+        else
+            fp_h_slab_kernel<4, SLAB_Z><<<grd, blk, smem, st>>>(G, map, x, h, angles, index, a0,
+                                                                y, b, r, status);
+        return launch_status();
+    }
     if (k == 2)
         fp_h_kernel<2><<<grd, blk, 0, st>>>(G, x, h, angles, index, a0, y, b, r);
     else if (k == 8)

@@ -14,13 +14,17 @@
 //   bpx, bpy float4[A][nz][nx], [A][nz][ny]  back-projection tables (update.cuh)
 //   gc       float[A][BINSy][BINSx]     gamma*yry (setup only)
 //   gr       float[A][BINSy][BINSx]     scatter in original order (setup only; with scatter)
+#include <cuda.h>
+
 #include "update.cuh"
 
 namespace nr {
 
-nr_status launch_fp_h(const nr_geom& g, int k, const float* x, float* h, const float* angles,
-                      const int32_t* index, int a0, int nviews, const float* y, const float* b,
-                      const float* r, cudaStream_t st);
+nr_status launch_fp_h(const nr_geom& g, int k, int stage, const float* x, float* h,
+                      const float* angles, const int32_t* index, int a0, int nviews,
+                      const float* y, const float* b, const float* r, int* status,
+                      const CUtensorMap* premap, cudaStream_t st);
+bool slab_map(const nr_geom& g, const float* x, CUtensorMap* map);
 nr_status launch_gamma_yry(const nr_geom& g, int gamma_mode, float* out, const float* angles,
                            const float* y, const float* r, cudaStream_t st);
 nr_status launch_bp(const nr_geom& g, bool ji, float* vol, const float* prj, const float* angles,
@@ -122,6 +126,7 @@ static nr_status check_params(const nr_geom* g, const nr_ostr_params* p) {
         return NR_ERR_BAD_ARGUMENT;
     if (p->upd_planes != 0 && p->upd_planes != 8 && p->upd_planes != 16 && p->upd_planes != 32)
         return NR_ERR_BAD_ARGUMENT;
+    if (p->fp_stage != NR_STAGE_OFF && p->fp_stage != NR_STAGE_TMA) return NR_ERR_BAD_ARGUMENT;
     if (g->ny > 65535 || g->nz > 65535 || g->n_angles > 65535) return NR_ERR_BAD_GEOMETRY;
     return NR_OK;
 }
@@ -244,7 +249,7 @@ NR_API nr_status nr_ostr_project(const nr_geom* g, const nr_ostr_params* p, cons
     if (!x || subset < 0 || subset >= p->subset_num) return NR_ERR_BAD_ARGUMENT;
     WS w = carve(workspace, L);
     const int Vs = g->n_angles / p->subset_num;
-    return launch_fp_h(*g, p->fp_batch, x, w.h, w.angles, w.index, subset * Vs, Vs, w.y, w.b, w.r,
+    return launch_fp_h(*g, p->fp_batch, p->fp_stage, x, w.h, w.angles, w.index, subset * Vs, Vs, w.y, w.b, w.r, w.status, nullptr,
                        as_stream(stream));
 }
 
@@ -294,7 +299,7 @@ NR_API nr_status nr_ostr_subiter(const nr_geom* g, const nr_ostr_params* p, floa
     const int A = g->n_angles, M = p->subset_num, Vs = A / M;
     const int64_t N = (int64_t)g->nx * g->ny * g->nz;
     const int a0 = subset * Vs;
-    if ((st = launch_fp_h(*g, p->fp_batch, x, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, s)) != NR_OK)
+    if ((st = launch_fp_h(*g, p->fp_batch, p->fp_stage, x, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, w.status, nullptr, s)) != NR_OK)
         return st;
     if ((st = launch_update(*g, p->potential, p->upd_planes, x, w.xtmp, w.d, w.h, w.angles, w.index, w.tab(), a0, Vs,
                             (float)M, p->beta, p->delta, w.status, s)) != NR_OK)
@@ -312,10 +317,15 @@ static nr_status enqueue_iterations(const nr_geom* g, const nr_ostr_params* p, f
     nr_status st;
     float* cur = x;
     float* nxt = w.xtmp;
+    // the staged projection's descriptors of the two volume buffers, once
+    CUtensorMap maps[2];
+    const bool staged = p->fp_stage == NR_STAGE_TMA && p->fp_batch != 8 &&
+                        slab_map(*g, x, &maps[0]) && slab_map(*g, w.xtmp, &maps[1]);
     for (int it = 0; it < n_iters; it++) {
         for (int a = 0; a < M; a++) {
             const int a0 = a * Vs;
-            if ((st = launch_fp_h(*g, p->fp_batch, cur, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, s)) !=
+            if ((st = launch_fp_h(*g, p->fp_batch, p->fp_stage, cur, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, w.status,
+                                  staged ? &maps[cur == x ? 0 : 1] : nullptr, s)) !=
                 NR_OK)
                 return st;
             if ((st = launch_update(*g, p->potential, p->upd_planes, cur, nxt, w.d, w.h, w.angles, w.index, w.tab(), a0, Vs,

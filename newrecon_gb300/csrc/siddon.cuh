@@ -58,24 +58,23 @@ __device__ __forceinline__ Axis axis_setup(float e, float d, float L, int n, flo
     return a;
 }
 
-// Traces the ray (x0,y0,z0) -> (x1,y1,z1).  MODE 0: sum_j len_j * vol_j;
-// MODE 1: in-volume chord length; MODE 2: full length |src - bin|; MODE 3:
-// out[0] = the MODE 0 sum and out[1] = the chord, from one walk (the sum and
-// sum_norm of rayTrace3D_GPU_direct_notexturememory, Tomo_OSTR.cu:327-610).
-// Returns false when the ray misses the volume (the reference's status -1).
-//
-// MODE 0 walks in batches of K steps: the voxel indices and chord lengths of
-// K segments are computed first (they do not depend on the volume), then the
-// K gathers are issued together and accumulated in segment order, so a warp
-// keeps K loads in flight instead of one.  The sum is bit-identical for every K.
-template <int MODE, int K = 4>
-__device__ __forceinline__ bool trace(const Geo& G, const float* __restrict__ vol, float x0,
-                                      float y0, float z0, float x1, float y1, float z1,
-                                      float* out) {
+// The walk's set-up for the ray (x0,y0,z0) -> (x1,y1,z1): its length L, the
+// per-axis state from the volume entry point and the exit distance smax.
+// Returns false when the ray misses the volume (the reference's status -1);
+// LENGTH_ONLY stops after the slab test with only L set.
+struct RayAxes {
+    Axis ax, ay, az;
+    float smax, L;
+};
+
+template <bool LENGTH_ONLY>
+__device__ __forceinline__ bool ray_axes(const Geo& G, float x0, float y0, float z0, float x1,
+                                         float y1, float z1, RayAxes& R) {
     const nr_geom& g = G.g;
     const float dx = x1 - x0, dy = y1 - y0, dz = z1 - z0;
     const float L = sqrtf(dx * dx + dy * dy + dz * dz);
     if (!(L > 0.f && L < NR_FINF)) return false;
+    R.L = L;
     float amin = -NR_FINF, amax = NR_FINF;
     // Parametric slab intersection, Tomo_OSTR.cu:641-726.
     if (dx != 0.f) {
@@ -100,19 +99,43 @@ __device__ __forceinline__ bool trace(const Geo& G, const float* __restrict__ vo
         return false;
     }
     if (!(amin < amax)) return false;
-    if (MODE == 2) {
-        *out = L;  // Tomo_OSTR.cu:1172
-        return true;
-    }
+    if (LENGTH_ONLY) return true;
     // Entry point in voxel units.
     const float ex = __fdiv_rn(__fmaf_rn(amin, dx, x0 - g.x_p0), g.vx);
     const float ey = __fdiv_rn(__fmaf_rn(amin, dy, y0 - g.y_p0), g.vy);
     const float ez = __fdiv_rn(__fmaf_rn(amin, dz, z0 - g.z_p0), g.vz);
-    const Axis ax = axis_setup(ex, dx, L, g.nx, g.vx);
-    const Axis ay = axis_setup(ey, dy, L, g.ny, g.vy);
-    const Axis az = axis_setup(ez, dz, L, g.nz, g.vz);
-    const float smax = fminf(fminf(ax.last, ay.last), az.last);
-    if (!(smax < NR_FINF)) return false;  // only when no axis is crossed at all
+    R.ax = axis_setup(ex, dx, L, g.nx, g.vx);
+    R.ay = axis_setup(ey, dy, L, g.ny, g.vy);
+    R.az = axis_setup(ez, dz, L, g.nz, g.vz);
+    R.smax = fminf(fminf(R.ax.last, R.ay.last), R.az.last);
+    return R.smax < NR_FINF;  // false only when no axis is crossed at all
+}
+
+// Traces the ray (x0,y0,z0) -> (x1,y1,z1).  MODE 0: sum_j len_j * vol_j;
+// MODE 1: in-volume chord length; MODE 2: full length |src - bin|; MODE 3:
+// out[0] = the MODE 0 sum and out[1] = the chord, from one walk (the sum and
+// sum_norm of rayTrace3D_GPU_direct_notexturememory, Tomo_OSTR.cu:327-610).
+// Returns false when the ray misses the volume (the reference's status -1).
+//
+// MODE 0 walks in batches of K steps: the voxel indices and chord lengths of
+// K segments are computed first (they do not depend on the volume), then the
+// K gathers are issued together and accumulated in segment order, so a warp
+// keeps K loads in flight instead of one.  The sum is bit-identical for every K.
+template <int MODE, int K = 4>
+__device__ __forceinline__ bool trace(const Geo& G, const float* __restrict__ vol, float x0,
+                                      float y0, float z0, float x1, float y1, float z1,
+                                      float* out) {
+    const nr_geom& g = G.g;
+    RayAxes R;
+    if (!ray_axes<MODE == 2>(G, x0, y0, z0, x1, y1, z1, R)) return false;
+    if (MODE == 2) {
+        *out = R.L;  // Tomo_OSTR.cu:1172
+        return true;
+    }
+    const Axis& ax = R.ax;
+    const Axis& ay = R.ay;
+    const Axis& az = R.az;
+    const float smax = R.smax;
     if (MODE == 1) {
         *out = smax;
         return true;

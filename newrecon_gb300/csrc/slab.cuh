@@ -1,0 +1,274 @@
+// slab.cuh -- the fused forward projection + OSTR gradient with the volume
+// staged slab by slab through shared memory by TMA (device code of
+// fp_h_slab_kernel in fp.cu).
+//
+// A block projects 32 x 4 bins of one view.  The volume is walked in slabs of
+// SZ planes, in the direction the rays travel through z.  For each slab, one
+// thread bounds the footprint of the block's rays in the slab: the position
+// of a ray at height z is affine in its bin's position and in z, so the 4
+// corner rays at the slab's two boundary planes bound every ray of the block.
+// Widened by 2 voxels on each side (the walk's float crossings can land one
+// voxel from the exact position), the box [x0, x0+FX) x [y0, y0+FY) x slab is
+// loaded by one TMA copy (cp.async.bulk.tensor.3d) into one of two shared
+// buffers while the block walks the other; voxels outside the volume read 0
+// and are never walked.  A slab whose footprint does not fit the box is read
+// from global memory instead (uniform per block).
+//
+// Each thread's Siddon walk is the one of siddon.cuh, resumed slab by slab:
+// the state (distance, crossing counters, next crossings) carries over, a
+// slab's steps stop where the ray leaves the slab's planes, and the segments
+// are accumulated in the same order with the same arithmetic -- the result is
+// bit-identical to fp_h_kernel's.  Shared-memory indices are kept
+// incrementally with the box's strides and clamped into the buffer, so no
+// access can leave it.  Every mbarrier wait is bounded; a wait that gives up
+// sets NR_FLAG_TIMEOUT and waits once more before the block moves on.
+#pragma once
+
+#include <cuda.h>
+
+#include "project.cuh"
+#include "tc.cuh"
+
+namespace nr {
+
+constexpr int SLAB_FX = 64;   // box width in x (a multiple of 4: 16-byte rows)
+constexpr int SLAB_FY = 16;
+constexpr int SLAB_WAIT = 1 << 22;
+
+template <int SZ>
+struct SlabCfg {
+    static constexpr int ELEMS = SLAB_FX * SLAB_FY * SZ;
+    static constexpr uint32_t BYTES = ELEMS * 4u;
+};
+
+// One slab's box: origin in voxels, the slab's planes, and whether the
+// block's footprint fits the box (else the slab is read from global memory).
+struct SlabBox {
+    int x0, y0, zlo, zhi, fits;
+};
+
+__device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, int x, int y,
+                                            int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(tc::smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(tc::smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
+}
+
+// Slab q's planes, walking down (dir < 0: from the top) or up.
+template <int SZ>
+__device__ __forceinline__ void slab_planes(int q, int nz, bool down, int* zlo, int* zhi) {
+    if (down) {
+        *zhi = nz - q * SZ;
+        *zlo = max(0, *zhi - SZ);
+    } else {
+        *zlo = q * SZ;
+        *zhi = min(nz, *zlo + SZ);
+    }
+}
+
+// Thread 0: the box of slab q for the block's corner bins (i0..i1, j0..j1),
+// then the TMA load of it into buffer `buf` (or a bare arrival when the
+// footprint does not fit).
+template <int SZ>
+__device__ __forceinline__ void slab_issue(const nr_geom& g, const ViewSrc& src,
+                                           const CUtensorMap* map, int q, bool down, int i0,
+                                           int i1, int j0, int j1, float* sbuf, SlabBox* box,
+                                           uint64_t* bar, int buf) {
+    int zlo, zhi;
+    slab_planes<SZ>(q, g.nz, down, &zlo, &zhi);
+    const float dzs = -g.detectorR - src.z0;
+    float xmin = NR_FINF, xmax = -NR_FINF, ymin = NR_FINF, ymax = -NR_FINF;
+    for (int e = 0; e < 2; e++) {
+        const float zp = g.z_p0 + (float)(e ? zhi : zlo) * g.vz;
+        const float t = (zp - src.z0) / dzs;
+        for (int c = 0; c < 4; c++) {
+            const float xb = bin_x(g, (c & 1) ? i1 : i0), yb = bin_y(g, (c & 2) ? j1 : j0);
+            const float px = src.x0 + (xb - src.x0) * t, py = src.y0 + (yb - src.y0) * t;
+            xmin = fminf(xmin, px);
+            xmax = fmaxf(xmax, px);
+            ymin = fminf(ymin, py);
+            ymax = fmaxf(ymax, py);
+        }
+    }
+    const int ix0 = (int)floorf((xmin - g.x_p0) / g.vx) - 2;
+    const int ix1 = (int)floorf((xmax - g.x_p0) / g.vx) + 2;
+    const int iy0 = (int)floorf((ymin - g.y_p0) / g.vy) - 2;
+    const int iy1 = (int)floorf((ymax - g.y_p0) / g.vy) + 2;
+    SlabBox bx;
+    bx.x0 = ix0 & ~3;  // TMA x coordinates are multiples of 4 floats
+    bx.y0 = iy0;
+    bx.zlo = zlo;
+    bx.zhi = zhi;
+    bx.fits = (ix1 - bx.x0 < SLAB_FX) && (iy1 - iy0 < SLAB_FY) && (xmin == xmin) &&
+              (xmax == xmax) && (ymin == ymin) && (ymax == ymax) && ix0 > -(1 << 28) &&
+              ix1 < (1 << 28) && iy0 > -(1 << 28) && iy1 < (1 << 28);
+    box[buf] = bx;
+    if (bx.fits) {
+        mbar_arrive_tx(&bar[buf], SlabCfg<SZ>::BYTES);
+        tma_load_3d(sbuf + buf * SlabCfg<SZ>::ELEMS, map, bx.x0, bx.y0, zlo, &bar[buf]);
+    } else {
+        mbar_arrive(&bar[buf]);
+    }
+}
+
+// Walks the ray through the current slab: steps while s < send, send being
+// the smaller of the exit distance and the distance of the z crossing that
+// leaves the slab (computed with the walk's own formula, so the walk stops
+// exactly after that crossing), reading vals[idx] with the given strides
+// (clamped to [0, lim] when CLAMP).  Same batching and order as trace<0, K>.
+template <int K, bool CLAMP>
+__device__ __forceinline__ void walk_slab(const float* __restrict__ vals, int& idx, int sx,
+                                          int sy, int sz, int lim, const Axis& ax,
+                                          const Axis& ay, const Axis& az, float send, float& s,
+                                          float& tx, float& ty, float& tz, float& cx,
+                                          float& cy, float& cz, float& sum) {
+    while (s < send) {
+        float seg[K];
+        int id[K];
+        bool on[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            on[k] = s < send;
+            const float m = fminf(fminf(tx, ty), tz);
+            seg[k] = m - s;
+            id[k] = idx;
+            if (on[k]) {
+                s = m;
+                if (tx == m) {
+                    cx += 1.f;
+                    tx = __fmaf_rn(cx, ax.step, ax.first);
+                    idx += sx;
+                }
+                if (ty == m) {
+                    cy += 1.f;
+                    ty = __fmaf_rn(cy, ay.step, ay.first);
+                    idx += sy;
+                }
+                if (tz == m) {
+                    cz += 1.f;
+                    tz = __fmaf_rn(cz, az.step, az.first);
+                    idx += sz;
+                }
+            }
+        }
+        float v[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const int j = CLAMP ? (int)min((unsigned)id[k], (unsigned)lim) : id[k];
+            v[k] = on[k] ? vals[j] : 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++)
+            if (on[k]) sum = __fmaf_rn(seg[k], v[k], sum);
+    }
+}
+
+// The slab-staged body of one block (32 x 4 bins of subset view bz).  Every
+// thread of the block runs it (it synchronises once per slab).
+template <int K, int SZ>
+__device__ __forceinline__ void fp_h_slab_tile(const Geo& G, const CUtensorMap* map,
+                                               const float* __restrict__ vol,
+                                               float* __restrict__ h,
+                                               const float* __restrict__ angles,
+                                               const int32_t* __restrict__ index, int a0,
+                                               const float* __restrict__ y,
+                                               const float* __restrict__ b,
+                                               const float* __restrict__ r,
+                                               int* __restrict__ status, float* sbuf,
+                                               ViewSrc& src, SlabBox* box, uint64_t* bar) {
+    const nr_geom& g = G.g;
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    const int a = a0 + blockIdx.z;
+    const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 4;
+    const int i1 = min(i0 + 31, g.nbx - 1), j1 = min(j0 + 3, g.nby - 1);
+    if (tid == 0) {
+        src = view_source(g, angles[index[a]]);
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    // rays run from the source to the detector plane z = -detectorR
+    const bool down = -g.detectorR < src.z0;
+    const int nslab = (g.nz + SZ - 1) / SZ;
+    if (tid == 0) {
+        slab_issue<SZ>(g, src, map, 0, down, i0, i1, j0, j1, sbuf, box, bar, 0);
+        if (nslab > 1) slab_issue<SZ>(g, src, map, 1, down, i0, i1, j0, j1, sbuf, box, bar, 1);
+    }
+    // this thread's ray
+    const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+    const bool active = i < g.nbx && j < g.nby;
+    RayAxes R;
+    bool hit = false;
+    if (active)
+        hit = ray_axes<false>(G, src.x0, src.y0, src.z0, bin_x(g, i), bin_y(g, j),
+                              -g.detectorR, R);
+    float s = 0.f, sum = 0.f, tx = 0.f, ty = 0.f, tz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    if (hit) {
+        tx = R.ax.first;
+        ty = R.ay.first;
+        tz = R.az.first;
+    }
+    for (int q = 0; q < nslab; q++) {
+        const int buf = q & 1;
+        if (!tc::mbar_wait(&bar[buf], (q >> 1) & 1, SLAB_WAIT)) {
+            if (tid == 0) atomicOr(status, NR_FLAG_TIMEOUT);
+            tc::mbar_wait(&bar[buf], (q >> 1) & 1, SLAB_WAIT);
+        }
+        const SlabBox bx = box[buf];
+        if (hit && s < R.smax) {
+            // the voxel the walk is in
+            const int ix = R.ax.idx + R.ax.dir * (int)cx;
+            const int iy = R.ay.idx + R.ay.dir * (int)cy;
+            const int iz = R.az.idx + R.az.dir * (int)cz;
+            if (iz >= bx.zlo && iz < bx.zhi) {
+                // the walk stays in the slab up to its z crossing number k,
+                // the one out of plane zlo (down) or zhi - 1 (up), at the
+                // distance the walk itself computes: fma(k, step, first)
+                float send = R.smax;
+                if (R.az.dir != 0) {
+                    const int k = R.az.dir < 0 ? R.az.idx - bx.zlo : bx.zhi - 1 - R.az.idx;
+                    send = fminf(send, __fmaf_rn((float)k, R.az.step, R.az.first));
+                }
+                if (bx.fits) {
+                    int idx = ((iz - bx.zlo) * SLAB_FY + (iy - bx.y0)) * SLAB_FX + (ix - bx.x0);
+                    walk_slab<K, true>(sbuf + buf * SlabCfg<SZ>::ELEMS, idx, R.ax.dir,
+                                       R.ay.dir * SLAB_FX, R.az.dir * SLAB_FX * SLAB_FY,
+                                       SlabCfg<SZ>::ELEMS - 1, R.ax, R.ay, R.az, send, s, tx,
+                                       ty, tz, cx, cy, cz, sum);
+                } else {
+                    int idx = (iz * g.ny + iy) * g.nx + ix;
+                    walk_slab<K, false>(vol, idx, R.ax.dir, R.ay.dir * g.nx,
+                                        R.az.dir * g.nx * g.ny, 0, R.ax, R.ay, R.az, send, s,
+                                        tx, ty, tz, cx, cy, cz, sum);
+                }
+            }
+        }
+        __syncthreads();  // buffer `buf` is free again
+        if (tid == 0 && q + 2 < nslab) {
+            tc::fence_async_smem();
+            slab_issue<SZ>(g, src, map, q + 2, down, i0, i1, j0, j1, sbuf, box, bar, buf);
+        }
+    }
+    if (!active) return;
+    const float l = hit ? sum * src.ct : 0.f;
+    const int64_t B = (int64_t)g.nbx * g.nby;
+    const int64_t o = (int64_t)a * B + bin_off<true>(g, i, j);
+    const float yb = b[o] * expf(-l);
+    const float den = yb + (r ? r[o] : 0.f);
+    h[(int64_t)blockIdx.z * B + bin_off<true>(g, i, j)] = (__fdiv_rn(y[o], den) - 1.f) * yb;
+}
+
+}  // namespace nr

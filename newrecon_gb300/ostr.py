@@ -356,12 +356,17 @@ class OSTR:
     """
 
     def __init__(self, geom: Geometry, *, subset_num: int, beta: float, delta: float,
-                 potential: str = "lange", gamma_mode: str = "length", has_scatter: bool = False):
+                 potential: str = "lange", gamma_mode: str = "length", has_scatter: bool = False,
+                 stage: bool = False):
+        """stage=True stages the projection's volume slab by slab in shared
+        memory by TMA instead of gathering it through L1/L2 (same result;
+        slower on the clinical workload)."""
         geom.validate(subset_num)
         self.geom = geom
         self.params = NrOstrParams(int(subset_num), int(POTENTIALS[potential]),
                                    int(GAMMA_MODES[gamma_mode]), int(bool(has_scatter)),
                                    float(beta), float(delta if potential != "q2" else 1.0))
+        self.params.fp_stage = 1 if stage else 0
         self.gc = geom.to_c()
         size = ctypes.c_size_t(0)
         native.call("nr_ostr_workspace_size", ctypes.byref(self.gc), ctypes.byref(self.params),

@@ -135,9 +135,9 @@ def test_autotune_variants_agree_and_cache(mod, tmp_path, monkeypatch):
     x = torch.zeros(cfg.geom.n_voxels, device="cuda")
     plan.iterate(x, 1)
     outs = []
-    for k in autotune.FP_BATCHES:
+    for k, st in autotune.FP_VARIANTS:
         for zc in autotune.UPD_PLANES:
-            plan.params.fp_batch, plan.params.upd_planes = k, zc
+            plan.params.fp_batch, plan.params.fp_stage, plan.params.upd_planes = k, st, zc
             xo = torch.empty_like(x)
             plan.project(x, 3)
             plan.update(x, xo, 3)
@@ -153,3 +153,4 @@ def test_autotune_variants_agree_and_cache(mod, tmp_path, monkeypatch):
     plan.params.fp_batch = plan.params.upd_planes = 0
     rec2 = plan.autotune(x)  # served from the cache
     assert (plan.params.fp_batch, plan.params.upd_planes) == (rec["fp_batch"], rec["upd_planes"])
+    assert plan.params.fp_stage == rec["fp_stage"]
