@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--batch", type=int, default=0,
                     help="also time N batched reconstructions (persistent launches)")
     ap.add_argument("--batch-steps", type=int, default=25)
+    ap.add_argument("--batch-config", default="mixed", choices=["mixed", "fullres"],
+                    help="mixed: uneven clinical-pitch cases; fullres: 2048x1024x70 breasts "
+                         "at 0.085 mm, 3328x1664 detector, 15 views")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--algo", default="ostr", choices=["ostr", "ossart", "dual-energy"],
                     help="ostr (the headline), ossart (the SART family on the same workload) "
@@ -60,6 +63,14 @@ def parse():
     ap.add_argument("--no-warm", action="store_true",
                     help="skip the learned warm-start comparison")
     return ap.parse_args()
+
+
+def workload_name(cfg):
+    g = cfg.geom
+    return (f"{cfg.name}: {g.nx}x{g.ny}x{g.nz} vox @{g.vx:g}x{g.vy:g}x{g.vz:g}mm, "
+            f"{g.nbx}x{g.nby} det @{g.bx:g}mm, {g.n_angles} views "
+            f"+-{float(np.degrees(np.abs(cfg.angles).max())):.3g}deg, {cfg.subset_num} subsets, "
+            f"{cfg.potential} d={cfg.delta:g} b={cfg.beta:g}, I0={cfg.I0:g}")
 
 
 def make_scan_gpu(cfg, seed):
@@ -260,7 +271,7 @@ def run_ours(args):
     ach = kern[dom]["gbs"]
     traffic = None
     prof_traffic = os.path.join(HERE, "profiles", "dram_traffic.txt")
-    if os.path.isfile(prof_traffic):
+    if os.path.isfile(prof_traffic) and args.config == "clinical":
         for ln in open(prof_traffic):
             parts = ln.split()
             if len(parts) >= 2 and not ln.startswith("#") and parts[0] == dom:
@@ -270,10 +281,11 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded breast phantom, Poisson counts)",
-        "config": {"workload": "clinical: 1024x512x60 vox @0.14x0.14x1mm, 1664x832 det @0.14mm, "
-                               "25 views +-25deg, 25 subsets, Huber d=0.003 b=100, I0=5e3",
-                   "step": "1 OSTR iteration = 25 sub-iterations", "parallelism": f"replicas x{ws}",
-                   "l2": "inputs larger than L2 (x, x', d: 3 x 126 MB; y, b: 2 x 138 MB)"},
+        "config": {"workload": workload_name(cfg),
+                   "step": f"1 OSTR iteration = {M} sub-iterations",
+                   "parallelism": f"replicas x{ws}",
+                   "l2": f"inputs larger than L2 (x, x', d: 3 x {4 * g.n_voxels / 1e6:.0f} MB; "
+                         f"y, b: 2 x {4 * g.n_angles * g.n_bins / 1e6:.0f} MB)"},
         "gpu_launches": 2 * M * args.steps,
         "tuned": None if tuned is None else {"fp_batch": tuned["fp_batch"],
                                              "fp_stage": tuned.get("fp_stage", 0),
@@ -296,6 +308,8 @@ def run_ours(args):
                                "kind": "port",
                                "sample": f"{len(times)} sub-iterations of the clinical workload "
                                          f"(FP32 restatement, OpenMP), {model}"}
+        out["cpu_baseline"]["sample"] = out["cpu_baseline"]["sample"].replace(
+            "clinical workload", f"{cfg.name} workload")
     if not args.no_warm:
         out["warm_start"] = warm_bench(cfg, plan, rank)
     if args.batch:
@@ -312,14 +326,22 @@ def batch_bench(args, rank):
     import torch
 
     from newrecon_gb300 import ostr, replicas
-    from newrecon_gb300.geometry import batch_configs
+    from newrecon_gb300.geometry import batch_configs, config
     from newrecon_gb300.phantom import breast_phantom, poisson_counts
 
-    cfgs = batch_configs(args.batch, seed=replicas.case_seed(7, rank))
+    fullres = args.batch_config == "fullres"
+    if fullres:
+        cfgs = [config("fullres", seed=replicas.case_seed(11, rank) * 100 + k)
+                for k in range(args.batch)]
+    else:
+        cfgs = batch_configs(args.batch, seed=replicas.case_seed(7, rank))
     cases = []
     for c in cfgs:
         g = c.geom
-        x = breast_phantom(g, c.seed, 0, c.n_calc, glandular_fraction=c.n_glandular / 100.0)
+        if fullres:
+            x = breast_phantom(g, c.seed, c.n_glandular, c.n_calc, thickness_mm=c.thickness_mm)
+        else:
+            x = breast_phantom(g, c.seed, 0, c.n_calc, glandular_fraction=c.n_glandular / 100.0)
         ostr.set_geometry(g)
         idx = np.arange(g.n_angles, dtype=np.int32)
         line = torch.zeros(g.n_angles * g.n_bins, device="cuda")
@@ -368,9 +390,13 @@ def batch_bench(args, rank):
             "projections_per_s": subits / t_batch,
             "volumes_per_hour": len(cases) * 3600.0 / (t_batch / steps * full_steps),
             "sequential_subset_iters_per_s": subits / t_seq,
-            "workload": "batch: thickness U(30,80), in-plane U(512,1024)xU(256,512) @0.14mm, "
-                        "9/15/25 views over +-U(7.5,25) deg, I0 U(3e3,2e4), gland U(10,50)%, "
-                        "hyperbola, 50 iterations"}
+            "workload": ("full resolution: 2048x1024x70 @0.085x0.085x1mm, 3328x1664 det "
+                         "@0.085mm, 15 views +-7.5deg, I0 4e3, hyperbola d=0.002 b=200, "
+                         "50 iterations" if fullres else
+                         "batch: thickness U(30,80), in-plane U(512,1024)xU(256,512) @0.14mm, "
+                         "9/15/25 views over +-U(7.5,25) deg, I0 U(3e3,2e4), gland U(10,50)%, "
+                         "hyperbola, 50 iterations"),
+            "gpu_memory_gb": torch.cuda.max_memory_allocated() / 1e9}
 
 
 def warm_bench(cfg, plan, rank, tol=1e-4, early=2):
