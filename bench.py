@@ -356,7 +356,7 @@ def batch_bench(args, rank):
     steps = min(args.batch_steps, bt.n_steps)
     stream = torch.cuda.current_stream()
     from newrecon_gb300 import native
-    tab = ctypes_ptr(bt.table)
+    tab = bt._table_ptr()  # host table: each launch carries it as its kernel parameter
     for k in range(min(3, steps)):  # warm-up (advances the cases; timing only)
         native.call("nr_batch_step", tab, k, stream_ptr())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

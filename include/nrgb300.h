@@ -243,20 +243,22 @@ typedef struct nr_batch_case {
     size_t ws_bytes;
 } nr_batch_case;
 
-/* Bytes of the device table describing n_cases cases. */
+/* Bytes of the case table describing n_cases cases (host memory: every batch
+ * launch takes the table as its kernel parameter). */
 nr_status nr_batch_table_size(int32_t n_cases, size_t* bytes);
-/* Writes the case table (256-byte aligned device memory of nr_batch_table_size
+/* Writes the case table (8-byte aligned HOST memory of nr_batch_table_size
  * bytes) and returns the number of batch steps (the largest n_iters * M).
- * Synchronises stream (the table image is copied from host memory). */
+ * Issues no GPU work (stream is not used). */
 nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, void* table,
                            size_t table_bytes, int32_t* n_steps, void* stream);
-/* One batch step (step = 0, 1, ... in order). */
+/* One batch step (step = 0, 1, ... in order).  The table is read when the
+ * call is made: it may be changed or freed once the call returns. */
 nr_status nr_batch_step(const void* table, int32_t step, void* stream);
 /* After the last step: moves results that ended in the ping-pong buffer into x. */
 nr_status nr_batch_finish(const void* table, void* stream);
 /* Captures steps 0 .. n_steps-1 and the finish into a CUDA graph (replay with
  * nr_ostr_graph_launch, release with nr_ostr_graph_destroy); stream must be a
- * non-default stream. */
+ * non-default stream.  The graph keeps the table as it was at capture. */
 nr_status nr_batch_graph_create(const void* table, int32_t n_steps, void* stream, void** graph);
 
 /* ---------------------------------------------------------------------------

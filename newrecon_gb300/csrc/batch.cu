@@ -1,22 +1,42 @@
-// batch.cu -- many independent reconstructions in one persistent launch.
+// batch.cu -- many independent reconstructions advanced by shared launches.
 //
-// A batch step advances every unfinished case by one sub-iteration with two
-// persistent launches (grid = SMs x resident blocks): the fused forward
-// projection + gradient of all cases, then the fused update of all cases.
-// Each launch walks one flat list of work items -- (case, detector tile, view)
-// or (case, volume tile, z chunk) -- built from per-case prefix offsets, so
-// cases of different sizes, view counts and potentials share the GPU in the
-// same launch and small cases fill the SMs that large ones leave idle.
-// Case c works on subset (step mod M_c) and ping-pongs x <-> xtmp; it stops
-// after n_iters_c * M_c steps, and nr_batch_finish moves an odd-parity result
-// back into x.  The tile bodies are the single-case ones (project.cuh,
-// update.cuh), so a batched case computes exactly what nr_ostr_iterate does.
+// A batch step advances every unfinished case by one sub-iteration: one
+// launch of the fused forward projection + gradient of all cases, then one
+// update launch per (potential, one view per subset) class.  Each launch
+// walks one flat list of work items -- (case, detector tile, view) or (case,
+// volume tile, z chunk) -- built from per-case prefix offsets, so cases of
+// different sizes, view counts and potentials share the GPU in the same launch
+// and small cases fill the SMs that large ones leave idle.  Case c works on
+// subset (step mod M_c) and ping-pongs x <-> xtmp; it stops after
+// n_iters_c * M_c steps, and nr_batch_finish moves an odd-parity result back
+// into x.  The tile bodies are the single-case ones (project.cuh, update.cuh),
+// so a batched case computes exactly what nr_ostr_iterate does.
+//
+// Scheduling: one block per work item, so the hardware block scheduler is the
+// work queue and uneven tiles balance themselves.  (A persistent grid of
+// SMs x resident blocks with a static grid-stride split of the same items
+// measured 12-21 % slower than the cases run one after another, because the
+// static split leaves SMs idle behind blocks that drew expensive tiles.)  Cases
+// are ordered by sub-iteration count, longest first, within each class and
+// in the projection order, so the cases still running at step k are a prefix
+// of every item range and each launch covers exactly the active items.
+//
+// The case table travels as a __grid_constant__ kernel parameter (at most
+// 64 cases: ~19 KB, inside the 32 KB parameter limit).  The item decode then
+// runs on block-uniform constant-bank values and the tile reads its case's
+// geometry from the constant bank as the single-case kernels do, instead of
+// from a shared-memory copy that costs registers: the one-view update fits
+// 32 registers (8 resident blocks per SM) without spills.
+#include <cstdint>
+#include <cstring>
+
 #include "project.cuh"
 #include "update.cuh"
 
 namespace nr {
 
 constexpr int BATCH_MAX = 64;
+constexpr int N_CLASSES = 8;
 
 struct CaseDev {
     Geo G;
@@ -35,87 +55,78 @@ struct CaseDev {
     int64_t N;
 };
 
-struct BatchHdr {
+__host__ __device__ constexpr int upd_class(int pot, bool one_view) { return 2 * pot + one_view; }
+
+struct BatchTable {
     int n;
-    int64_t fp_total, up_total;
-    int64_t fp_off[BATCH_MAX + 1], up_off[BATCH_MAX + 1];
-    int64_t pot_lo[4], pot_hi[4];  // update items of each potential (cases sorted by potential)
+    // cases c[] are in class order (potential, then one view per subset), and
+    // by sub-iteration count, longest first, within a class
+    int cls_first[N_CLASSES], cls_end[N_CLASSES];  // cases [first, end) of each class
+    int up_off[BATCH_MAX + 1];                     // update items: prefix over c[]
+    int fp_case[BATCH_MAX];                        // projection order (longest first)
+    int fp_off[BATCH_MAX + 1];                     // projection items: prefix over fp_case
+    CaseDev c[BATCH_MAX];
 };
+static_assert(sizeof(BatchTable) <= 32764 - 16, "kernel parameter limit");
 
-constexpr size_t HDR_BYTES = (sizeof(BatchHdr) + 255) & ~(size_t)255;
-
-__device__ __forceinline__ int find_case(const int64_t* off, int n, int64_t it) {
+__device__ __forceinline__ int find_case(const int* off, int n, int it) {
     int c = 0;
     while (c + 1 < n && it >= off[c + 1]) c++;
     return c;
 }
 
-// All threads copy case c's descriptor into shared memory (word by word).
-__device__ __forceinline__ void load_case(CaseDev& dst, const CaseDev* C, int c, int tid,
-                                          int nthreads) {
-    static_assert(sizeof(CaseDev) % 4 == 0, "word copy");
-    const int* src = (const int*)(C + c);
-    int* d = (int*)&dst;
-    for (int k = tid; k < (int)(sizeof(CaseDev) / 4); k += nthreads) d[k] = src[k];
-}
-
-__global__ void __launch_bounds__(128) fp_batch_kernel(const void* __restrict__ table, int step) {
-    __shared__ CaseDev cd;
+// Projection items [0, hi) of step `step` (hi: the active prefix).  12 resident
+// blocks per SM, as fp_h_kernel.
+__global__ void __launch_bounds__(128, 12) fp_batch_kernel(const __grid_constant__ BatchTable P,
+                                                           int step, int hi) {
     __shared__ ViewSrc src;
-    const BatchHdr* H = (const BatchHdr*)table;
-    const CaseDev* C = (const CaseDev*)((const char*)table + HDR_BYTES);
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    for (int64_t it = blockIdx.x; it < H->fp_total; it += gridDim.x) {
-        const int c = find_case(H->fp_off, H->n, it);
-        __syncthreads();  // previous item's readers of cd / src are done
-        load_case(cd, C, c, tid, 128);
-        __syncthreads();
+    for (int it = blockIdx.x; it < hi; it += gridDim.x) {
+        const int p = find_case(P.fp_off, P.n, it);
+        const CaseDev& cd = P.c[P.fp_case[p]];
+        __syncthreads();  // previous item's readers of src are done
         if (step >= cd.total_sub) continue;
-        const int64_t local = it - H->fp_off[c];
-        const int bx = (int)(local % cd.fp_tx);
-        const int by = (int)((local / cd.fp_tx) % cd.fp_ty);
-        const int bz = (int)(local / ((int64_t)cd.fp_tx * cd.fp_ty));
+        const int local = it - P.fp_off[p];
+        const int bx = local % cd.fp_tx;
+        const int by = (local / cd.fp_tx) % cd.fp_ty;
+        const int bz = local / (cd.fp_tx * cd.fp_ty);
         const int a0 = (step % (int)cd.M) * cd.Vs;
         const float* cur = (step & 1) ? cd.xtmp : cd.x;
         fp_h_tile(cd.G, cur, cd.h, cd.angles, cd.index, a0, cd.y, cd.b, cd.r, bx, by, bz, src);
     }
 }
 
-template <int POT>
-__global__ void __launch_bounds__(256, 5) update_batch_kernel(const void* __restrict__ table,
-                                                           int step) {
-    __shared__ CaseDev cd;
+// Update items [lo, hi) of one (potential, NV) class.  NV = 1 serves the cases
+// whose subsets hold one view (the compile-time view count of update_tile: 32
+// registers, 8 resident blocks per SM); NV = 0 the others.
+template <int POT, int NV>
+__global__ void __launch_bounds__(256, NV ? 8 : 5) update_batch_kernel(
+    const __grid_constant__ BatchTable P, int step, int lo, int hi) {
     __shared__ UpdSmem sm;
-    const BatchHdr* H = (const BatchHdr*)table;
-    const CaseDev* C = (const CaseDev*)((const char*)table + HDR_BYTES);
-    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    for (int64_t it = H->pot_lo[POT] + blockIdx.x; it < H->pot_hi[POT]; it += gridDim.x) {
-        const int c = find_case(H->up_off, H->n, it);
-        __syncthreads();
-        load_case(cd, C, c, tid, 256);
-        __syncthreads();
+    for (int it = lo + blockIdx.x; it < hi; it += gridDim.x) {
+        const int c = find_case(P.up_off, P.n, it);
+        const CaseDev& cd = P.c[c];
+        __syncthreads();  // previous item's readers of sm are done
         if (step >= cd.total_sub) continue;
-        const int64_t local = it - H->up_off[c];
-        const int bx = (int)(local % cd.up_tx);
-        const int by = (int)((local / cd.up_tx) % cd.up_ty);
-        const int bz = (int)(local / ((int64_t)cd.up_tx * cd.up_ty));
+        const int local = it - P.up_off[c];
+        const int bx = local % cd.up_tx;
+        const int by = (local / cd.up_tx) % cd.up_ty;
+        const int bz = local / (cd.up_tx * cd.up_ty);
         const int a0 = (step % (int)cd.M) * cd.Vs;
         const float* cur = (step & 1) ? cd.xtmp : cd.x;
         float* nxt = (step & 1) ? cd.x : cd.xtmp;
-        update_tile<POT>(cd.G, cd.W, cur, nxt, cd.d, cd.h, cd.angles, cd.index, cd.T, a0, cd.Vs, cd.M,
-                         cd.beta, cd.delta, cd.status, bx, by, bz, sm);
+        update_tile<POT, UZC, UPD_OSTR, NV>(cd.G, cd.W, cur, nxt, cd.d, cd.h, cd.angles, cd.index,
+                                            cd.T, a0, cd.Vs, cd.M, cd.beta, cd.delta, cd.status,
+                                            bx, by, bz, sm);
     }
 }
 
 // Cases whose sub-iteration count is odd end in xtmp: copy them back to x.
-__global__ void finish_kernel(const void* __restrict__ table) {
-    const BatchHdr* H = (const BatchHdr*)table;
-    const CaseDev* C = (const CaseDev*)((const char*)table + HDR_BYTES);
-    for (int c = 0; c < H->n; c++) {
-        if ((C[c].total_sub & 1) == 0) continue;
-        const float* __restrict__ s = C[c].xtmp;
-        float* __restrict__ dst = C[c].x;
-        for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < C[c].N;
+__global__ void finish_kernel(const __grid_constant__ BatchTable P) {
+    for (int c = 0; c < P.n; c++) {
+        if ((P.c[c].total_sub & 1) == 0) continue;
+        const float* __restrict__ s = P.c[c].xtmp;
+        float* __restrict__ dst = P.c[c].x;
+        for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < P.c[c].N;
              k += (int64_t)gridDim.x * blockDim.x)
             dst[k] = s[k];
     }
@@ -127,12 +138,23 @@ nr_status ostr_sections(const nr_geom* g, const nr_ostr_params* p, void* ws, siz
                         const float** b, const float** r, const float** angles,
                         const int32_t** index, int** status, BpTab* tab);
 
-static int persistent_blocks(const void* kernel, int threads, size_t smem) {
-    int dev = 0, sms = 152, per = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem);
-    return sms * (per > 0 ? per : 1);
+// A table written by nr_batch_prepare: its counts and offsets are consistent
+// (a table from anywhere else is refused).
+static bool table_ok(const void* table) {
+    if (!table || ((uintptr_t)table & 7) != 0) return false;
+    const BatchTable& P = *(const BatchTable*)table;
+    if (P.n < 1 || P.n > BATCH_MAX || P.fp_off[0] != 0 || P.up_off[0] != 0) return false;
+    bool seen[BATCH_MAX] = {};
+    for (int c = 0; c < P.n; c++) {
+        if (P.fp_off[c + 1] < P.fp_off[c] || P.up_off[c + 1] < P.up_off[c]) return false;
+        const int f = P.fp_case[c];
+        if (f < 0 || f >= P.n || seen[f]) return false;
+        seen[f] = true;
+    }
+    for (int k = 0; k < N_CLASSES; k++)
+        if (P.cls_first[k] < 0 || P.cls_first[k] > P.cls_end[k] || P.cls_end[k] > P.n)
+            return false;
+    return true;
 }
 
 }  // namespace nr
@@ -141,45 +163,53 @@ using namespace nr;
 
 NR_API nr_status nr_batch_table_size(int32_t n_cases, size_t* bytes) {
     if (n_cases <= 0 || n_cases > BATCH_MAX || !bytes) return NR_ERR_BAD_ARGUMENT;
-    *bytes = HDR_BYTES + (size_t)n_cases * sizeof(CaseDev);
+    *bytes = sizeof(BatchTable);
     return NR_OK;
 }
 
 NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, void* table,
                                   size_t table_bytes, int32_t* n_steps, void* stream) {
+    (void)stream;
     size_t need = 0;
     nr_status st = nr_batch_table_size(n_cases, &need);
     if (st != NR_OK) return st;
-    if (!cases || !table || table_bytes < need || ((uintptr_t)table & 255) != 0)
+    if (!cases || !table || table_bytes < need || ((uintptr_t)table & 7) != 0)
         return NR_ERR_WORKSPACE;
-    static_assert(sizeof(BatchHdr) <= HDR_BYTES, "header");
-    // Host image of the table; copied to the device with one cudaMemcpyAsync.
-    char* img = new char[need]();
-    BatchHdr* H = (BatchHdr*)img;
-    CaseDev* C = (CaseDev*)(img + HDR_BYTES);
-    H->n = n_cases;
-    int steps = 0;
-    // cases ordered by potential, so each potential's update items are one range
-    int order[BATCH_MAX];
-    int no = 0;
-    for (int pot = NR_POT_Q2; pot <= NR_POT_HUBER; pot++)
-        for (int c = 0; c < n_cases; c++)
-            if (cases[c].p.potential == pot) order[no++] = c;
-    if (no != n_cases) {
-        delete[] img;
-        return NR_ERR_BAD_ARGUMENT;  // unknown potential
+    for (int c = 0; c < n_cases; c++) {
+        const nr_batch_case& k = cases[c];
+        if (k.n_iters < 0 || !k.x || k.p.subset_num < 1 || k.p.potential < NR_POT_Q2 ||
+            k.p.potential > NR_POT_HUBER)
+            return NR_ERR_BAD_ARGUMENT;
     }
+    auto total_sub = [&](int c) { return cases[c].n_iters * cases[c].p.subset_num; };
+    auto cls_of = [&](int c) {
+        const nr_batch_case& k = cases[c];
+        return upd_class(k.p.potential, k.g.n_angles == k.p.subset_num);
+    };
+    // case order: by class, then by sub-iteration count, longest first (stable)
+    int order[BATCH_MAX];
+    for (int c = 0; c < n_cases; c++) order[c] = c;
+    for (int i = 1; i < n_cases; i++) {
+        const int v = order[i];
+        int j = i;
+        while (j > 0 && (cls_of(order[j - 1]) > cls_of(v) ||
+                         (cls_of(order[j - 1]) == cls_of(v) && total_sub(order[j - 1]) < total_sub(v)))) {
+            order[j] = order[j - 1];
+            j--;
+        }
+        order[j] = v;
+    }
+    BatchTable* P = new BatchTable();
+    P->n = n_cases;
+    int steps = 0;
+    int64_t up_off = 0;
     for (int c = 0; c < n_cases; c++) {
         const nr_batch_case& k = cases[order[c]];
-        CaseDev& d = C[c];
-        if (k.n_iters < 0 || !k.x) {
-            delete[] img;
-            return NR_ERR_BAD_ARGUMENT;
-        }
+        CaseDev& d = P->c[c];
         st = ostr_sections(&k.g, &k.p, k.workspace, k.ws_bytes, &d.xtmp, &d.h, &d.d, &d.y, &d.b,
                            &d.r, &d.angles, &d.index, &d.status, &d.T);
         if (st != NR_OK) {
-            delete[] img;
+            delete P;
             return st;
         }
         const nr_geom& g = k.g;
@@ -190,80 +220,119 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
         d.M = (float)k.p.subset_num;
         d.pot = k.p.potential;
         d.Vs = g.n_angles / k.p.subset_num;
-        d.total_sub = k.n_iters * k.p.subset_num;
+        d.total_sub = total_sub(order[c]);
         d.x = k.x;
         d.fp_tx = (int)cdiv(g.nbx, 32);
         d.fp_ty = (int)cdiv(g.nby, 4);
         d.up_tx = (int)cdiv(g.nx, UTX);
         d.up_ty = (int)cdiv(g.ny, UTY);
         d.N = (int64_t)g.nx * g.ny * g.nz;
-        H->fp_off[c + 1] = H->fp_off[c] + (int64_t)d.fp_tx * d.fp_ty * d.Vs;
-        H->up_off[c + 1] = H->up_off[c] + (int64_t)d.up_tx * d.up_ty * cdiv(g.nz, UZC);
+        up_off += (int64_t)d.up_tx * d.up_ty * cdiv(g.nz, UZC);
+        if (up_off > INT32_MAX) {
+            delete P;
+            return NR_ERR_BAD_ARGUMENT;  // work items are counted in 32 bits
+        }
+        P->up_off[c + 1] = (int)up_off;
         steps = d.total_sub > steps ? d.total_sub : steps;
     }
-    H->fp_total = H->fp_off[n_cases];
-    H->up_total = H->up_off[n_cases];
-    for (int pot = 0; pot < 4; pot++) {
-        H->pot_lo[pot] = H->up_total;
-        H->pot_hi[pot] = H->up_total;
-    }
+    for (int k = 0; k < N_CLASSES; k++) P->cls_first[k] = P->cls_end[k] = 0;
     for (int c = n_cases - 1; c >= 0; c--) {
-        const int pot = C[c].pot;
-        H->pot_lo[pot] = H->up_off[c];
-        if (H->pot_hi[pot] == H->up_total && (c == n_cases - 1 || C[c + 1].pot != pot))
-            H->pot_hi[pot] = H->up_off[c + 1];
+        const int k = upd_class(P->c[c].pot, P->c[c].Vs == 1);
+        if (P->cls_end[k] == 0) P->cls_end[k] = c + 1;
+        P->cls_first[k] = c;
     }
-    const cudaError_t e =
-        cudaMemcpyAsync(table, img, need, cudaMemcpyHostToDevice, as_stream(stream));
-    const cudaError_t e2 = cudaStreamSynchronize(as_stream(stream));  // img is pageable
-    delete[] img;
-    if (e != cudaSuccess || e2 != cudaSuccess) return NR_ERR_CUDA;
+    // projection order: all cases by sub-iteration count, longest first (stable)
+    for (int c = 0; c < n_cases; c++) P->fp_case[c] = c;
+    for (int i = 1; i < n_cases; i++) {
+        const int v = P->fp_case[i];
+        int j = i;
+        while (j > 0 && P->c[P->fp_case[j - 1]].total_sub < P->c[v].total_sub) {
+            P->fp_case[j] = P->fp_case[j - 1];
+            j--;
+        }
+        P->fp_case[j] = v;
+    }
+    int64_t fp_off = 0;
+    for (int p = 0; p < n_cases; p++) {
+        const CaseDev& d = P->c[P->fp_case[p]];
+        fp_off += (int64_t)d.fp_tx * d.fp_ty * d.Vs;
+        if (fp_off > INT32_MAX) {
+            delete P;
+            return NR_ERR_BAD_ARGUMENT;
+        }
+        P->fp_off[p + 1] = (int)fp_off;
+    }
+    memcpy(table, P, sizeof(BatchTable));
+    delete P;
     if (n_steps) *n_steps = steps;
     return NR_OK;
 }
 
-// One step: the projection of all cases, then one update launch per potential
-// (each walks its own item range; a potential no case uses has an empty range).
-static nr_status enqueue_steps(const void* table, int32_t first, int32_t count, cudaStream_t s) {
-    const int fp_blocks = persistent_blocks((const void*)fp_batch_kernel, 128, 0);
-    const int ub0 = persistent_blocks((const void*)update_batch_kernel<NR_POT_Q2>, 256, 0);
-    const int ub1 = persistent_blocks((const void*)update_batch_kernel<NR_POT_LANGE>, 256, 0);
-    const int ub2 = persistent_blocks((const void*)update_batch_kernel<NR_POT_HYPERBOLA>, 256, 0);
-    const int ub3 = persistent_blocks((const void*)update_batch_kernel<NR_POT_HUBER>, 256, 0);
-    const dim3 ut(UTX, UTY);
+namespace {
+
+template <int POT, int NV>
+void launch_class_t(const BatchTable& P, int32_t k, int lo, int hi, cudaStream_t s) {
+    update_batch_kernel<POT, NV><<<hi - lo, dim3(UTX, UTY), 0, s>>>(P, k, lo, hi);
+}
+
+void launch_class(int cls, const BatchTable& P, int32_t k, int lo, int hi, cudaStream_t s) {
+    switch (cls) {
+    case upd_class(NR_POT_Q2, false): return launch_class_t<NR_POT_Q2, 0>(P, k, lo, hi, s);
+    case upd_class(NR_POT_Q2, true): return launch_class_t<NR_POT_Q2, 1>(P, k, lo, hi, s);
+    case upd_class(NR_POT_LANGE, false): return launch_class_t<NR_POT_LANGE, 0>(P, k, lo, hi, s);
+    case upd_class(NR_POT_LANGE, true): return launch_class_t<NR_POT_LANGE, 1>(P, k, lo, hi, s);
+    case upd_class(NR_POT_HYPERBOLA, false):
+        return launch_class_t<NR_POT_HYPERBOLA, 0>(P, k, lo, hi, s);
+    case upd_class(NR_POT_HYPERBOLA, true):
+        return launch_class_t<NR_POT_HYPERBOLA, 1>(P, k, lo, hi, s);
+    case upd_class(NR_POT_HUBER, false): return launch_class_t<NR_POT_HUBER, 0>(P, k, lo, hi, s);
+    default: return launch_class_t<NR_POT_HUBER, 1>(P, k, lo, hi, s);
+    }
+}
+
+// Steps first .. first+count-1: the projection of the active items, then one
+// update launch per class that has active cases (one block per item; the
+// active cases are a prefix of each range, so finished cases cost nothing).
+nr_status enqueue_steps(const BatchTable& P, int32_t first, int32_t count, cudaStream_t s) {
     for (int32_t k = first; k < first + count; k++) {
-        fp_batch_kernel<<<fp_blocks, dim3(32, 4), 0, s>>>(table, k);
-        update_batch_kernel<NR_POT_Q2><<<ub0, ut, 0, s>>>(table, k);
-        update_batch_kernel<NR_POT_LANGE><<<ub1, ut, 0, s>>>(table, k);
-        update_batch_kernel<NR_POT_HYPERBOLA><<<ub2, ut, 0, s>>>(table, k);
-        update_batch_kernel<NR_POT_HUBER><<<ub3, ut, 0, s>>>(table, k);
+        int np = 0;
+        while (np < P.n && P.c[P.fp_case[np]].total_sub > k) np++;
+        if (np == 0) continue;  // every case is done
+        fp_batch_kernel<<<P.fp_off[np], dim3(32, 4), 0, s>>>(P, k, P.fp_off[np]);
+        for (int cls = 0; cls < N_CLASSES; cls++) {
+            int e = P.cls_first[cls];
+            while (e < P.cls_end[cls] && P.c[e].total_sub > k) e++;
+            const int lo = P.up_off[P.cls_first[cls]], hi = P.up_off[e];
+            if (hi > lo) launch_class(cls, P, k, lo, hi, s);
+        }
     }
     return launch_status();
 }
 
+}  // namespace
+
 NR_API nr_status nr_batch_step(const void* table, int32_t step, void* stream) {
-    if (!table || step < 0) return NR_ERR_BAD_ARGUMENT;
-    return enqueue_steps(table, step, 1, as_stream(stream));
+    if (!table_ok(table) || step < 0) return NR_ERR_BAD_ARGUMENT;
+    return enqueue_steps(*(const BatchTable*)table, step, 1, as_stream(stream));
 }
 
 NR_API nr_status nr_batch_finish(const void* table, void* stream) {
-    if (!table) return NR_ERR_BAD_ARGUMENT;
-    finish_kernel<<<1024, 256, 0, as_stream(stream)>>>(table);
+    if (!table_ok(table)) return NR_ERR_BAD_ARGUMENT;
+    finish_kernel<<<1024, 256, 0, as_stream(stream)>>>(*(const BatchTable*)table);
     return launch_status();
 }
 
 NR_API nr_status nr_batch_graph_create(const void* table, int32_t n_steps, void* stream,
                                        void** graph) {
-    if (!table || n_steps < 1 || !graph || !stream) return NR_ERR_BAD_ARGUMENT;
+    if (!table_ok(table) || n_steps < 1 || !graph || !stream) return NR_ERR_BAD_ARGUMENT;
     *graph = nullptr;
+    const BatchTable& P = *(const BatchTable*)table;
     cudaStream_t s = as_stream(stream);
-    // occupancy queries happen before the capture starts
-    persistent_blocks((const void*)fp_batch_kernel, 128, 0);
     if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         return NR_ERR_CUDA;
-    nr_status st = enqueue_steps(table, 0, n_steps, s);
+    nr_status st = enqueue_steps(P, 0, n_steps, s);
     if (st == NR_OK) {
-        finish_kernel<<<1024, 256, 0, s>>>(table);
+        finish_kernel<<<1024, 256, 0, s>>>(P);
         st = launch_status();
     }
     return finish_capture(s, st, graph);

@@ -525,17 +525,21 @@ class Batch:
         self._cases = arr
         size = ctypes.c_size_t(0)
         native.call("nr_batch_table_size", len(cases), ctypes.byref(size))
-        self.table = torch.empty(int(size.value), dtype=torch.uint8, device=self.x[0].device)
+        # host memory: each batch launch carries the table as its kernel parameter
+        self.table = np.zeros(int(size.value), dtype=np.uint8)
         steps = ctypes.c_int32(0)
-        native.call("nr_batch_prepare", arr, len(cases), _p(self.table), size,
+        native.call("nr_batch_prepare", arr, len(cases), self._table_ptr(), size,
                     ctypes.byref(steps), _stream())
         self.n_steps = int(steps.value)
+
+    def _table_ptr(self) -> ctypes.c_void_p:
+        return ctypes.c_void_p(self.table.ctypes.data)
 
     def run(self):
         """All steps and the finish on the current stream; returns the volumes."""
         for k in range(self.n_steps):
-            native.call("nr_batch_step", _p(self.table), k, _stream())
-        native.call("nr_batch_finish", _p(self.table), _stream())
+            native.call("nr_batch_step", self._table_ptr(), k, _stream())
+        native.call("nr_batch_finish", self._table_ptr(), _stream())
         self.check()
         return self.x
 
@@ -555,7 +559,7 @@ class BatchGraph:
         self.handle = ctypes.c_void_p(0)
         self._stream = torch.cuda.Stream()
         self._stream.wait_stream(torch.cuda.current_stream())
-        native.call("nr_batch_graph_create", _p(batch.table), batch.n_steps,
+        native.call("nr_batch_graph_create", batch._table_ptr(), batch.n_steps,
                     ctypes.c_void_p(self._stream.cuda_stream), ctypes.byref(self.handle))
 
     def launch(self) -> None:
