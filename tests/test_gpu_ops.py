@@ -218,6 +218,51 @@ def test_numba_style_float64_buffers(ostr):
     assert maxrel(host, ref) < TOL
 
 
+class DevArray:
+    """A device array known only through ``__cuda_array_interface__`` (what a
+    Numba device array exposes; numba itself is not needed)."""
+
+    def __init__(self, t: torch.Tensor):
+        self._t = t.contiguous()  # owns the memory; never handed to the wrapper
+        self.__cuda_array_interface__ = {
+            "shape": tuple(self._t.shape), "strides": None, "version": 3,
+            "typestr": {torch.float32: "<f4", torch.float64: "<f8",
+                        torch.int32: "<i4"}[self._t.dtype],
+            "data": (self._t.data_ptr(), False)}
+
+
+def test_cuda_array_interface_objects(ostr):
+    """Interface-only device arrays go in and come out in place, with results
+    identical to the same calls on torch tensors (accumulating operators add
+    to what the caller's buffer held)."""
+    z = golden("tiny")
+    g = geom_of(z)
+    ostr.set_geometry(g)
+    A = g.n_angles
+    idx = dev(np.arange(A), torch.int32)
+    ang = dev(z["angles"])
+    x = dev(z["x"])
+    line = torch.zeros(A * g.n_bins, device="cuda")
+    ostr.fprojectCB_1R_GPU_OSTR_cos(x, line, ang, idx, 0, A)
+    line_da = DevArray(torch.zeros(A * g.n_bins, device="cuda"))
+    ostr.fprojectCB_1R_GPU_OSTR_cos(DevArray(x), line_da, DevArray(ang), DevArray(idx), 0, A)
+    assert torch.equal(line_da._t, line)
+
+    h = dev(z["bp_in"])
+    vol = torch.ones(g.n_voxels, device="cuda")
+    ostr.bprojectCB_GPU_SBP(vol, h, idx, ang, 0, A)
+    vol_da = DevArray(torch.ones(g.n_voxels, dtype=torch.float64, device="cuda"))
+    ostr.bprojectCB_GPU_SBP(vol_da, DevArray(h), DevArray(idx), DevArray(ang), 0, A)
+    assert torch.equal(vol_da._t.float(), vol)
+
+    rdd, rd = torch.zeros_like(x), torch.full_like(x, 0.5)
+    ostr.prior_GPU_OSTR(rdd, rd, x, float(z["delta"]), g.z_xy_ratio)
+    rdd_da = DevArray(torch.zeros_like(x))
+    rd_da = DevArray(torch.full_like(x, 0.5))
+    ostr.prior_GPU_OSTR(rdd_da, rd_da, DevArray(x), float(z["delta"]), g.z_xy_ratio)
+    assert torch.equal(rdd_da._t, rdd) and torch.equal(rd_da._t, rd)
+
+
 def test_bad_arguments_raise(ostr):
     from newrecon_gb300.native import NrError
 
