@@ -352,7 +352,7 @@ def batch_bench(args, rank):
         cases.append(dict(geom=g, angles=c.angles, prj=y, blank=np.full_like(y, c.I0),
                           subset_num=c.subset_num, iter_num=c.iter_num, beta=c.beta,
                           delta=c.delta, potential=c.potential))
-    bt = ostr.Batch(cases)
+    bt = ostr.Batch(cases, tune=not args.no_tune)
     steps = min(args.batch_steps, bt.n_steps)
     stream = torch.cuda.current_stream()
     from newrecon_gb300 import native

@@ -36,7 +36,8 @@
 namespace nr {
 
 constexpr int BATCH_MAX = 64;
-constexpr int N_CLASSES = 8;
+constexpr int N_ZC = 3;                      // update slab depths 8, 16, 32 planes
+constexpr int N_CLASSES = 4 * 2 * N_ZC;      // potential x one-view x slab depth
 
 struct CaseDev {
     Geo G;
@@ -51,16 +52,20 @@ struct CaseDev {
     int* status;
     BpTab T;               // the case's back-projection tables
     int fp_tx, fp_ty;      // detector tiles of 32 x 4 bins
-    int up_tx, up_ty;      // volume tiles of 32 x 8 columns (z chunks of UZC planes)
+    int up_tx, up_ty;      // volume tiles of 32 x 8 columns
+    int zc;                // z planes per update item (the plan's upd_planes)
     int64_t N;
 };
 
-__host__ __device__ constexpr int upd_class(int pot, bool one_view) { return 2 * pot + one_view; }
+__host__ __device__ constexpr int zc_index(int zc) { return zc == 8 ? 0 : (zc == 32 ? 2 : 1); }
+__host__ __device__ constexpr int upd_class(int pot, bool one_view, int zc) {
+    return (2 * pot + one_view) * N_ZC + zc_index(zc);
+}
 
 struct BatchTable {
     int n;
-    // cases c[] are in class order (potential, then one view per subset), and
-    // by sub-iteration count, longest first, within a class
+    // cases c[] are in class order (potential, one view per subset, slab
+    // depth), and by sub-iteration count, longest first, within a class
     int cls_first[N_CLASSES], cls_end[N_CLASSES];  // cases [first, end) of each class
     int up_off[BATCH_MAX + 1];                     // update items: prefix over c[]
     int fp_case[BATCH_MAX];                        // projection order (longest first)
@@ -96,10 +101,11 @@ __global__ void __launch_bounds__(128, 12) fp_batch_kernel(const __grid_constant
     }
 }
 
-// Update items [lo, hi) of one (potential, NV) class.  NV = 1 serves the cases
-// whose subsets hold one view (the compile-time view count of update_tile: 32
-// registers, 8 resident blocks per SM); NV = 0 the others.
-template <int POT, int NV>
+// Update items [lo, hi) of one (potential, NV, ZC) class.  NV = 1 serves the
+// cases whose subsets hold one view (the compile-time view count of
+// update_tile: 32 registers, 8 resident blocks per SM); NV = 0 the others.  ZC
+// is the case's slab depth (planes per item), as the autotuner picked it.
+template <int POT, int NV, int ZC>
 __global__ void __launch_bounds__(256, NV ? 8 : 5) update_batch_kernel(
     const __grid_constant__ BatchTable P, int step, int lo, int hi) {
     __shared__ UpdSmem sm;
@@ -122,7 +128,7 @@ __global__ void __launch_bounds__(256, NV ? 8 : 5) update_batch_kernel(
         const Geo G = cd.G;
         const PriorW5 W = cd.W;
         const BpTab T = cd.T;
-        update_tile<POT, UZC, UPD_OSTR, NV>(G, W, cur, nxt, cd.d, cd.h, cd.angles, cd.index, T, a0,
+        update_tile<POT, ZC, UPD_OSTR, NV>(G, W, cur, nxt, cd.d, cd.h, cd.angles, cd.index, T, a0,
                                             cd.Vs, cd.M, cd.beta, cd.delta, cd.status, bx, by, bz,
                                             sm);
     }
@@ -186,13 +192,16 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
     for (int c = 0; c < n_cases; c++) {
         const nr_batch_case& k = cases[c];
         if (k.n_iters < 0 || !k.x || k.p.subset_num < 1 || k.p.potential < NR_POT_Q2 ||
-            k.p.potential > NR_POT_HUBER)
+            k.p.potential > NR_POT_HUBER ||
+            (k.p.upd_planes != 0 && k.p.upd_planes != 8 && k.p.upd_planes != 16 &&
+             k.p.upd_planes != 32))
             return NR_ERR_BAD_ARGUMENT;
     }
     auto total_sub = [&](int c) { return cases[c].n_iters * cases[c].p.subset_num; };
+    auto zc_of = [&](int c) { return cases[c].p.upd_planes == 0 ? UZC : cases[c].p.upd_planes; };
     auto cls_of = [&](int c) {
         const nr_batch_case& k = cases[c];
-        return upd_class(k.p.potential, k.g.n_angles == k.p.subset_num);
+        return upd_class(k.p.potential, k.g.n_angles == k.p.subset_num, zc_of(c));
     };
     // case order: by class, then by sub-iteration count, longest first (stable)
     int order[BATCH_MAX];
@@ -234,8 +243,9 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
         d.fp_ty = (int)cdiv(g.nby, 4);
         d.up_tx = (int)cdiv(g.nx, UTX);
         d.up_ty = (int)cdiv(g.ny, UTY);
+        d.zc = zc_of(order[c]);
         d.N = (int64_t)g.nx * g.ny * g.nz;
-        up_off += (int64_t)d.up_tx * d.up_ty * cdiv(g.nz, UZC);
+        up_off += (int64_t)d.up_tx * d.up_ty * cdiv(g.nz, d.zc);
         if (up_off > INT32_MAX) {
             delete P;
             return NR_ERR_BAD_ARGUMENT;  // work items are counted in 32 bits
@@ -245,7 +255,7 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
     }
     for (int k = 0; k < N_CLASSES; k++) P->cls_first[k] = P->cls_end[k] = 0;
     for (int c = n_cases - 1; c >= 0; c--) {
-        const int k = upd_class(P->c[c].pot, P->c[c].Vs == 1);
+        const int k = upd_class(P->c[c].pot, P->c[c].Vs == 1, P->c[c].zc);
         if (P->cls_end[k] == 0) P->cls_end[k] = c + 1;
         P->cls_first[k] = c;
     }
@@ -278,23 +288,33 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
 
 namespace {
 
-template <int POT, int NV>
+template <int POT, int NV, int ZC>
 void launch_class_t(const BatchTable& P, int32_t k, int lo, int hi, cudaStream_t s) {
-    update_batch_kernel<POT, NV><<<hi - lo, dim3(UTX, UTY), 0, s>>>(P, k, lo, hi);
+    update_batch_kernel<POT, NV, ZC><<<hi - lo, dim3(UTX, UTY), 0, s>>>(P, k, lo, hi);
+}
+
+template <int POT, int NV>
+void launch_class_z(int zi, const BatchTable& P, int32_t k, int lo, int hi, cudaStream_t s) {
+    if (zi == 0) return launch_class_t<POT, NV, 8>(P, k, lo, hi, s);
+    if (zi == 2) return launch_class_t<POT, NV, 32>(P, k, lo, hi, s);
+    return launch_class_t<POT, NV, 16>(P, k, lo, hi, s);
+}
+
+template <int POT>
+void launch_class_nv(bool one, int zi, const BatchTable& P, int32_t k, int lo, int hi,
+                     cudaStream_t s) {
+    if (one) return launch_class_z<POT, 1>(zi, P, k, lo, hi, s);
+    return launch_class_z<POT, 0>(zi, P, k, lo, hi, s);
 }
 
 void launch_class(int cls, const BatchTable& P, int32_t k, int lo, int hi, cudaStream_t s) {
-    switch (cls) {
-    case upd_class(NR_POT_Q2, false): return launch_class_t<NR_POT_Q2, 0>(P, k, lo, hi, s);
-    case upd_class(NR_POT_Q2, true): return launch_class_t<NR_POT_Q2, 1>(P, k, lo, hi, s);
-    case upd_class(NR_POT_LANGE, false): return launch_class_t<NR_POT_LANGE, 0>(P, k, lo, hi, s);
-    case upd_class(NR_POT_LANGE, true): return launch_class_t<NR_POT_LANGE, 1>(P, k, lo, hi, s);
-    case upd_class(NR_POT_HYPERBOLA, false):
-        return launch_class_t<NR_POT_HYPERBOLA, 0>(P, k, lo, hi, s);
-    case upd_class(NR_POT_HYPERBOLA, true):
-        return launch_class_t<NR_POT_HYPERBOLA, 1>(P, k, lo, hi, s);
-    case upd_class(NR_POT_HUBER, false): return launch_class_t<NR_POT_HUBER, 0>(P, k, lo, hi, s);
-    default: return launch_class_t<NR_POT_HUBER, 1>(P, k, lo, hi, s);
+    const int zi = cls % N_ZC, pot = cls / (2 * N_ZC);
+    const bool one = (cls / N_ZC) % 2 == 1;
+    switch (pot) {
+    case NR_POT_Q2: return launch_class_nv<NR_POT_Q2>(one, zi, P, k, lo, hi, s);
+    case NR_POT_LANGE: return launch_class_nv<NR_POT_LANGE>(one, zi, P, k, lo, hi, s);
+    case NR_POT_HYPERBOLA: return launch_class_nv<NR_POT_HYPERBOLA>(one, zi, P, k, lo, hi, s);
+    default: return launch_class_nv<NR_POT_HUBER>(one, zi, P, k, lo, hi, s);
     }
 }
 

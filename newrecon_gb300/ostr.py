@@ -501,9 +501,13 @@ class Batch:
     >>> b = Batch([dict(geom=g1, angles=a1, prj=y1, blank=b1, subset_num=9, iter_num=50,
     ...                 beta=50, delta=0.002, potential="hyperbola"), ...])
     >>> volumes = b.run()            # or: gr = b.graph(); gr.launch()
+
+    tune=True runs the autotuner on each case's plan first (cached per
+    geometry): the batched update then walks each case with its tuned slab
+    depth.  The batched projection always uses 4-step gathers.
     """
 
-    def __init__(self, cases):
+    def __init__(self, cases, tune: bool = False):
         if not 1 <= len(cases) <= 64:
             raise ValueError("a batch holds 1 to 64 cases")
         self.plans, self.x = [], []
@@ -517,6 +521,10 @@ class Batch:
             x0 = c.get("x0")
             x = (torch.zeros(c["geom"].n_voxels, dtype=torch.float32, device=plan.ws.device)
                  if x0 is None else _in(x0).clone())
+            if tune:
+                plan.autotune(x)
+            if "upd_planes" in c:  # an explicit slab depth (8, 16 or 32) wins
+                plan.params.upd_planes = int(c["upd_planes"])
             self.plans.append(plan)
             self.x.append(x)
             arr[k] = NrBatchCase(plan.gc, plan.params, int(c["iter_num"]),

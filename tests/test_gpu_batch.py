@@ -107,6 +107,17 @@ def test_batch_matches_single_reconstructions(mod):
         assert close(xb, xs), c["potential"]
 
 
+def test_batch_slab_depths_match_single(mod):
+    """Cases walked with different slab depths share the launches (one update
+    class per depth) and compute what the single-case path does."""
+    cases = batch_cases()
+    for c, zc in zip(cases, (8, 32, 16, 32)):
+        c["upd_planes"] = zc
+    out = [x.cpu().numpy() for x in mod.Batch(cases).run()]
+    for c, xb in zip(cases, out):
+        assert close(xb, single(mod, c)), (c["potential"], c["upd_planes"])
+
+
 def test_batch_graph_matches_run(mod):
     cases = batch_cases()
     b1 = mod.Batch(cases)
