@@ -50,7 +50,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--batch", type=int, default=0,
                     help="also time N batched reconstructions (persistent launches)")
-    ap.add_argument("--batch-steps", type=int, default=25)
+    ap.add_argument("--batch-steps", type=int, default=0,
+                    help="batch steps to time (0: the whole run, every case to its last "
+                         "iteration)")
+    ap.add_argument("--batch-runs", type=int, default=2,
+                    help="timed replays of the batch graph (the best is reported)")
     ap.add_argument("--batch-config", default="mixed", choices=["mixed", "fullres"],
                     help="mixed: uneven clinical-pitch cases; fullres: 2048x1024x70 breasts "
                          "at 0.085 mm, 3328x1664 detector, 15 views")
@@ -321,8 +325,9 @@ def run_ours(args):
 
 
 def batch_bench(args, rank):
-    """N independent reconstructions of uneven size and view count, advanced by
-    persistent batched launches; the same cases one after another for scale."""
+    """N independent reconstructions of uneven size and view count advanced
+    together by shared batched launches (the whole loop one CUDA graph); the
+    same cases one after another, each through its own graph, for scale."""
     import torch
 
     from newrecon_gb300 import ostr, replicas
@@ -353,43 +358,65 @@ def batch_bench(args, rank):
                           subset_num=c.subset_num, iter_num=c.iter_num, beta=c.beta,
                           delta=c.delta, potential=c.potential))
     bt = ostr.Batch(cases, tune=not args.no_tune)
-    steps = min(args.batch_steps, bt.n_steps)
     stream = torch.cuda.current_stream()
-    from newrecon_gb300 import native
-    tab = bt._table_ptr()  # host table: each launch carries it as its kernel parameter
-    for k in range(min(3, steps)):  # warm-up (advances the cases; timing only)
-        native.call("nr_batch_step", tab, k, stream_ptr())
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for k in range(steps):
-        native.call("nr_batch_step", tab, k, stream_ptr())
-    e1.record(stream)
-    torch.cuda.synchronize()
-    t_batch = e0.elapsed_time(e1) / 1e3
-    bt.check()
+    full = args.batch_steps <= 0 or args.batch_steps >= bt.n_steps
+    steps = bt.n_steps if full else args.batch_steps
     subits = sum(min(steps, cs["iter_num"] * cs["subset_num"]) for cs in cases)
-    # the same cases one at a time (single-reconstruction kernels), same steps
+
+    def timed(launch, reset):
+        """Best of args.batch_runs replays after one warm-up, each from x = 0."""
+        launch()
+        best = float("inf")
+        for _ in range(max(1, args.batch_runs)):
+            reset()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            launch()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) / 1e3)
+        return best
+
+    def zero_all():
+        for xx in bt.x:
+            xx.zero_()
+
+    # the batch: steps 0 .. steps-1 (and the finish) captured once as a CUDA graph
+    gr = bt.graph(steps)
+    t_batch = timed(gr.launch, zero_all)
+    bt.check()
+    gr.close()
+    # the same cases one after another through the single-case kernels: each
+    # case's whole iteration loop as its own graph (or, for a partial run, its
+    # first sub-iterations launched one by one)
     t_seq = 0.0
-    for p, xx in zip(bt.plans, bt.x):
-        xo = torch.empty_like(xx)
-        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a0.record(stream)
-        for k in range(steps):
-            s_ = k % p.params.subset_num
-            p.project(xx, s_)
-            p.update(xx, xo, s_)
-            xx, xo = xo, xx
-        a1.record(stream)
-        torch.cuda.synchronize()
-        t_seq += a0.elapsed_time(a1) / 1e3
-    full_steps = bt.n_steps
+    for p, xx, cs in zip(bt.plans, bt.x, cases):
+        if full:
+            g1 = p.graph(xx, cs["iter_num"])
+            t_seq += timed(g1.launch, xx.zero_)
+            g1.close()
+        else:
+            n = min(steps, cs["iter_num"] * cs["subset_num"])
+            xo = torch.empty_like(xx)
+
+            def run(p=p, xx=xx, xo=xo, n=n):
+                a, b_ = xx, xo
+                for k in range(n):
+                    s_ = k % p.params.subset_num
+                    p.project(a, s_)
+                    p.update(a, b_, s_)
+                    a, b_ = b_, a
+            t_seq += timed(run, xx.zero_)
     vox = sum(cs["geom"].n_voxels for cs in cases)
-    return {"cases": len(cases), "steps_timed": steps, "voxels_total": vox,
+    return {"cases": len(cases), "steps_timed": steps, "whole_run": full,
+            "timing": "CUDA graph replay of " + ("the whole batch (every step and the finish)"
+                                                 if full else f"the first {steps} steps"),
+            "voxels_total": vox, "seconds": t_batch,
             "subset_iters_per_s": subits / t_batch,
             "projections_per_s": subits / t_batch,
-            "volumes_per_hour": len(cases) * 3600.0 / (t_batch / steps * full_steps),
+            "volumes_per_hour": len(cases) * 3600.0 / t_batch if full else None,
             "sequential_subset_iters_per_s": subits / t_seq,
+            "sequential_volumes_per_hour": len(cases) * 3600.0 / t_seq if full else None,
             "workload": ("full resolution: 2048x1024x70 @0.085x0.085x1mm, 3328x1664 det "
                          "@0.085mm, 15 views +-7.5deg, I0 4e3, hyperbola d=0.002 b=200, "
                          "50 iterations" if fullres else

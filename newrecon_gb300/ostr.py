@@ -555,19 +555,25 @@ class Batch:
         for p in self.plans:
             p.check()
 
-    def graph(self) -> "BatchGraph":
-        return BatchGraph(self)
+    def graph(self, n_steps: Optional[int] = None) -> "BatchGraph":
+        """The batch loop as one CUDA graph: every step (or the first n_steps,
+        for timing a part of the run) and the finish."""
+        return BatchGraph(self, n_steps)
 
 
 class BatchGraph:
-    """The whole batch loop (all steps + finish) captured once as a CUDA graph."""
+    """The batch loop (all steps + finish) captured once as a CUDA graph.
+    Each launch() runs it again from the cases' current volumes.  With n_steps
+    below the batch's step count the graph runs only the first steps; the
+    volumes are then intermediate states (for timing and profiling)."""
 
-    def __init__(self, batch: Batch):
+    def __init__(self, batch: Batch, n_steps: Optional[int] = None):
         self.batch = batch
         self.handle = ctypes.c_void_p(0)
         self._stream = torch.cuda.Stream()
         self._stream.wait_stream(torch.cuda.current_stream())
-        native.call("nr_batch_graph_create", batch._table_ptr(), batch.n_steps,
+        steps = batch.n_steps if n_steps is None else int(n_steps)
+        native.call("nr_batch_graph_create", batch._table_ptr(), steps,
                     ctypes.c_void_p(self._stream.cuda_stream), ctypes.byref(self.handle))
 
     def launch(self) -> None:
