@@ -103,10 +103,11 @@ __global__ void __launch_bounds__(128, 12) fp_batch_kernel(const __grid_constant
 
 // Update items [lo, hi) of one (potential, NV, ZC) class.  NV = 1 serves the
 // cases whose subsets hold one view (the compile-time view count of
-// update_tile: 32 registers, 8 resident blocks per SM); NV = 0 the others.  ZC
+// update_tile: 32 registers, 8 resident blocks per SM); NV = 0 the others
+// (no block minimum, as update_kernel: 40 registers).  ZC
 // is the case's slab depth (planes per item), as the autotuner picked it.
 template <int POT, int NV, int ZC>
-__global__ void __launch_bounds__(256, NV ? 8 : 5) update_batch_kernel(
+__global__ void __launch_bounds__(256, NV ? 8 : 0) update_batch_kernel(
     const __grid_constant__ BatchTable P, int step, int lo, int hi) {
     __shared__ UpdSmem sm;
     for (int it = lo + blockIdx.x; it < hi; it += gridDim.x) {

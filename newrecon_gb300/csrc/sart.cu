@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(256) sart_fp_diff_4r_kernel(
 }
 
 template <int KIND, int ZC, int NV>
-__global__ void __launch_bounds__(256) sart_update_kernel(
+__global__ void __launch_bounds__(256, NV == 1 ? 8 : 0) sart_update_kernel(
     const __grid_constant__ Geo G, const __grid_constant__ PriorW5 W,
     const float* __restrict__ x, float* __restrict__ x_out, const float* __restrict__ diff,
     const float* __restrict__ angles, const int32_t* __restrict__ index,

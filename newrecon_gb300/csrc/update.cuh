@@ -8,7 +8,6 @@
 #pragma once
 
 #include <cmath>
-#include <utility>
 
 #include "common.cuh"
 
@@ -59,61 +58,111 @@ __device__ __forceinline__ float rsqrt_approx(float v) {
     return r;
 }
 
-// Neighbour K = ((dz+1)*3 + (dy+1))*3 + (dx+1) of the centre at offset
-// `base` in the shared-memory planes: adds w omega(t) to sdd and w omega(t) t
-// to sd (two accumulator pairs, even/odd K, to shorten the dependency
-// chains).  EDGE: out-of-volume cells hold NaN and count as t = 0.
-template <int POT, bool EDGE, int K>
-__device__ __forceinline__ void nb_term(const float* __restrict__ pb, const float* __restrict__ pc,
-                                        const float* __restrict__ pa, int base, float xc,
-                                        const PriorW5& W, float delta, float inv_delta,
-                                        float& sdd0, float& sd0, float& sdd1, float& sd1) {
-    constexpr int dz = K / 9 - 1, dy = (K / 3) % 3 - 1, dx = K % 3 - 1;
-    if constexpr (K == 13) {
-        return;  // the centre itself
-    } else {
-        constexpr int nxy = (dx != 0) + (dy != 0);
-        const float* pl = dz < 0 ? pb : (dz == 0 ? pc : pa);
-        float t = xc - pl[base + dy * USW + dx];
-        if (EDGE) t = (t == t) ? t : 0.f;
-        float w, wd;
-        if (dz == 0) {
-            w = nxy == 1 ? W.w1 : W.w2;
-            wd = nxy == 1 ? W.d1 : W.d2;
-        } else {
-            w = nxy == 0 ? W.wz : (nxy == 1 ? W.wz1 : W.wz2);
-            wd = nxy == 0 ? W.dz : (nxy == 1 ? W.dz1 : W.dz2);
-        }
-        float wo;
-        if (POT == NR_POT_Q2) {
-            wo = w;
-        } else if (POT == NR_POT_LANGE) {
-            wo = w * rcp_approx(__fmaf_rn(fabsf(t), inv_delta, 1.f));
-        } else if (POT == NR_POT_HYPERBOLA) {
-            const float u = t * inv_delta;
-            wo = w * rsqrt_approx(__fmaf_rn(u, u, 1.f));
-        } else {
-            wo = wd * rcp_approx(fmaxf(fabsf(t), delta));  // w min(1, delta/|t|)
-        }
-        if (K & 1) {
-            sdd1 += wo;
-            sd1 = __fmaf_rn(wo, t, sd1);
-        } else {
-            sdd0 += wo;
-            sd0 = __fmaf_rn(wo, t, sd0);
-        }
-    }
+// Packed FP32 pairs (add / sub / mul / fma on .f32x2): two neighbour terms per
+// instruction, each lane rounded as the scalar operation would be.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk2(f32x2 r, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
 }
 
-template <int POT, bool EDGE, int... Ks>
-__device__ __forceinline__ void prior_all(std::integer_sequence<int, Ks...>,
-                                          const float* __restrict__ pb,
-                                          const float* __restrict__ pc,
-                                          const float* __restrict__ pa, int base, float xc,
-                                          const PriorW5& W, float delta, float inv_delta,
-                                          float* rdd, float* rd) {
-    float a0 = 0.f, b0 = 0.f, a1 = 0.f, b1 = 0.f;
-    (nb_term<POT, EDGE, Ks>(pb, pc, pa, base, xc, W, delta, inv_delta, a0, b0, a1, b1), ...);
+// Neighbour K = ((dz+1)*3 + (dy+1))*3 + (dx+1) of the centre at offset `base`
+// in the shared-memory planes contributes w omega(t) to RDD and w omega(t) t
+// to RD.  Neighbours KA and KB (same weight class) go in one packed step:
+// lane 0 accumulates KA's terms, lane 1 KB's.  Against one neighbour per
+// step this saves the difference, the weight product and both accumulations
+// of every second neighbour (5 instead of 7 instructions per Huber term, 5.5
+// instead of 8 per hyperbola term; measured 5 % / 8 % off the update).  EDGE:
+// out-of-volume cells hold NaN and count as t = 0.
+template <int POT, bool EDGE, int KA, int KB>
+__device__ __forceinline__ void nb_pair(const float* __restrict__ pb, const float* __restrict__ pc,
+                                        const float* __restrict__ pa, int base, f32x2 xc2,
+                                        const PriorW5& W, float delta, float inv_delta,
+                                        f32x2& sdd, f32x2& sd) {
+    constexpr int dza = KA / 9 - 1, dya = (KA / 3) % 3 - 1, dxa = KA % 3 - 1;
+    constexpr int dzb = KB / 9 - 1, dyb = (KB / 3) % 3 - 1, dxb = KB % 3 - 1;
+    constexpr int nxy = (dxa != 0) + (dya != 0);
+    static_assert(nxy == (dxb != 0) + (dyb != 0) && (dza == 0) == (dzb == 0), "one weight class");
+    const float* pla = dza < 0 ? pb : (dza == 0 ? pc : pa);
+    const float* plb = dzb < 0 ? pb : (dzb == 0 ? pc : pa);
+    f32x2 t2 = sub2(xc2, pk2(pla[base + dya * USW + dxa], plb[base + dyb * USW + dxb]));
+    float ta, tb;
+    upk2(t2, ta, tb);
+    if (EDGE) {
+        ta = (ta == ta) ? ta : 0.f;
+        tb = (tb == tb) ? tb : 0.f;
+        t2 = pk2(ta, tb);
+    }
+    float w, wd;
+    if (dza == 0) {
+        w = nxy == 1 ? W.w1 : W.w2;
+        wd = nxy == 1 ? W.d1 : W.d2;
+    } else {
+        w = nxy == 0 ? W.wz : (nxy == 1 ? W.wz1 : W.wz2);
+        wd = nxy == 0 ? W.dz : (nxy == 1 ? W.dz1 : W.dz2);
+    }
+    f32x2 wo2;
+    if (POT == NR_POT_Q2) {
+        wo2 = pk2(w, w);
+    } else if (POT == NR_POT_LANGE) {
+        wo2 = mul2(pk2(w, w), pk2(rcp_approx(__fmaf_rn(fabsf(ta), inv_delta, 1.f)),
+                                  rcp_approx(__fmaf_rn(fabsf(tb), inv_delta, 1.f))));
+    } else if (POT == NR_POT_HYPERBOLA) {
+        const f32x2 u2 = mul2(t2, pk2(inv_delta, inv_delta));
+        float qa, qb;
+        upk2(fma2(u2, u2, pk2(1.f, 1.f)), qa, qb);
+        wo2 = mul2(pk2(w, w), pk2(rsqrt_approx(qa), rsqrt_approx(qb)));
+    } else {
+        wo2 = mul2(pk2(wd, wd), pk2(rcp_approx(fmaxf(fabsf(ta), delta)),
+                                    rcp_approx(fmaxf(fabsf(tb), delta))));
+    }
+    sdd = add2(sdd, wo2);
+    sd = fma2(wo2, t2, sd);
+}
+
+// The 26 neighbours as 13 equal-weight pairs: (dx = -1, dx = +1) of each
+// (dy, dz) row, and the dx = 0 cells paired across dy or dz.
+template <int POT, bool EDGE>
+__device__ __forceinline__ void prior_pairs(const float* __restrict__ pb,
+                                            const float* __restrict__ pc,
+                                            const float* __restrict__ pa, int base, float xc,
+                                            const PriorW5& W, float delta, float inv_delta,
+                                            float* rdd, float* rd) {
+    const f32x2 xc2 = pk2(xc, xc);
+    f32x2 sdd = pk2(0.f, 0.f), sd = pk2(0.f, 0.f);
+#define NR_PAIR(a, b) nb_pair<POT, EDGE, a, b>(pb, pc, pa, base, xc2, W, delta, inv_delta, sdd, sd)
+    NR_PAIR(0, 2); NR_PAIR(3, 5); NR_PAIR(6, 8);      // dz = -1 rows
+    NR_PAIR(9, 11); NR_PAIR(12, 14); NR_PAIR(15, 17); // dz = 0 rows
+    NR_PAIR(18, 20); NR_PAIR(21, 23); NR_PAIR(24, 26);  // dz = +1 rows
+    NR_PAIR(1, 7); NR_PAIR(19, 25); NR_PAIR(4, 22); NR_PAIR(10, 16);
+#undef NR_PAIR
+    float a0, a1, b0, b1;
+    upk2(sdd, a0, a1);
+    upk2(sd, b0, b1);
     *rdd = a0 + a1;
     *rd = b0 + b1;
 }
@@ -308,11 +357,9 @@ __device__ __forceinline__ void update_tile(
             const int base = r * USW + c;
             if (KIND != UPD_SART) {
                 if (edge_xy || z == 0 || z == g.nz - 1)
-                    prior_all<POT, true>(std::make_integer_sequence<int, 27>{}, pb, pc, pa, base,
-                                         xc, W, delta, inv_delta, &rdd, &rd);
+                    prior_pairs<POT, true>(pb, pc, pa, base, xc, W, delta, inv_delta, &rdd, &rd);
                 else
-                    prior_all<POT, false>(std::make_integer_sequence<int, 27>{}, pb, pc, pa, base,
-                                          xc, W, delta, inv_delta, &rdd, &rd);
+                    prior_pairs<POT, false>(pb, pc, pa, base, xc, W, delta, inv_delta, &rdd, &rd);
             }
             float xn;
             if (KIND == UPD_OSTR) {
@@ -339,8 +386,12 @@ __device__ __forceinline__ void update_tile(
 }
 
 // One block per (x, y) tile and chunk of ZC planes; NV as in update_tile.
+// One-view kernels are held to 32 registers (8 resident blocks per SM: the
+// paired prior would otherwise take 35-38).  The others carry no block
+// minimum (40-44 registers, no spills); a minimum of 1 lets ptxas take 80-119
+// and one of 5 spills 80 bytes.
 template <int POT, int ZC, int NV>
-__global__ void __launch_bounds__(256) update_kernel(
+__global__ void __launch_bounds__(256, NV == 1 ? 8 : 0) update_kernel(
     const __grid_constant__ Geo G, const __grid_constant__ PriorW5 W,
     const float* __restrict__ x, float* __restrict__ x_out, const float* __restrict__ d,
     const float* __restrict__ h, const float* __restrict__ angles,
