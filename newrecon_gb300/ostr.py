@@ -368,6 +368,8 @@ class OSTR:
                                    float(beta), float(delta if potential != "q2" else 1.0))
         self.params.fp_stage = 1 if stage else 0
         self.gc = geom.to_c()
+        self.history = None      # objectives of a monotone iterate()
+        self.rejected_at = None  # the iteration a monotone iterate() undid
         size = ctypes.c_size_t(0)
         native.call("nr_ostr_workspace_size", ctypes.byref(self.gc), ctypes.byref(self.params),
                     ctypes.byref(size))
@@ -391,10 +393,36 @@ class OSTR:
                     _p(y), _p(b), _p(s), ws, n, _stream())
         self._keep = (ang, y, b, s)
 
-    def iterate(self, x: torch.Tensor, n_iters: int) -> torch.Tensor:
+    def iterate(self, x: torch.Tensor, n_iters: int, monotone: bool = False) -> torch.Tensor:
+        """n_iters iterations (every subset once each) on x in place.
+
+        monotone=True accepts an iteration only if it does not raise the FP64
+        penalized-likelihood objective (ordered subsets do not guarantee a
+        monotone decrease near convergence): the first iteration that would
+        raise it, or make it NaN, is undone and the loop stops there.
+        ``history`` then holds the objectives of the accepted iterates (the
+        start included) and ``rejected_at`` the rejected iteration, or None.
+        Each check costs one objective evaluation (a projection of all views
+        and the penalty)."""
         ws, n = self._ws()
-        native.call("nr_ostr_iterate", ctypes.byref(self.gc), ctypes.byref(self.params), _p(x),
-                    int(n_iters), ws, n, _stream())
+        if not monotone:
+            native.call("nr_ostr_iterate", ctypes.byref(self.gc), ctypes.byref(self.params),
+                        _p(x), int(n_iters), ws, n, _stream())
+            return x
+        prev = torch.empty_like(x)
+        hist = [self.total_objective(x)]
+        self.rejected_at = None
+        for k in range(int(n_iters)):
+            prev.copy_(x)
+            native.call("nr_ostr_iterate", ctypes.byref(self.gc), ctypes.byref(self.params),
+                        _p(x), 1, ws, n, _stream())
+            f = self.total_objective(x)
+            if not f <= hist[-1]:
+                x.copy_(prev)
+                self.rejected_at = k
+                break
+            hist.append(f)
+        self.history = hist
         return x
 
     def subiter(self, x: torch.Tensor, subset: int) -> torch.Tensor:
@@ -594,12 +622,13 @@ class BatchGraph:
 
 def reconstruct(geom: Geometry, prj, blank, scatter=None, *, angles, subset_num: int,
                 iter_num: int, beta: float, delta: float, potential: str = "lange",
-                gamma_mode: str = "length", x0=None):
+                gamma_mode: str = "length", x0=None, monotone: bool = False):
     """OSTR reconstruction: transmission counts in, attenuation (1/mm) out.
 
     prj, blank, scatter: [view][i][j] in original view order (the layout
     load_prj produces).  Returns the volume [z][y][x]; numpy when prj was a
-    host array, else a CUDA tensor.
+    host array, else a CUDA tensor.  monotone=True stops before the first
+    iteration that would raise the FP64 objective (OSTR.iterate).
     """
     plan = OSTR(geom, subset_num=subset_num, beta=beta, delta=delta, potential=potential,
                 gamma_mode=gamma_mode, has_scatter=scatter is not None)
@@ -608,6 +637,6 @@ def reconstruct(geom: Geometry, prj, blank, scatter=None, *, angles, subset_num:
         x = torch.zeros(geom.n_voxels, dtype=torch.float32, device=plan.ws.device)
     else:
         x = _in(x0).clone()
-    plan.iterate(x, iter_num)
+    plan.iterate(x, iter_num, monotone=monotone)
     plan.check()
     return _like_input(prj, x)

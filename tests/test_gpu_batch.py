@@ -132,6 +132,29 @@ def test_batch_graph_matches_run(mod):
     gr.close()
 
 
+def test_partial_batch_graph_matches_steps(mod):
+    """A graph of the first k steps (and the finish) runs what k step calls
+    and the finish run, from the same volumes."""
+    import ctypes
+
+    from newrecon_gb300 import native
+
+    cases = batch_cases()
+    k = 5
+    b1 = mod.Batch(cases)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for step in range(k):
+        native.call("nr_batch_step", b1._table_ptr(), step, stream)
+    native.call("nr_batch_finish", b1._table_ptr(), stream)
+    b2 = mod.Batch(cases)
+    gr = b2.graph(k)
+    gr.launch()
+    torch.cuda.synchronize()
+    for x1, x2 in zip(b1.x, b2.x):
+        assert torch.equal(x1, x2)
+    gr.close()
+
+
 def test_autotune_variants_agree_and_cache(mod, tmp_path, monkeypatch):
     """Every kernel variant computes the same sub-iteration; the tuner caches."""
     import json

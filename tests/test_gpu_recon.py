@@ -211,3 +211,46 @@ def test_staged_projection_is_bit_identical(mod, cfgname):
         hs.append((torch.stack(outs), x0))
     assert torch.equal(hs[0][0], hs[1][0])
     assert torch.equal(hs[0][1], hs[1][1])
+
+
+def test_monotone_iterations_accept_only_decreases(mod):
+    """monotone=True keeps the FP64 objective non-increasing; while no
+    iteration is rejected it computes exactly what plain iterations do."""
+    z = golden("tiny")
+    g = geom_of(z)
+    kw = dict(subset_num=3, beta=float(z["beta"]), delta=float(z["delta"]), potential="lange")
+    plan = mod.OSTR(g, **kw)
+    plan.setup(z["angles"], z["y"], z["b"])
+    x = torch.zeros(g.n_voxels, device="cuda")
+    plan.iterate(x, 4, monotone=True)
+    h = plan.history
+    assert all(b <= a for a, b in zip(h, h[1:]))
+    n_ok = len(h) - 1
+    ref = mod.OSTR(g, **kw)
+    ref.setup(z["angles"], z["y"], z["b"])
+    xr = torch.zeros(g.n_voxels, device="cuda")
+    ref.iterate(xr, n_ok)
+    torch.cuda.synchronize()
+    assert torch.equal(x, xr)
+    assert plan.rejected_at is None or plan.rejected_at == n_ok
+
+
+def test_monotone_undoes_a_rising_iteration(mod, monkeypatch):
+    """An iteration whose objective rises (planted on the host) is undone and
+    the loop stops: x is the iterate before it."""
+    z = golden("tiny")
+    g = geom_of(z)
+    kw = dict(subset_num=3, beta=float(z["beta"]), delta=float(z["delta"]), potential="lange")
+    plan = mod.OSTR(g, **kw)
+    plan.setup(z["angles"], z["y"], z["b"])
+    values = iter([10.0, 5.0, 7.0, 1.0])
+    monkeypatch.setattr(plan, "total_objective", lambda x: next(values))
+    x = torch.zeros(g.n_voxels, device="cuda")
+    plan.iterate(x, 3, monotone=True)
+    assert plan.history == [10.0, 5.0] and plan.rejected_at == 1
+    ref = mod.OSTR(g, **kw)
+    ref.setup(z["angles"], z["y"], z["b"])
+    xr = torch.zeros(g.n_voxels, device="cuda")
+    ref.iterate(xr, 1)
+    torch.cuda.synchronize()
+    assert torch.equal(x, xr)
