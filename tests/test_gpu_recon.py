@@ -254,3 +254,20 @@ def test_monotone_undoes_a_rising_iteration(mod, monkeypatch):
     ref.iterate(xr, 1)
     torch.cuda.synchronize()
     assert torch.equal(x, xr)
+
+
+def test_pinned_inputs_return_a_pinned_volume(mod):
+    """Host tensors in pinned memory give the volume back in pinned memory (the
+    download skips the pageable bounce), equal to the device result."""
+    z = golden("tiny")
+    g = geom_of(z)
+    kw = dict(angles=z["angles"], subset_num=3, iter_num=2, beta=float(z["beta"]),
+              delta=float(z["delta"]), potential="lange")
+    y = torch.from_numpy(z["y"]).pin_memory()
+    b = torch.from_numpy(z["b"]).pin_memory()
+    vol = mod.reconstruct(g, y, b, **kw)
+    assert vol.device.type == "cpu" and vol.is_pinned()
+    ref = mod.reconstruct(g, y.cuda(), b.cuda(), **kw)
+    assert torch.equal(vol, ref.cpu())
+    pageable = mod.reconstruct(g, torch.from_numpy(z["y"]), torch.from_numpy(z["b"]), **kw)
+    assert not pageable.is_pinned() and torch.equal(pageable, vol)
