@@ -18,6 +18,14 @@ namespace nr {
 
 #define NR_FINF __int_as_float(0x7f800000)
 
+// min(a, b, c) in one three-input min (sm_100 and later): the walk takes the
+// nearest of the three axis crossings once per segment.
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
 // Per-axis walk state.
 struct Axis {
     float first;   // distance (mm) from the entry point to the first plane crossed
@@ -153,7 +161,7 @@ __device__ __forceinline__ bool trace(const Geo& G, const float* __restrict__ vo
 #pragma unroll
         for (int k = 0; k < K; k++) {
             on[k] = s < smax;
-            const float m = fminf(fminf(tx, ty), tz);
+            const float m = fmin3(tx, ty, tz);
             seg[k] = m - s;
             id[k] = idx;
             if (on[k]) {

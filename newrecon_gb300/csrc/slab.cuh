@@ -141,7 +141,7 @@ __device__ __forceinline__ void walk_slab(const float* __restrict__ vals, int& i
 #pragma unroll
         for (int k = 0; k < K; k++) {
             on[k] = s < send;
-            const float m = fminf(fminf(tx, ty), tz);
+            const float m = fmin3(tx, ty, tz);
             seg[k] = m - s;
             id[k] = idx;
             if (on[k]) {
