@@ -71,7 +71,7 @@ static Layout layout(const nr_geom& g, const nr_ostr_params& p) {
     L.r = p.has_scatter ? take(A * B * sizeof(float)) : (size_t)-1;
     L.d = take(N * sizeof(float));
     L.xtmp = take(N * sizeof(float));
-    L.h = take(Vs * B * sizeof(float));
+    L.h = take((Vs * B + bp_pad(g)) * sizeof(float));  // + zeros the tap pairs may reach
     L.bpx = take((size_t)A * g.nz * g.nx * sizeof(float4));
     L.bpy = take((size_t)A * g.nz * g.ny * sizeof(float4));
     L.gc = take(A * B * sizeof(float));
@@ -235,6 +235,9 @@ NR_API nr_status nr_ostr_setup(const nr_geom* g, const nr_ostr_params* p, const 
     // gc <- yry(gc, r) * gamma, original order, identity index.
     if ((st = launch_gamma_yry(*g, p->gamma_mode, w.gc, angles, w.gc, w.gr, s)) != NR_OK)
         return st;
+    if (cudaMemsetAsync(w.h + (int64_t)Vs * g->nbx * g->nby, 0, bp_pad(*g) * sizeof(float), s) !=
+        cudaSuccess)
+        return NR_ERR_CUDA;
     if (cudaMemsetAsync(w.d, 0, N * sizeof(float), s) != cudaSuccess) return NR_ERR_CUDA;
     // d = SBP(gamma*yry) over all views, original order (Tomo_OSTR_gold.cpp:528-565).
     if ((st = launch_bp(*g, true, w.d, w.gc, angles, nullptr, 0, A, s)) != NR_OK) return st;

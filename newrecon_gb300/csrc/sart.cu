@@ -69,7 +69,7 @@ SartLayout sart_layout(const nr_geom& g, const nr_sart_params& p) {
     L.angles = take(A * sizeof(float));
     L.p = take(A * B * sizeof(float));
     L.norm = take(A * B * sizeof(float));
-    L.diff = take(Vs * B * sizeof(float));
+    L.diff = take((Vs * B + bp_pad(g)) * sizeof(float));  // + zeros the tap pairs may reach
     L.xtmp = take(N * sizeof(float));
     L.bpx = take((size_t)A * g.nz * g.nx * sizeof(float4));
     L.bpy = take((size_t)A * g.nz * g.ny * sizeof(float4));
@@ -377,6 +377,9 @@ NR_API nr_status nr_sart_setup(const nr_geom* g, const nr_sart_params* p, const 
     if ((st = launch_clear_status(w.status, s)) != NR_OK) return st;
     if ((st = launch_subset_index(w.index, angles, w.angles, A, M, s)) != NR_OK) return st;
     if ((st = launch_bp_tables(*g, w.angles, w.index, w.bpx, w.bpy, s)) != NR_OK) return st;
+    if (cudaMemsetAsync(w.diff + (int64_t)Vs * g->nbx * g->nby, 0, bp_pad(*g) * sizeof(float),
+                        s) != cudaSuccess)
+        return NR_ERR_CUDA;
     // [view][i][j] original order -> [view][j][i] subset order.
     if ((st = launch_transpose(w.p, line, g->nbx, g->nby, A, M, Vs, s)) != NR_OK) return st;
     if (p->supersample) {

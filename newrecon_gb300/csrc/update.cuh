@@ -184,15 +184,22 @@ struct UpdSmem {
 // the voxel centre meets the detector plane at x0 + (x1 - x0) t(z), y0 +
 // (y1 - y0) t(z)).  Neither depends on the volume, so they are tabulated once
 // per reconstruction, per view (subset order), plane and column / row, with
-// the arithmetic of bp.cu's sbp_term in reciprocal-multiply form:
-//   x[(a nz + z) nx + i] = {ilb, fracI, (x0 - x1)^2, tap bits}
-//   y[(a nz + z) ny + j] = {jlb * BINSx, fracJ, (y0 - y1)^2 + (z0 - z1)^2, tap bits}
-// Tap bits: x gives i0 | i1<<1 | i0<<2 | i1<<3, y gives j0 | j0<<1 | j1<<2 |
-// j1<<3 (0 when the plane holds the source, Tomo_OSTR.cu:1643), so bit k of
-// their AND says whether tap k = (00, 10, 01, 11) of the bilinear stencil lies
-// on the detector (the rules of :1684-1715).  Each update reads one entry of
-// each per voxel and view (the x entries of a warp are consecutive, its y
-// entry is one broadcast); the tables of a subset stay in L2.
+// the arithmetic of bp.cu's sbp_term in reciprocal-multiply form, as a tap
+// pair and its weights:
+//   x[(a nz + z) nx + i] = {c, w0, w1, (x0 - x1)^2}
+//   y[(a nz + z) ny + j] = {r * BINSx, v0, v1, (y0 - y1)^2 + (z0 - z1)^2}
+// The bilinear stencil's columns are ilb, ilb + 1 with weights 1 - fracI,
+// fracI; a column off the detector gets weight 0 (the rules of
+// Tomo_OSTR.cu:1684-1715), and c is ilb clamped to [0, BINSx - 2] with the
+// weights moved to the columns they belong to, so both loads of a pair are
+// in bounds and need no test.  Rows likewise (both weights 0 when the plane
+// holds the source, :1643).  Interior taps compute exactly what the masked
+// stencil did; an edge tap adds w * h + 0 * h' = w * h.  With a detector one
+// bin wide (or high) the second load of a pair lands up to BINSx + 1 floats
+// past the subset's views: the h sections carry that many zeros (bp_pad).
+// Each update reads one entry of each per voxel and view (the x entries of a
+// warp are consecutive, its y entry is one broadcast); the tables of a subset
+// stay in L2.
 struct BpTab {
     const float4* __restrict__ x;
     const float4* __restrict__ y;
@@ -200,6 +207,29 @@ struct BpTab {
 
 __device__ __forceinline__ float bp_tt(const nr_geom& g, const ViewSrc& vs, float z1) {
     return z1 != vs.z0 ? __fdividef(-g.detectorR - vs.z0, z1 - vs.z0) : 0.f;
+}
+
+// Floats of zero padding after an h section (see the tables above).
+__host__ __device__ inline int64_t bp_pad(const nr_geom& g) { return (int64_t)g.nbx + 1; }
+
+// The tap pair (c, c + 1) of two taps at (lb, lb + 1) with weights (w0, w1)
+// on a line of n detector bins, weights of off-detector taps already 0.
+__device__ __forceinline__ void bp_pair(int lb, float w0, float w1, int n, int& c, float& p0,
+                                        float& p1) {
+    c = max(0, min(n - 2, lb));
+    if (lb == c) {
+        p0 = w0;
+        p1 = w1;
+    } else if (lb == c - 1) {  // lb = -1: only tap lb + 1 = c can be on the detector
+        p0 = w1;
+        p1 = 0.f;
+    } else if (lb == c + 1) {  // lb = n - 1 (n >= 2): only tap lb = c + 1
+        p0 = 0.f;
+        p1 = w0;
+    } else {                   // both taps off the detector (w0 = w1 = 0)
+        p0 = 0.f;
+        p1 = 0.f;
+    }
 }
 
 __device__ __forceinline__ float4 bp_entry_x(const nr_geom& g, const ViewSrc& vs, float tt,
@@ -211,10 +241,12 @@ __device__ __forceinline__ float4 bp_entry_x(const nr_geom& g, const ViewSrc& vs
     int ilb = (int)floorf(imb);
     if (imb < (float)ilb + 0.5f) ilb -= 1;
     const float fracI = imb - ((float)ilb + 0.5f);
-    const int i0 = (ilb < g.nbx) && (ilb >= 0);
-    const int i1 = (ilb < g.nbx - 1) && (ilb >= -1);
-    return make_float4(__int_as_float(ilb), fracI, ddx * ddx,
-                       __int_as_float(i0 | (i1 << 1) | (i0 << 2) | (i1 << 3)));
+    const bool i0 = (ilb < g.nbx) && (ilb >= 0);
+    const bool i1 = (ilb < g.nbx - 1) && (ilb >= -1);
+    int c;
+    float p0, p1;
+    bp_pair(ilb, i0 ? 1.f - fracI : 0.f, i1 ? fracI : 0.f, g.nbx, c, p0, p1);
+    return make_float4(__int_as_float(c), p0, p1, ddx * ddx);
 }
 
 __device__ __forceinline__ float4 bp_entry_y(const nr_geom& g, const ViewSrc& vs, float z1,
@@ -227,10 +259,12 @@ __device__ __forceinline__ float4 bp_entry_y(const nr_geom& g, const ViewSrc& vs
     int jlb = (int)floorf(jmb);
     if (jmb < (float)jlb + 0.5f) jlb -= 1;
     const float fracJ = jmb - ((float)jlb + 0.5f);
-    const int j0 = valid && (jlb < g.nby) && (jlb >= 0);
-    const int j1 = valid && (jlb < g.nby - 1) && (jlb >= -1);
-    return make_float4(__int_as_float(jlb * g.nbx), fracJ, ddy * ddy + ddz * ddz,
-                       __int_as_float(j0 | (j0 << 1) | (j1 << 2) | (j1 << 3)));
+    const bool j0 = valid && (jlb < g.nby) && (jlb >= 0);
+    const bool j1 = valid && (jlb < g.nby - 1) && (jlb >= -1);
+    int r;
+    float p0, p1;
+    bp_pair(jlb, j0 ? 1.f - fracJ : 0.f, j1 ? fracJ : 0.f, g.nby, r, p0, p1);
+    return make_float4(__int_as_float(r * g.nbx), p0, p1, ddy * ddy + ddz * ddz);
 }
 
 // One sub-iteration's update, fused: SBP of h (subset views, [view][j][i]),
@@ -325,33 +359,22 @@ __device__ __forceinline__ void update_tile(
             const float4* ty = T.y + ((int64_t)a0 * g.nz + z) * g.ny + iy;
             const int64_t sx = (int64_t)g.nz * g.nx, sy = (int64_t)g.nz * g.ny;
             for (int t = 0; t < (NV ? NV : nv); t++, p += B, tx += sx, ty += sy) {
+                // tap pair (c, c + 1) x rows (r, r + 1), off-detector taps
+                // weighted 0 and their loads kept in bounds by the tables
                 const float4 ex = __ldg(tx);
                 const float4 ey = __ldg(ty);
-                const int m = __float_as_int(ex.w) & __float_as_int(ey.w);
-                const float fracI = ex.y, fracJ = ey.y;
-                const float dw = __fdividef(sv[t].s2, ex.z + ey.z);
+                const float dw = __fdividef(sv[t].s2, ex.w + ey.w);
                 const float* q0 = p + (__float_as_int(ey.x) + __float_as_int(ex.x));
                 const float* q1 = q0 + g.nbx;
-                float d1 = 0.f, d2 = 0.f;
-                float s1 = 0.f, s2 = 0.f;  // sensitivity taps (OS-SART only)
-                if (m & 1) {
-                    d1 = (1.f - fracI) * __ldg(q0);
-                    s1 = 1.f - fracI;
+                float d1 = ex.y * __ldg(q0);
+                d1 = d1 + ex.z * __ldg(q0 + 1);
+                float d2 = ex.y * __ldg(q1);
+                d2 = d2 + ex.z * __ldg(q1 + 1);
+                capL = capL + (ey.y * d1 + ey.z * d2) * g.vz * dw;
+                if (KIND != UPD_OSTR) {  // sensitivity: the same weights on ones
+                    const float s1 = ex.y + ex.z;
+                    sens = sens + (ey.y * s1 + ey.z * s1) * g.vz * dw;
                 }
-                if (m & 2) {
-                    d1 = d1 + fracI * __ldg(q0 + 1);
-                    s1 = s1 + fracI;
-                }
-                if (m & 4) {
-                    d2 = (1.f - fracI) * __ldg(q1);
-                    s2 = 1.f - fracI;
-                }
-                if (m & 8) {
-                    d2 = d2 + fracI * __ldg(q1 + 1);
-                    s2 = s2 + fracI;
-                }
-                capL = capL + ((1.f - fracJ) * d1 + fracJ * d2) * g.vz * dw;
-                if (KIND != UPD_OSTR) sens = sens + ((1.f - fracJ) * s1 + fracJ * s2) * g.vz * dw;
             }
             float rdd = 0.f, rd = 0.f;
             const int base = r * USW + c;
