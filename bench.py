@@ -539,7 +539,11 @@ def e2e_ours(args, cfg, y, b):
     ostr.reconstruct(g, y_h, b_h, **kw)  # warm-up
     torch.cuda.synchronize()
     ts = []
+    vol = None
     for _ in range(args.e2e_runs):
+        # the caller is done with the previous volume (its pinned block goes
+        # back to torch's host cache, as in a stream of reconstructions)
+        vol = None
         t0 = time.perf_counter()
         vol = ostr.reconstruct(g, y_h, b_h, **kw)
         torch.cuda.synchronize()
@@ -752,7 +756,9 @@ def run_ossart(args):
         sart.ossart_reconstruct(g, l_h, **kw)
         torch.cuda.synchronize()
         ts = []
+        vol = None
         for _ in range(args.e2e_runs):
+            vol = None  # the previous volume released, as in ostr's e2e leg
             t0 = time.perf_counter()
             vol = sart.ossart_reconstruct(g, l_h, **kw)
             torch.cuda.synchronize()
