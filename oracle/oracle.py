@@ -6,8 +6,8 @@ build of the reference.
                       float32 (the timed CPU baseline).
 ``Reference()``    -- oracle/_ref/libostr_ref.so, the reference's own kernel
                       bodies and gold driver compiled for the CPU by
-                      oracle/build_ref.sh (only where the reference sources
-                      are present; never on the GPU machine).
+                      oracle/build_ref.sh (only on a machine that holds the
+                      reference sources).
 """
 from __future__ import annotations
 
