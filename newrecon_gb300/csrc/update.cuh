@@ -20,10 +20,16 @@ constexpr int UPLANE = USW * USH;
 
 // The five distinct neighbour weights 1/sqrt(dx^2+dy^2+(dz zr)^2) of the
 // 26-neighbourhood (in-plane face, in-plane diagonal, z face, z edge, z
-// corner) and the same times delta (Huber).
-struct PriorW5 {
-    float w1, w2, wz, wz1, wz2;
-    float d1, d2, dz, dz1, dz2;
+// corner), the same times delta (Huber), 1/delta and 1, each duplicated into
+// both halves of a packed FP32 pair: the penalty works on neighbour pairs
+// (nb_pair), and a pair operand read whole from the constant bank costs no
+// instruction to assemble.
+enum { W_FACE, W_DIAG, W_ZFACE, W_ZEDGE, W_ZCORNER, W_CLASSES };
+struct alignas(8) PriorW5 {
+    float2 w[W_CLASSES];   // weight of each class
+    float2 wd[W_CLASSES];  // weight x delta
+    float2 inv_delta;      // 1 / delta (hyperbola)
+    float2 one;
 };
 
 __host__ inline PriorW5 make_w5(float zxy, float delta) {
@@ -31,17 +37,15 @@ __host__ inline PriorW5 make_w5(float zxy, float delta) {
         const float dist = std::sqrt((float)(dx * dx + dy * dy) + (float)(dz * dz) * zxy * zxy);
         return (float)(1.0 / (double)dist);
     };
+    const float cls[W_CLASSES] = {w(1, 0, 0), w(1, 1, 0), w(0, 0, 1), w(1, 0, 1), w(1, 1, 1)};
     PriorW5 p;
-    p.w1 = w(1, 0, 0);
-    p.w2 = w(1, 1, 0);
-    p.wz = w(0, 0, 1);
-    p.wz1 = w(1, 0, 1);
-    p.wz2 = w(1, 1, 1);
-    p.d1 = p.w1 * delta;
-    p.d2 = p.w2 * delta;
-    p.dz = p.wz * delta;
-    p.dz1 = p.wz1 * delta;
-    p.dz2 = p.wz2 * delta;
+    for (int k = 0; k < W_CLASSES; k++) {
+        p.w[k] = make_float2(cls[k], cls[k]);
+        p.wd[k] = make_float2(cls[k] * delta, cls[k] * delta);
+    }
+    const float idl = 1.f / delta;
+    p.inv_delta = make_float2(idl, idl);
+    p.one = make_float2(1.f, 1.f);
     return p;
 }
 
@@ -68,6 +72,10 @@ __device__ __forceinline__ f32x2 pk2(float a, float b) {
 }
 __device__ __forceinline__ void upk2(f32x2 r, float& a, float& b) {
     asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+// A duplicated pair stored as float2, read as one 64-bit value.
+__device__ __forceinline__ f32x2 ld2(const float2& v) {
+    return *reinterpret_cast<const f32x2*>(&v);
 }
 __device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
     f32x2 r;
@@ -117,28 +125,23 @@ __device__ __forceinline__ void nb_pair(const float* __restrict__ pb, const floa
         tb = (tb == tb) ? tb : 0.f;
         t2 = pk2(ta, tb);
     }
-    float w, wd;
-    if (dza == 0) {
-        w = nxy == 1 ? W.w1 : W.w2;
-        wd = nxy == 1 ? W.d1 : W.d2;
-    } else {
-        w = nxy == 0 ? W.wz : (nxy == 1 ? W.wz1 : W.wz2);
-        wd = nxy == 0 ? W.dz : (nxy == 1 ? W.dz1 : W.dz2);
-    }
+    constexpr int cls = dza == 0 ? (nxy == 1 ? W_FACE : W_DIAG)
+                                 : (nxy == 0 ? W_ZFACE : (nxy == 1 ? W_ZEDGE : W_ZCORNER));
+    const f32x2 w2 = ld2(W.w[cls]);
     f32x2 wo2;
     if (POT == NR_POT_Q2) {
-        wo2 = pk2(w, w);
+        wo2 = w2;
     } else if (POT == NR_POT_LANGE) {
-        wo2 = mul2(pk2(w, w), pk2(rcp_approx(__fmaf_rn(fabsf(ta), inv_delta, 1.f)),
-                                  rcp_approx(__fmaf_rn(fabsf(tb), inv_delta, 1.f))));
+        wo2 = mul2(w2, pk2(rcp_approx(__fmaf_rn(fabsf(ta), inv_delta, 1.f)),
+                           rcp_approx(__fmaf_rn(fabsf(tb), inv_delta, 1.f))));
     } else if (POT == NR_POT_HYPERBOLA) {
-        const f32x2 u2 = mul2(t2, pk2(inv_delta, inv_delta));
+        const f32x2 u2 = mul2(t2, ld2(W.inv_delta));
         float qa, qb;
-        upk2(fma2(u2, u2, pk2(1.f, 1.f)), qa, qb);
-        wo2 = mul2(pk2(w, w), pk2(rsqrt_approx(qa), rsqrt_approx(qb)));
+        upk2(fma2(u2, u2, ld2(W.one)), qa, qb);
+        wo2 = mul2(w2, pk2(rsqrt_approx(qa), rsqrt_approx(qb)));
     } else {
-        wo2 = mul2(pk2(wd, wd), pk2(rcp_approx(fmaxf(fabsf(ta), delta)),
-                                    rcp_approx(fmaxf(fabsf(tb), delta))));
+        wo2 = mul2(ld2(W.wd[cls]), pk2(rcp_approx(fmaxf(fabsf(ta), delta)),
+                                       rcp_approx(fmaxf(fabsf(tb), delta))));
     }
     sdd = add2(sdd, wo2);
     sd = fma2(wo2, t2, sd);
