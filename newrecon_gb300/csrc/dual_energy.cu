@@ -24,9 +24,12 @@ constexpr int DE_MAX_WEIGHTS = 16;
 
 struct DeWeights {
     double w[DE_MAX_WEIGHTS];
+    float w1[DE_MAX_WEIGHTS], w2[DE_MAX_WEIGHTS];  // w = w1 + w2 + (|.| <= 2^-47 |w|)
+    unsigned fast;     // bit k: weight k takes the FP32 path (de_fast)
     int k;
     int masked;        // 1: he and le multiplied by (he > level) first
     double level;
+    float level_f;     // the largest float <= level: (double)h > level iff h > level_f
 };
 
 __device__ __forceinline__ int im8_bin(double v) {
@@ -37,6 +40,53 @@ __device__ __forceinline__ int im8_bin(double v) {
 
 __device__ __forceinline__ double de_value(double h, double l, double w) {
     return __dadd_rn(h, -__dmul_rn(l, w));
+}
+
+// float(double(b) - double(a) * w) without the FP64 pipe, or NaN when the
+// FP32 evaluation cannot decide it (the caller then takes de_value).
+//
+// a w1 = p1 + e1 exactly (FMA), a w2 rounds once; two error-free sums give
+// b - a w ~ hi + lo with hi = RN(hi + lo).  Every term dropped on the way
+// (a w2's rounding, the w tail, the float sums of the small terms) and both
+// roundings of the double evaluation move the value by less than
+// B = 2^-43 (|b| + |p1|) (the bound works out near 2^-44.4).  So when
+// |lo| + B stays below half the gap between hi and its nearest neighbour
+// (a quarter ulp below a power of two), the double path rounds to hi as
+// well.  Otherwise -- about (|b| + |p1|) / |hi| x 2^-19 of the outputs, and
+// tiny, huge or non-finite values -- the answer is left to FP64.  a = 0 is
+// exact in float (b - 0 w1, with IEEE's signed zeros, as double does).
+__device__ __forceinline__ float de_fast(float b, float a, float w1, float w2) {
+    if (a == 0.f) return __fsub_rn(b, __fmul_rn(a, w1));
+    const float p1 = __fmul_rn(a, w1);
+    const float e1 = __fmaf_rn(a, w1, -p1);
+    const float q = __fmul_rn(a, w2);
+    const float s = __fsub_rn(b, p1);  // TwoSum(b, -p1)
+    const float bp = __fsub_rn(s, b);
+    const float ap = __fsub_rn(s, bp);
+    const float serr = __fadd_rn(__fsub_rn(b, ap), __fsub_rn(__fsub_rn(0.f, p1), bp));
+    const float t = __fsub_rn(__fsub_rn(serr, e1), q);
+    const float hi = __fadd_rn(s, t);  // TwoSum(s, t)
+    const float tp = __fsub_rn(hi, s);
+    const float sp = __fsub_rn(hi, tp);
+    const float lo = __fadd_rn(__fsub_rn(s, sp), __fsub_rn(t, tp));
+    const float B = __fmul_rn(__fadd_rn(fabsf(b), fabsf(p1)), 0x1p-43f);
+    const unsigned hb = __float_as_uint(hi) & 0x7fffffffu;
+    const int e = (int)(hb >> 23);
+    const float ap1 = fabsf(p1);
+    if (e >= 27 && e < 255 && ap1 >= 0x1p-100f && ap1 <= 0x1p100f) {
+        const int te = e - 24 - ((hb & 0x7fffffu) == 0u);
+        const float T = __uint_as_float((unsigned)te << 23);
+        if (__fadd_rn(fabsf(lo), B) < T) return hi;
+    }
+    return __int_as_float(0x7fc00000);
+}
+
+__device__ __forceinline__ float de_out(float b, float a, int k, const DeWeights& W) {
+    if ((W.fast >> k) & 1u) {
+        const float r = de_fast(b, a, W.w1[k], W.w2[k]);
+        if (r == r) return r;
+    }
+    return __double2float_rn(de_value(b, a, W.w[k]));
 }
 
 // d[k][i] = float(he[i] - le[i] * w_k).  VEC (n a multiple of 4, so that every
@@ -52,26 +102,25 @@ __global__ void __launch_bounds__(256) de_subtract_kernel(const float* __restric
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4; q += stride) {
         const float4 h4 = __ldg(reinterpret_cast<const float4*>(he) + q);
         const float4 l4 = __ldg(reinterpret_cast<const float4*>(le) + q);
-        double h[4] = {h4.x, h4.y, h4.z, h4.w};
-        double l[4] = {l4.x, l4.y, l4.z, l4.w};
+        float h[4] = {h4.x, h4.y, h4.z, h4.w};
+        float l[4] = {l4.x, l4.y, l4.z, l4.w};
         if (W.masked)
             for (int t = 0; t < 4; t++)
-                if (!(h[t] > W.level)) h[t] = l[t] = 0.0;
+                if (!(h[t] > W.level_f)) h[t] = l[t] = 0.f;
         for (int k = 0; k < W.k; k++) {
             float4 o;
-            o.x = __double2float_rn(de_value(h[0], l[0], W.w[k]));
-            o.y = __double2float_rn(de_value(h[1], l[1], W.w[k]));
-            o.z = __double2float_rn(de_value(h[2], l[2], W.w[k]));
-            o.w = __double2float_rn(de_value(h[3], l[3], W.w[k]));
+            o.x = de_out(h[0], l[0], k, W);
+            o.y = de_out(h[1], l[1], k, W);
+            o.z = de_out(h[2], l[2], k, W);
+            o.w = de_out(h[3], l[3], k, W);
             __stcs(reinterpret_cast<float4*>(d + (int64_t)k * n) + q, o);
         }
     }
     // everything when !VEC
     for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
-        double h = he[i], l = le[i];
-        if (W.masked && !(h > W.level)) h = l = 0.0;
-        for (int k = 0; k < W.k; k++)
-            d[(int64_t)k * n + i] = __double2float_rn(de_value(h, l, W.w[k]));
+        float h = he[i], l = le[i];
+        if (W.masked && !(h > W.level_f)) h = l = 0.f;
+        for (int k = 0; k < W.k; k++) d[(int64_t)k * n + i] = de_out(h, l, k, W);
     }
 }
 
@@ -130,11 +179,27 @@ NR_API nr_status nr_de_subtract(const float* he, const float* le, const double* 
     // float4 path: he, le, d 16-byte aligned (checked) and n % 4 == 0, so each
     // row d + k n is aligned too; q < n/4 keeps every access below n.
     DeWeights W;
-    for (int k = 0; k < n_weights; k++) W.w[k] = weights[k];
-    for (int k = n_weights; k < DE_MAX_WEIGHTS; k++) W.w[k] = 0.0;
+    W.fast = 0u;
+    for (int k = 0; k < DE_MAX_WEIGHTS; k++) {
+        const double w = k < n_weights ? weights[k] : 0.0;
+        W.w[k] = w;
+        // w = w1 + w2 + w3: both differences are exact in double
+        const float w1 = (float)w;
+        const float w2 = (float)(w - (double)w1);
+        const double w3 = (w - (double)w1) - (double)w2;
+        W.w1[k] = w1;
+        W.w2[k] = w2;
+        const double aw = std::fabs(w);
+        if (k < n_weights && std::isfinite(w) && aw >= 0x1p-60 && aw <= 0x1p60 &&
+            std::fabs(w3) <= std::ldexp(aw, -47))
+            W.fast |= 1u << k;
+    }
     W.k = n_weights;
     W.masked = mask_level >= 0.0;
     W.level = mask_level;
+    float lf = (float)mask_level;
+    if ((double)lf > mask_level) lf = std::nextafterf(lf, -INFINITY);
+    W.level_f = lf;
     cudaStream_t s = as_stream(stream);
     if (n > 0 && n % 4 == 0)
         de_subtract_kernel<true><<<de_blocks(n / 4), 256, 0, s>>>(he, le, d, n, W);

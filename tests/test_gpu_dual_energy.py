@@ -104,3 +104,63 @@ def test_bad_arguments(mod):
     assert e.value.code == 2
     with pytest.raises(ValueError):
         mod.subtract(he, he, list(np.linspace(0, 1, 17)))
+
+
+def _hard_cases(weights, n_each, seed):
+    """he, le pairs that put b - a w near float rounding boundaries, in heavy
+    cancellation, and on special values, for the weights given."""
+    rng = np.random.default_rng(seed)
+    he, le = [], []
+    for w in weights:
+        if w == 0.0 or not np.isfinite(w):
+            continue
+        # near-ties: a w = ulp(b)/2 (1 + delta), delta log-uniform 2^-30 .. 2^-8, either sign
+        b = rng.uniform(0.5, 4.0, n_each).astype(np.float32) * np.float32(2.0) ** rng.integers(-20, 20, n_each).astype(np.float32)
+        ulp = np.spacing(b).astype(np.float64)
+        delta = 2.0 ** rng.uniform(-30, -8, n_each) * rng.choice([-1.0, 1.0], n_each)
+        k = rng.integers(1, 8, n_each) * 2 - 1          # odd multiples of half an ulp
+        a = (k * ulp / 2 * (1 + delta) / w).astype(np.float32)
+        he.append(b); le.append(a)
+        # cancellation: b = a w (1 + delta), delta log-uniform 2^-24 .. 2^-2
+        a = rng.gamma(2.0, 0.02, n_each).astype(np.float32)
+        delta = 2.0 ** rng.uniform(-24, -2, n_each) * rng.choice([-1.0, 1.0], n_each)
+        he.append((a.astype(np.float64) * w * (1 + delta)).astype(np.float32)); le.append(a)
+    # special values and magnitudes
+    sp = np.array([0.0, -0.0, 1e-45, -1e-45, 1e-38, 3.4e38, -3.4e38, np.inf, -np.inf, np.nan,
+                   1.0, -1.0, 2.0 ** -100, 2.0 ** 100, 0.0501, 0.08], np.float32)
+    hh, ll = np.meshgrid(sp, sp)
+    he.append(hh.ravel()); le.append(ll.ravel())
+    he = np.concatenate(he).astype(np.float32)
+    le = np.concatenate(le).astype(np.float32)
+    pad = (-he.size) % 4
+    return np.concatenate([he, np.ones(pad, np.float32)]), np.concatenate([le, np.ones(pad, np.float32)])
+
+
+def _same_bits(got, ref):
+    nan = np.isnan(ref)
+    assert np.array_equal(np.isnan(got), nan)
+    return np.array_equal(got[~nan].view(np.uint32), ref[~nan].view(np.uint32))
+
+
+@pytest.mark.parametrize("weights", [
+    [0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.8, 0.9],
+    [1 / 3, np.pi / 10, -0.45, 1e-30, 3e25, 1.0, 0.0, 2.0 ** -40, 1.2345678901234567],
+], ids=["syncrecon", "awkward"])
+def test_fp32_path_is_bit_exact_on_hard_cases(mod, weights):
+    """The FP32 evaluation (with its FP64 fallback) reproduces
+    float(double(he) - double(le) * w) bit for bit, signed zeros included,
+    near float rounding boundaries, in heavy cancellation and on special values."""
+    he, le = _hard_cases(weights, 200_000, 5)
+    d, _ = mod.subtract(torch.from_numpy(he).cuda(), torch.from_numpy(le).cuda(), weights)
+    ref, _ = de.subtract(he, le, weights)
+    got = d.cpu().numpy()
+    for k in range(len(weights)):
+        assert _same_bits(got[k], ref[k]), weights[k]
+    # the unaligned (scalar) path too, and the mask
+    n = he.size - 3
+    d, _ = mod.subtract(torch.from_numpy(he[:n]).cuda(), torch.from_numpy(le[:n]).cuda(), weights,
+                        mask_level=0.05)
+    ref, _ = de.subtract(he[:n], le[:n], weights, mask_level=0.05)
+    got = d.cpu().numpy()
+    for k in range(len(weights)):
+        assert _same_bits(got[k], ref[k]), weights[k]
