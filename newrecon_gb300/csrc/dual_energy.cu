@@ -26,6 +26,7 @@ struct DeWeights {
     double w[DE_MAX_WEIGHTS];
     float w1[DE_MAX_WEIGHTS], w2[DE_MAX_WEIGHTS];  // w = w1 + w2 + (|.| <= 2^-47 |w|)
     unsigned fast;     // bit k: weight k takes the FP32 path (de_fast)
+    unsigned pow2;     // bit k: weight k is a power of two (a w exact in float)
     int k;
     int masked;        // 1: he and le multiplied by (he > level) first
     double level;
@@ -43,50 +44,89 @@ __device__ __forceinline__ double de_value(double h, double l, double w) {
 }
 
 // float(double(b) - double(a) * w) without the FP64 pipe, or NaN when the
-// FP32 evaluation cannot decide it (the caller then takes de_value).
+// FP32 evaluation cannot decide it (the caller then takes the FP64 path).
 //
 // a w1 = p1 + e1 exactly (FMA), a w2 rounds once; two error-free sums give
-// b - a w ~ hi + lo with hi = RN(hi + lo).  Every term dropped on the way
-// (a w2's rounding, the w tail, the float sums of the small terms) and both
-// roundings of the double evaluation move the value by less than
-// B = 2^-43 (|b| + |p1|) (the bound works out near 2^-44.4).  So when
-// |lo| + B stays below half the gap between hi and its nearest neighbour
-// (a quarter ulp below a power of two), the double path rounds to hi as
-// well.  Otherwise -- about (|b| + |p1|) / |hi| x 2^-19 of the outputs, and
-// tiny, huge or non-finite values -- the answer is left to FP64.  a = 0 is
-// exact in float (b - 0 w1, with IEEE's signed zeros, as double does).
+// b - a w ~ hi + lo with hi = RN(hi + lo).  The terms dropped on the way (a
+// w2's rounding and the w tail, under 2^-47 |p1|; the float sums of the
+// small terms, under 2^-48 (2 |s| + 3 |p1|), s = RN(b - p1)) and both
+// roundings of the double evaluation (under 2^-53 (|b| + 2 |p1|)) add up to
+// less than 2^-45.2 |p1| + 2^-46.9 |b|; B = 2^-44 |p1| + 2^-46 |b| bounds
+// them with a factor of 1.8 to spare.  If hi + m and hi - m, m = |lo| + B,
+// both round back to hi, the double evaluation lies strictly inside hi's
+// rounding interval and rounds to hi too.  Otherwise -- about 2^-20 |p1| /
+// |hi| of the outputs (cancellation), and tiny, huge or non-finite products
+// -- the answer is left to FP64.
 __device__ __forceinline__ float de_fast(float b, float a, float w1, float w2) {
-    if (a == 0.f) return __fsub_rn(b, __fmul_rn(a, w1));
     const float p1 = __fmul_rn(a, w1);
+    const float ap1 = fabsf(p1);
+    if (!(ap1 >= 0x1p-100f && ap1 <= 0x1p100f)) return __int_as_float(0x7fc00000);
     const float e1 = __fmaf_rn(a, w1, -p1);
     const float q = __fmul_rn(a, w2);
     const float s = __fsub_rn(b, p1);  // TwoSum(b, -p1)
     const float bp = __fsub_rn(s, b);
     const float ap = __fsub_rn(s, bp);
-    const float serr = __fadd_rn(__fsub_rn(b, ap), __fsub_rn(__fsub_rn(0.f, p1), bp));
+    const float serr = __fsub_rn(__fsub_rn(b, ap), __fadd_rn(p1, bp));
     const float t = __fsub_rn(__fsub_rn(serr, e1), q);
     const float hi = __fadd_rn(s, t);  // TwoSum(s, t)
     const float tp = __fsub_rn(hi, s);
     const float sp = __fsub_rn(hi, tp);
     const float lo = __fadd_rn(__fsub_rn(s, sp), __fsub_rn(t, tp));
-    const float B = __fmul_rn(__fadd_rn(fabsf(b), fabsf(p1)), 0x1p-43f);
-    const unsigned hb = __float_as_uint(hi) & 0x7fffffffu;
-    const int e = (int)(hb >> 23);
-    const float ap1 = fabsf(p1);
-    if (e >= 27 && e < 255 && ap1 >= 0x1p-100f && ap1 <= 0x1p100f) {
-        const int te = e - 24 - ((hb & 0x7fffffu) == 0u);
-        const float T = __uint_as_float((unsigned)te << 23);
-        if (__fadd_rn(fabsf(lo), B) < T) return hi;
-    }
+    const float B = __fmaf_rn(fabsf(b), 0x1p-46f, __fmul_rn(ap1, 0x1p-44f));
+    const float m = __fadd_rn(fabsf(lo), B);
+    if (__fadd_rn(hi, m) == hi && __fsub_rn(hi, m) == hi) return hi;
     return __int_as_float(0x7fc00000);
 }
 
-__device__ __forceinline__ float de_out(float b, float a, int k, const DeWeights& W) {
-    if ((W.fast >> k) & 1u) {
-        const float r = de_fast(b, a, W.w1[k], W.w2[k]);
+// The FP64 evaluation, out of line: inlined, ptxas predicates it and runs
+// it for every output beside the FP32 one.
+__device__ __noinline__ float de_slow(float b, float a, double w) {
+    return __double2float_rn(de_value(b, a, w));
+}
+
+template <int K>
+__device__ __forceinline__ float de_out(float b, float a, const DeWeights& W) {
+    if ((W.pow2 >> K) & 1u) {
+        // a w exact: double(b) - a w needs more than 53 bits only when one
+        // operand is below 2^-29 of the other, and then both roundings land
+        // on the float of b - a w (the nearest float midpoint is 2^-25 away)
+        const float p = __fmul_rn(a, W.w1[K]);
+        const float ap = fabsf(p);
+        if (a == 0.f || (ap >= 0x1p-100f && ap <= 0x1p100f)) return __fsub_rn(b, p);
+    } else if ((W.fast >> K) & 1u) {
+        const float r = de_fast(b, a, W.w1[K], W.w2[K]);
         if (r == r) return r;
+        // a = 0 is exact in float: b - 0 w1, with IEEE's signed zeros as in double
+        if (a == 0.f) return __fsub_rn(b, __fmul_rn(a, W.w1[K]));
     }
-    return __double2float_rn(de_value(b, a, W.w[k]));
+    return de_slow(b, a, W.w[K]);
+}
+
+// Weights K, K + 1, ... of four voxels (16-byte store per weight) or of one.
+template <int K>
+__device__ __forceinline__ void de_row(const float (&h)[4], const float (&l)[4],
+                                       const DeWeights& W, float* __restrict__ d, int64_t n,
+                                       int64_t q) {
+    if constexpr (K < DE_MAX_WEIGHTS) {
+        if (K >= W.k) return;
+        float4 o;
+        o.x = de_out<K>(h[0], l[0], W);
+        o.y = de_out<K>(h[1], l[1], W);
+        o.z = de_out<K>(h[2], l[2], W);
+        o.w = de_out<K>(h[3], l[3], W);
+        __stcs(reinterpret_cast<float4*>(d + (int64_t)K * n) + q, o);
+        de_row<K + 1>(h, l, W, d, n, q);
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void de_one(float h, float l, const DeWeights& W,
+                                       float* __restrict__ d, int64_t n, int64_t i) {
+    if constexpr (K < DE_MAX_WEIGHTS) {
+        if (K >= W.k) return;
+        d[(int64_t)K * n + i] = de_out<K>(h, l, W);
+        de_one<K + 1>(h, l, W, d, n, i);
+    }
 }
 
 // d[k][i] = float(he[i] - le[i] * w_k).  VEC (n a multiple of 4, so that every
@@ -107,20 +147,15 @@ __global__ void __launch_bounds__(256) de_subtract_kernel(const float* __restric
         if (W.masked)
             for (int t = 0; t < 4; t++)
                 if (!(h[t] > W.level_f)) h[t] = l[t] = 0.f;
-        for (int k = 0; k < W.k; k++) {
-            float4 o;
-            o.x = de_out(h[0], l[0], k, W);
-            o.y = de_out(h[1], l[1], k, W);
-            o.z = de_out(h[2], l[2], k, W);
-            o.w = de_out(h[3], l[3], k, W);
-            __stcs(reinterpret_cast<float4*>(d + (int64_t)k * n) + q, o);
-        }
+        // unrolled over the weights: each weight's constants are fixed
+        // constant-bank operands
+        de_row<0>(h, l, W, d, n, q);
     }
     // everything when !VEC
     for (int64_t i = 4 * n4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
         float h = he[i], l = le[i];
         if (W.masked && !(h > W.level_f)) h = l = 0.f;
-        for (int k = 0; k < W.k; k++) d[(int64_t)k * n + i] = de_out(h, l, k, W);
+        de_one<0>(h, l, W, d, n, i);
     }
 }
 
@@ -180,6 +215,7 @@ NR_API nr_status nr_de_subtract(const float* he, const float* le, const double* 
     // row d + k n is aligned too; q < n/4 keeps every access below n.
     DeWeights W;
     W.fast = 0u;
+    W.pow2 = 0u;
     for (int k = 0; k < DE_MAX_WEIGHTS; k++) {
         const double w = k < n_weights ? weights[k] : 0.0;
         W.w[k] = w;
@@ -193,6 +229,10 @@ NR_API nr_status nr_de_subtract(const float* he, const float* le, const double* 
         if (k < n_weights && std::isfinite(w) && aw >= 0x1p-60 && aw <= 0x1p60 &&
             std::fabs(w3) <= std::ldexp(aw, -47))
             W.fast |= 1u << k;
+        int ex = 0;
+        if (k < n_weights && std::isfinite(w) && w != 0.0 && std::fabs(std::frexp(w, &ex)) == 0.5 &&
+            ex > -90 && ex < 90)
+            W.pow2 |= 1u << k;
     }
     W.k = n_weights;
     W.masked = mask_level >= 0.0;
