@@ -892,7 +892,7 @@ def run_dual_energy(args):
         "metric": DE_METRIC, "value": 1e3 / ms.mean() * len(w), "unit": "volumes/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": float(ms.mean()), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64 arithmetic, f32 volumes",
+        "vs_baseline": None, "dtype": "f32 error-free arithmetic (f64 for undecided near-ties), f32 volumes",
         "data": "synthetic gamma-distributed volumes",
         "config": {"workload": f"{g.nx}x{g.ny}x{g.nz} HE and LE volumes, 9 weights 0.1..0.9, "
                                f"slice-{g.nz // 2} entropies (syncrecon.m)",
