@@ -57,10 +57,13 @@ __device__ __forceinline__ double de_value(double h, double l, double w) {
 // rounding interval and rounds to hi too.  Otherwise -- about 2^-20 |p1| /
 // |hi| of the outputs (cancellation), and tiny, huge or non-finite products
 // -- the answer is left to FP64.
-__device__ __forceinline__ float de_fast(float b, float a, float w1, float w2) {
+// b - a w ~ hi + lo as above, with B bounding |the double value - (hi + lo)|;
+// false for tiny, huge or non-finite products.
+__device__ __forceinline__ bool de_sum(float b, float a, float w1, float w2, float& hi, float& lo,
+                                       float& B) {
     const float p1 = __fmul_rn(a, w1);
     const float ap1 = fabsf(p1);
-    if (!(ap1 >= 0x1p-100f && ap1 <= 0x1p100f)) return __int_as_float(0x7fc00000);
+    if (!(ap1 >= 0x1p-100f && ap1 <= 0x1p100f)) return false;
     const float e1 = __fmaf_rn(a, w1, -p1);
     const float q = __fmul_rn(a, w2);
     const float s = __fsub_rn(b, p1);  // TwoSum(b, -p1)
@@ -68,14 +71,35 @@ __device__ __forceinline__ float de_fast(float b, float a, float w1, float w2) {
     const float ap = __fsub_rn(s, bp);
     const float serr = __fsub_rn(__fsub_rn(b, ap), __fadd_rn(p1, bp));
     const float t = __fsub_rn(__fsub_rn(serr, e1), q);
-    const float hi = __fadd_rn(s, t);  // TwoSum(s, t)
+    hi = __fadd_rn(s, t);  // TwoSum(s, t)
     const float tp = __fsub_rn(hi, s);
     const float sp = __fsub_rn(hi, tp);
-    const float lo = __fadd_rn(__fsub_rn(s, sp), __fsub_rn(t, tp));
-    const float B = __fmaf_rn(fabsf(b), 0x1p-46f, __fmul_rn(ap1, 0x1p-44f));
-    const float m = __fadd_rn(fabsf(lo), B);
-    if (__fadd_rn(hi, m) == hi && __fsub_rn(hi, m) == hi) return hi;
+    lo = __fadd_rn(__fsub_rn(s, sp), __fsub_rn(t, tp));
+    B = __fmaf_rn(fabsf(b), 0x1p-46f, __fmul_rn(ap1, 0x1p-44f));
+    return true;
+}
+
+__device__ __forceinline__ float de_fast(float b, float a, float w1, float w2) {
+    float hi, lo, B;
+    if (de_sum(b, a, w1, w2, hi, lo, B)) {
+        const float m = __fadd_rn(fabsf(lo), B);
+        if (__fadd_rn(hi, m) == hi && __fsub_rn(hi, m) == hi) return hi;
+    }
     return __int_as_float(0x7fc00000);
+}
+
+// im8_bin of a double value v known as |v - (hi + lo)| <= B: round(255 v)
+// half away from zero, saturated to [0, 255]; -1 when v lies too close to a
+// bin edge (255 v = k + 1/2) for the float evaluation to tell.
+__device__ __forceinline__ int de_bin(float hi, float lo, float B) {
+    const float yh = __fmul_rn(255.f, hi);
+    const float ye = __fmaf_rn(255.f, hi, -yh);  // exact
+    const float y = __fadd_rn(yh, __fmaf_rn(255.f, lo, ye));
+    const float err = __fmaf_rn(255.f, B, __fmaf_rn(fabsf(y), 0x1p-22f, 0x1p-40f));
+    const float f = floorf(__fadd_rn(y, 0.5f));
+    const float dist = __fsub_rn(0.5f, fabsf(__fsub_rn(y, f)));
+    if (!(dist > err)) return -1;  // also NaN
+    return f <= 0.f ? 0 : (f >= 255.f ? 255 : (int)f);
 }
 
 // The FP64 evaluation, out of line: inlined, ptxas predicates it and runs
@@ -171,9 +195,17 @@ __global__ void __launch_bounds__(256) de_hist_kernel(const float* __restrict__ 
     __syncthreads();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len;
          i += (int64_t)gridDim.x * blockDim.x) {
-        double h = he[begin + i], l = le[begin + i];
-        if (W.masked && !(h > W.level)) h = l = 0.0;
-        for (int k = 0; k < W.k; k++) atomicAdd(&sh[k * 256 + im8_bin(de_value(h, l, W.w[k]))], 1);
+        float h = he[begin + i], l = le[begin + i];
+        if (W.masked && !(h > W.level_f)) h = l = 0.f;
+        for (int k = 0; k < W.k; k++) {
+            int bin = -1;
+            if ((W.fast >> k) & 1u) {
+                float hi = h, lo = 0.f, B = 0.f;  // a = 0: the double value is b
+                if (l == 0.f || de_sum(h, l, W.w1[k], W.w2[k], hi, lo, B)) bin = de_bin(hi, lo, B);
+            }
+            if (bin < 0) bin = im8_bin(de_value(h, l, W.w[k]));
+            atomicAdd(&sh[k * 256 + bin], 1);
+        }
     }
     __syncthreads();
     for (int t = threadIdx.x; t < W.k * 256; t += blockDim.x)

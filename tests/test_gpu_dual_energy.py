@@ -164,3 +164,34 @@ def test_fp32_path_is_bit_exact_on_hard_cases(mod, weights):
     got = d.cpu().numpy()
     for k in range(len(weights)):
         assert _same_bits(got[k], ref[k]), weights[k]
+
+
+def test_slice_histograms_exact_near_bin_edges(mod):
+    """The per-weight 8-bit histograms of the double values, counted exactly,
+    with values placed near the bin edges 255 v = k + 1/2 (the float
+    evaluation must leave the undecidable ones to FP64)."""
+    from newrecon_gb300 import native
+
+    rng = np.random.default_rng(11)
+    weights = [0.1, 0.3, 0.5, 0.7, 0.9, 1 / 3]
+    n = 1 << 18
+    le = rng.uniform(0.0, 0.3, n).astype(np.float32)
+    k = rng.integers(-2, 258, n)
+    off = 2.0 ** rng.uniform(-30, -17, n) * rng.choice([-1.0, 1.0], n)
+    w = np.array(weights)[rng.integers(0, len(weights), n)]
+    he = ((k + 0.5) / 255.0 + off + le.astype(np.float64) * w).astype(np.float32)
+    he[:64] = np.float32(np.nan)
+    he[64:128] = 0.0
+    le[64:96] = 0.0
+    h_d, l_d = torch.from_numpy(he).cuda(), torch.from_numpy(le).cuda()
+    wd = np.asarray(weights, np.float64)
+    d = torch.empty((len(weights), n), device="cuda")
+    hist = torch.zeros((len(weights), 256), dtype=torch.int32, device="cuda")
+    native.call("nr_de_subtract", ctypes.c_void_p(h_d.data_ptr()), ctypes.c_void_p(l_d.data_ptr()),
+                wd.ctypes.data_as(ctypes.c_void_p), len(weights), n, -1.0,
+                ctypes.c_void_p(d.data_ptr()), 0, n, ctypes.c_void_p(hist.data_ptr()), None)
+    torch.cuda.synchronize()
+    _, ref64 = de.subtract(he, le, weights)
+    got = hist.cpu().numpy()
+    for j in range(len(weights)):
+        assert np.array_equal(got[j], de.hist8(ref64[j])), weights[j]
