@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--batch", type=int, default=0,
-                    help="also time N batched reconstructions (persistent launches)")
+                    help="also time N batched reconstructions (shared launches, one CUDA graph)")
     ap.add_argument("--batch-steps", type=int, default=0,
                     help="batch steps to time (0: the whole run, every case to its last "
                          "iteration)")

@@ -231,8 +231,9 @@ nr_status nr_ostr_graph_destroy(void* graph);
  * Batched reconstructions (no reference counterpart: the reference runs one
  * case per process).  Each case has its own geometry, parameters, volume and
  * workspace (set up with nr_ostr_setup); a batch step advances every
- * unfinished case by one sub-iteration with two persistent launches over all
- * cases' work items.  Up to 64 cases.
+ * unfinished case by one sub-iteration with one projection launch and one
+ * update launch per (potential, one-view, slab depth) class over all cases'
+ * work items, one block per item.  Up to 64 cases.
  * ------------------------------------------------------------------------- */
 typedef struct nr_batch_case {
     nr_geom g;

@@ -6,10 +6,11 @@
 // Otsu threshold of he (graythresh) whose mask it applies in commented-out
 // lines.  MATLAB reads the float32 files as double, so d is
 //     float(double(he) - double(le) * w)        (two roundings in double)
-// which the kernel reproduces bit for bit with separate double multiply and
-// subtract (no contraction to an FMA).  The K outputs of one voxel are
-// written from one read of he and le; the stream is HBM bound on the K
-// writes, with the double arithmetic on the FP64 pipe beside it.
+// which the kernel reproduces bit for bit: in FP32 by error-free transforms
+// where a bound on what they drop decides the rounding (de_fast), and with
+// separate double multiply and subtract (no contraction to an FMA) where it
+// cannot -- GB300's FP64 pipe runs at about 1/64 of the FP32 rate.  The K
+// outputs of one voxel are written from one read of he and le.
 //
 // Image-statistics helpers (the 8-bit conversion of MATLAB's entropy and
 // graythresh): a value v maps to bin round(255 v) (half away from zero),

@@ -531,9 +531,10 @@ class OstrGraph:
 
 
 class Batch:
-    """Many independent reconstructions advanced together by persistent
-    batched launches (nr_batch_*): each case has its own geometry, view
-    count, potential and iteration count.
+    """Many independent reconstructions advanced together by shared batched
+    launches (nr_batch_*: one launch per kernel covers every case's work
+    items): each case has its own geometry, view count, potential and
+    iteration count.
 
     >>> b = Batch([dict(geom=g1, angles=a1, prj=y1, blank=b1, subset_num=9, iter_num=50,
     ...                 beta=50, delta=0.002, potential="hyperbola"), ...])
