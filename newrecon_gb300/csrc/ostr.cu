@@ -128,6 +128,7 @@ static nr_status check_params(const nr_geom* g, const nr_ostr_params* p) {
         return NR_ERR_BAD_ARGUMENT;
     if (p->fp_stage != NR_STAGE_OFF && p->fp_stage != NR_STAGE_TMA) return NR_ERR_BAD_ARGUMENT;
     if (g->ny > 65535 || g->nz > 65535 || g->n_angles > 65535) return NR_ERR_BAD_GEOMETRY;
+    if (!bp_tables_fit(*g)) return NR_ERR_BAD_GEOMETRY;
     return NR_OK;
 }
 

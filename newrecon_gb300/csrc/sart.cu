@@ -113,6 +113,7 @@ nr_status sart_check_params(const nr_geom* g, const nr_sart_params* p) {
         return NR_ERR_BAD_ARGUMENT;
     if (p->supersample != 0 && p->supersample != 1) return NR_ERR_BAD_ARGUMENT;
     if (g->ny > 65535 || g->nz > 65535 || g->n_angles > 65535) return NR_ERR_BAD_GEOMETRY;
+    if (!bp_tables_fit(*g)) return NR_ERR_BAD_GEOMETRY;
     return NR_OK;
 }
 

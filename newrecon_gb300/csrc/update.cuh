@@ -212,6 +212,13 @@ __device__ __forceinline__ float bp_tt(const nr_geom& g, const ViewSrc& vs, floa
     return z1 != vs.z0 ? __fdividef(-g.detectorR - vs.z0, z1 - vs.z0) : 0.f;
 }
 
+// The tables are indexed in 32 bits: true when both hold fewer than 2^31
+// entries (the device-resident paths refuse a geometry otherwise).
+__host__ inline bool bp_tables_fit(const nr_geom& g) {
+    const int64_t n = (int64_t)g.n_angles * g.nz * (g.nx > g.ny ? g.nx : g.ny);
+    return n < ((int64_t)1 << 31);
+}
+
 // Floats of zero padding after an h section (see the tables above).
 __host__ __device__ inline int64_t bp_pad(const nr_geom& g) { return (int64_t)g.nbx + 1; }
 
@@ -304,26 +311,28 @@ __device__ __forceinline__ void update_tile(
         sv[t] = view_source(g, angles[index[a0 + t]]);
     const int x0t = bx * UTX, y0t = by * UTY;
     const int zb = bz * ZC, ze = min(zb + ZC, g.nz);
-    const int64_t plane = (int64_t)g.nx * g.ny;
+    // voxel and table indices in 32 bits: volumes hold fewer than 2^31 voxels
+    // (geom_ok) and the tables fewer than 2^31 entries (bp_tables_fit)
+    const int plane = g.nx * g.ny;
     // This thread's (at most two) cells of a halo plane tile.
     constexpr int NT = UTX * UTY;
     static_assert(UPLANE <= 2 * NT, "two cells per thread");
     const int e1 = tid + NT;
     const bool has1 = e1 < UPLANE;
-    auto cell_off = [&](int k, bool& ok) -> int64_t {
+    auto cell_off = [&](int k, bool& ok) -> int {
         const int r = k / USW, c = k - r * USW;
         const int gx = x0t - 1 + c, gy = y0t - 1 + r;
         ok = gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny;
-        return ok ? (int64_t)gy * g.nx + gx : 0;
+        return ok ? gy * g.nx + gx : 0;
     };
     bool ok0, ok1 = false;
-    const int64_t off0 = cell_off(tid, ok0);
-    const int64_t off1 = has1 ? cell_off(e1, ok1) : 0;
+    const int off0 = cell_off(tid, ok0);
+    const int off1 = has1 ? cell_off(e1, ok1) : 0;
     const float qnan = __int_as_float(0x7fc00000);  // outside the volume
     auto fetch = [&](int z, float& v0, float& v1) {
         const bool zin = z >= 0 && z < g.nz;
-        v0 = (zin && ok0) ? __ldg(x + (int64_t)z * plane + off0) : qnan;
-        v1 = (zin && ok1) ? __ldg(x + (int64_t)z * plane + off1) : qnan;
+        v0 = (zin && ok0) ? __ldg(x + (z * plane + off0)) : qnan;
+        v1 = (zin && ok1) ? __ldg(x + (z * plane + off1)) : qnan;
     };
     float* pb = tile[0];
     float* pc = tile[1];
@@ -351,21 +360,21 @@ __device__ __forceinline__ void update_tile(
         __syncthreads();
         if (z + 1 < ze) fetch(z + 2, n0, n1);
         if (active) {
-            const int64_t v = (int64_t)z * plane + (int64_t)iy * g.nx + ix;
+            const int v = z * plane + iy * g.nx + ix;
             const float dv = KIND == UPD_OSTR ? __ldg(d + v) : 0.f;
             const float xc = pc[r * USW + c];
             // M * SBP(h) from the plane's tables: the taps and weights of
             // bp.cu's sbp_term on the [j][i] layout.
             float capL = 0.f, sens = 0.f;
             const float* p = h;
-            const float4* tx = T.x + ((int64_t)a0 * g.nz + z) * g.nx + ix;
-            const float4* ty = T.y + ((int64_t)a0 * g.nz + z) * g.ny + iy;
-            const int64_t sx = (int64_t)g.nz * g.nx, sy = (int64_t)g.nz * g.ny;
-            for (int t = 0; t < (NV ? NV : nv); t++, p += B, tx += sx, ty += sy) {
+            int tix = (a0 * g.nz + z) * g.nx + ix;
+            int tiy = (a0 * g.nz + z) * g.ny + iy;
+            const int sx = g.nz * g.nx, sy = g.nz * g.ny;
+            for (int t = 0; t < (NV ? NV : nv); t++, p += B, tix += sx, tiy += sy) {
                 // tap pair (c, c + 1) x rows (r, r + 1), off-detector taps
                 // weighted 0 and their loads kept in bounds by the tables
-                const float4 ex = __ldg(tx);
-                const float4 ey = __ldg(ty);
+                const float4 ex = __ldg(T.x + tix);
+                const float4 ey = __ldg(T.y + tiy);
                 const float dw = __fdividef(sv[t].s2, ex.w + ey.w);
                 const float* q0 = p + (__float_as_int(ey.x) + __float_as_int(ex.x));
                 const float* q1 = q0 + g.nbx;
