@@ -51,3 +51,23 @@ def test_pitch_and_subsets(native):
     assert status(native, dataclasses.replace(g, vy=g.vx * 1.5)) == 1
     assert status(native, g, 3) == 0
     assert status(native, g, 4) == 1
+
+
+def test_device_path_refuses_tables_past_32_bits(native):
+    """The fused update indexes its back-projection tables (views x planes x
+    columns or rows) in 32 bits: the device-resident paths refuse a geometry
+    whose tables would hold 2^31 entries or more."""
+    from newrecon_gb300.geometry import NrOstrParams, NrSartParams, config
+
+    g = config("tiny").geom
+    size = ctypes.c_size_t(0)
+    lib = native.load()
+    ok = dataclasses.replace(g, nx=4096, ny=1, nz=4096, n_angles=127, nbx=8, nby=8)
+    big = dataclasses.replace(ok, n_angles=128)               # 128 * 4096 * 4096 = 2^31
+    for geom, want in ((ok, 0), (big, 1)):
+        gc = geom.to_c()
+        p = NrOstrParams(geom.n_angles, 1, 0, 0, 1.0, 0.002)  # one view per subset
+        assert lib.nr_ostr_workspace_size(ctypes.byref(gc), ctypes.byref(p), ctypes.byref(size)) == want
+        sp = NrSartParams()
+        sp.subset_num = geom.n_angles
+        assert lib.nr_sart_workspace_size(ctypes.byref(gc), ctypes.byref(sp), ctypes.byref(size)) == want
