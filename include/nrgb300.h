@@ -317,6 +317,15 @@ nr_status nr_ostr_objective(const nr_geom* g, const nr_ostr_params* p,
 nr_status nr_ostr_check(void* workspace, size_t ws_bytes, int32_t* flags,
                         void* stream);
 
+/* The same three entry points under the names of the path's C-ABI contract
+ * (fused sub-iteration, FP64 objective, workspace size): identical arguments
+ * and behaviour. */
+nr_status nr_ostr_subset(const nr_geom* g, const nr_ostr_params* p, float* x, int32_t subset,
+                         void* workspace, size_t ws_bytes, void* stream);
+nr_status nr_objective_fp64(const nr_geom* g, const nr_ostr_params* p, const float* x,
+                            double* out, void* workspace, size_t ws_bytes, void* stream);
+nr_status nr_workspace_size(const nr_geom* g, const nr_ostr_params* p, size_t* bytes);
+
 /* The penalty of nr_ostr_objective (out[1] there) computed without any
  * workspace, into out[0] (one device double), for callers that may not
  * allocate device memory: a scanner-side reconstruction service whose memory

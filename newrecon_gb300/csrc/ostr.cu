@@ -414,3 +414,17 @@ NR_API nr_status nr_ostr_check(void* workspace, size_t ws_bytes, int32_t* flags,
 }
 
 NR_API const char* nr_version(void) { return "nrgb300 0.1.0 sm_103a"; }
+
+NR_API nr_status nr_ostr_subset(const nr_geom* g, const nr_ostr_params* p, float* x,
+                                int32_t subset, void* workspace, size_t ws_bytes, void* stream) {
+    return nr_ostr_subiter(g, p, x, subset, workspace, ws_bytes, stream);
+}
+
+NR_API nr_status nr_objective_fp64(const nr_geom* g, const nr_ostr_params* p, const float* x,
+                                   double* out, void* workspace, size_t ws_bytes, void* stream) {
+    return nr_ostr_objective(g, p, x, out, workspace, ws_bytes, stream);
+}
+
+NR_API nr_status nr_workspace_size(const nr_geom* g, const nr_ostr_params* p, size_t* bytes) {
+    return nr_ostr_workspace_size(g, p, bytes);
+}

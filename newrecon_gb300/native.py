@@ -51,6 +51,9 @@ SIGNATURES = {
     "nr_ostr_iterate": (_I32, [_GP, _PP, _P, _I32, _P, ctypes.c_size_t, _P]),
     "nr_ostr_subiter": (_I32, [_GP, _PP, _P, _I32, _P, ctypes.c_size_t, _P]),
     "nr_ostr_objective": (_I32, [_GP, _PP, _P, _P, _P, ctypes.c_size_t, _P]),
+    "nr_ostr_subset": (_I32, [_GP, _PP, _P, _I32, _P, ctypes.c_size_t, _P]),
+    "nr_objective_fp64": (_I32, [_GP, _PP, _P, _P, _P, ctypes.c_size_t, _P]),
+    "nr_workspace_size": (_I32, [_GP, _PP, ctypes.POINTER(ctypes.c_size_t)]),
     "nr_ostr_project": (_I32, [_GP, _PP, _P, _I32, _P, ctypes.c_size_t, _P]),
     "nr_ostr_update": (_I32, [_GP, _PP, _P, _P, _I32, _P, ctypes.c_size_t, _P]),
     "nr_ostr_workspace_section": (_I32, [_GP, _PP, _I32, _P, ctypes.c_size_t,

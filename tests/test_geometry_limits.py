@@ -71,3 +71,27 @@ def test_device_path_refuses_tables_past_32_bits(native):
         sp = NrSartParams()
         sp.subset_num = geom.n_angles
         assert lib.nr_sart_workspace_size(ctypes.byref(gc), ctypes.byref(sp), ctypes.byref(size)) == want
+
+
+def test_contract_names_alias_the_fused_entry_points(native):
+    """nr_workspace_size answers as nr_ostr_workspace_size (and refuses what it
+    refuses); nr_ostr_subset / nr_objective_fp64 refuse a missing workspace as
+    nr_ostr_subiter / nr_ostr_objective do, before any CUDA call."""
+    from newrecon_gb300.geometry import NrOstrParams, config
+
+    lib = native.load()
+    g = config("small").geom
+    gc = g.to_c()
+    for m in (1, 3, 9):
+        p = NrOstrParams(m, 2, 0, 0, 50.0, 0.002)
+        a, b = ctypes.c_size_t(0), ctypes.c_size_t(0)
+        assert lib.nr_workspace_size(ctypes.byref(gc), ctypes.byref(p), ctypes.byref(a)) == \
+            lib.nr_ostr_workspace_size(ctypes.byref(gc), ctypes.byref(p), ctypes.byref(b))
+        assert a.value == b.value
+        assert lib.nr_ostr_subset(ctypes.byref(gc), ctypes.byref(p), None, 0, None, 0, None) == \
+            lib.nr_ostr_subiter(ctypes.byref(gc), ctypes.byref(p), None, 0, None, 0, None) != 0
+        assert lib.nr_objective_fp64(ctypes.byref(gc), ctypes.byref(p), None, None, None, 0, None) == \
+            lib.nr_ostr_objective(ctypes.byref(gc), ctypes.byref(p), None, None, None, 0, None) != 0
+    p = NrOstrParams(4, 2, 0, 0, 50.0, 0.002)  # 9 views: 4 subsets do not divide them
+    a = ctypes.c_size_t(0)
+    assert lib.nr_workspace_size(ctypes.byref(gc), ctypes.byref(p), ctypes.byref(a)) == 1
