@@ -47,6 +47,10 @@ def parse():
     ap.add_argument("--e2e-runs", type=int, default=2)
     ap.add_argument("--cpu-subiters", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-threads", type=int, default=0,
+                    help="host threads of the CPU baseline (0: all cores)")
+    ap.add_argument("--cpu-dtype", default="f32", choices=["f32", "f64"],
+                    help="the CPU baseline's arithmetic: the FP32 restatement or the FP64 oracle")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--batch", type=int, default=0,
                     help="also time N batched reconstructions (shared launches, one CUDA graph)")
@@ -167,12 +171,13 @@ def cpu_info():
     return os.cpu_count(), model
 
 
-def cpu_port_subiters(cfg, x_true, y, b, d, n_sub: int, threads: int):
-    """FP32 CPU restatement, n_sub sub-iterations on the host cores (s per sub-iter)."""
+def cpu_port_subiters(cfg, x_true, y, b, d, n_sub: int, threads: int, dtype=np.float32):
+    """The CPU restatement (FP32, or FP64 as the oracle), n_sub sub-iterations
+    on `threads` host cores (s per sub-iter)."""
     from oracle.oracle import Oracle
 
     g = cfg.geom
-    O = Oracle(np.float32)
+    O = Oracle(dtype)
     O.set_threads(threads)
     M = cfg.subset_num
     A = g.n_angles
@@ -180,8 +185,8 @@ def cpu_port_subiters(cfg, x_true, y, b, d, n_sub: int, threads: int):
     yr = O.regroup(y, A, M)
     br = O.regroup(b, A, M)
     Vs = A // M
-    x = np.zeros(g.n_voxels, np.float32)
-    d = np.ascontiguousarray(d, np.float32)
+    x = np.zeros(g.n_voxels, dtype)
+    d = np.ascontiguousarray(d, dtype)
     times = []
     for k in range(n_sub):
         a = k % M
@@ -305,15 +310,15 @@ def run_ours(args):
         out["e2e"] = e2e_ours(args, cfg, y, b)
     if rank == 0 and not args.no_cpu_baseline:
         d = plan.section("d").cpu().numpy()
-        threads = os.cpu_count() or 1
-        times = cpu_port_subiters(cfg, x_true, y, b, d, args.cpu_subiters, threads)
+        threads = args.cpu_threads or os.cpu_count() or 1
+        dt = np.float64 if args.cpu_dtype == "f64" else np.float32
+        times = cpu_port_subiters(cfg, x_true, y, b, d, args.cpu_subiters, threads, dt)
         ncpu, model = cpu_info()
+        prec = "FP64 oracle" if dt == np.float64 else "FP32 restatement"
         out["cpu_baseline"] = {"value": len(times) / sum(times), "unit": UNIT, "cores": threads,
                                "kind": "port",
-                               "sample": f"{len(times)} sub-iterations of the clinical workload "
-                                         f"(FP32 restatement, OpenMP), {model}"}
-        out["cpu_baseline"]["sample"] = out["cpu_baseline"]["sample"].replace(
-            "clinical workload", f"{cfg.name} workload")
+                               "sample": f"{len(times)} sub-iterations of the {cfg.name} workload "
+                                         f"({prec}, OpenMP on {threads} of {ncpu} cores), {model}"}
     if not args.no_warm:
         out["warm_start"] = warm_bench(cfg, plan, rank)
     if args.batch:
