@@ -63,6 +63,9 @@ def parse():
                     help="mixed: uneven clinical-pitch cases; fullres: 2048x1024x70 breasts "
                          "at 0.085 mm, 3328x1664 detector, 15 views")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--upd-tile", type=int, default=None, choices=[0, 1],
+                    help="force the OSTR update tile (0: one voxel per thread, 1: two) "
+                         "instead of the tuner's or the default choice")
     ap.add_argument("--algo", default="ostr", choices=["ostr", "ossart", "dual-energy"],
                     help="ostr (the headline), ossart (the SART family on the same workload) "
                          "or dual-energy (syncrecon.m's subtraction on clinical-size volumes)")
@@ -221,6 +224,8 @@ def run_ours(args):
     xa = torch.zeros(g.n_voxels, device="cuda")
     xb = torch.zeros(g.n_voxels, device="cuda")
     tuned = None if args.no_tune else plan.autotune(xa)
+    if args.upd_tile is not None:
+        plan.params.upd_tile = args.upd_tile
     stream = torch.cuda.current_stream()
 
     def step(evs=None):
@@ -280,10 +285,12 @@ def run_ours(args):
     ach = kern[dom]["gbs"]
     traffic = None
     prof_traffic = os.path.join(HERE, "profiles", "dram_traffic.txt")
+    # the ncu figure of the variant that ran (the two-voxel update tile has its own)
+    tkey = dom + ("_x2" if dom == "ostr_update" and plan.params.upd_tile == 1 and Vs == 1 else "")
     if os.path.isfile(prof_traffic) and args.config == "clinical":
         for ln in open(prof_traffic):
             parts = ln.split()
-            if len(parts) >= 2 and not ln.startswith("#") and parts[0] == dom:
+            if len(parts) >= 2 and not ln.startswith("#") and parts[0] == tkey:
                 traffic = float(parts[1])
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -299,7 +306,9 @@ def run_ours(args):
         "tuned": None if tuned is None else {"fp_batch": tuned["fp_batch"],
                                              "fp_stage": tuned.get("fp_stage", 0),
                                              "upd_planes": tuned["upd_planes"],
-                                             "fp_ms": tuned.get("fp_ms")},
+                                             "upd_tile": tuned.get("upd_tile", 0),
+                                             "fp_ms": tuned.get("fp_ms"),
+                                             "update_ms": tuned.get("update_ms")},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": ach / peak,
                      "traffic": traffic, "kernels": kern},

@@ -154,6 +154,12 @@ typedef struct nr_ostr_params {
                                   4, x 16-byte aligned; fp_batch 2 or 4).  Same
                                   result either way; on the clinical workload the
                                   staged form is slower (0.255 vs 0.162 ms).     */
+    int32_t upd_tile;          /* NR_TILE_1 (default): the update gives each thread
+                                  one voxel of a 32 x 8-column tile; NR_TILE_2: two
+                                  voxels side by side in x of a 64 x 8-column tile
+                                  (one-view subsets; others use NR_TILE_1).  Same
+                                  result bit for bit; fewer instructions per voxel,
+                                  fewer resident blocks.                         */
 } nr_ostr_params;
 
 enum {
@@ -161,9 +167,15 @@ enum {
     NR_STAGE_TMA = 1
 };
 
-/* fp_batch and upd_planes select kernel variants only (every variant gives the
- * same result); the autotuner (newrecon_gb300/autotune.py) picks them per
- * geometry.  The batched path uses the defaults. */
+enum {
+    NR_TILE_1 = 0,
+    NR_TILE_2 = 1
+};
+
+/* fp_batch, fp_stage, upd_planes and upd_tile select kernel variants only
+ * (every variant gives the same result); the autotuner
+ * (newrecon_gb300/autotune.py) picks them per geometry.  The batched path
+ * uses the defaults. */
 
 /* Bytes of workspace the fused path needs for this geometry and parameters. */
 nr_status nr_ostr_workspace_size(const nr_geom* g, const nr_ostr_params* p,

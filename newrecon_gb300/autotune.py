@@ -9,7 +9,10 @@ computes the same result, bit for bit):
   volume staged slab by slab in shared memory by TMA (``fp_stage``), where
   the geometry allows it;
 * ``upd_planes`` -- z planes walked per block by the fused update (8, 16, 32):
-  deeper slabs amortise the halo planes, shallower ones give more blocks.
+  deeper slabs amortise the halo planes, shallower ones give more blocks;
+  tried with both update tiles (``upd_tile``: one voxel per thread, or two
+  side by side in x with fewer instructions per voxel but fewer resident
+  blocks) when the subsets hold one view each.
 
 The tuner times each variant on the plan's own geometry (CUDA events on the
 launching stream, best of a few repetitions over all subsets) and keeps the
@@ -30,6 +33,7 @@ FP_BATCHES = (2, 4, 8)
 # batch, TMA-staged slabs for 2 and 4
 FP_VARIANTS = ((2, 0), (4, 0), (8, 0), (2, 1), (4, 1))
 UPD_PLANES = (8, 16, 32)
+UPD_TILES = (0, 1)  # NR_TILE_1, NR_TILE_2
 
 
 def cache_path() -> str:
@@ -42,7 +46,7 @@ def signature(plan) -> str:
     p = plan.params
     dev = torch.cuda.get_device_name(plan.ws.device)
     return (f"{dev}|{g.nx}x{g.ny}x{g.nz}|{g.nbx}x{g.nby}|A{g.n_angles}|M{p.subset_num}"
-            f"|pot{p.potential}|scat{p.has_scatter}|v2")
+            f"|pot{p.potential}|scat{p.has_scatter}|v3")
 
 
 def _load() -> Dict[str, dict]:
@@ -83,7 +87,8 @@ def _time(fn, reps: int) -> float:
 
 def tune(plan, x: Optional[torch.Tensor] = None, reps: int = 3,
          use_cache: bool = True) -> Tuple[int, int, dict]:
-    """Picks (fp_batch, upd_planes) for a set-up plan and applies them."""
+    """Picks (fp_batch, upd_planes) -- with fp_stage and upd_tile -- for a set-up
+    plan and applies them."""
     key = signature(plan)
     if use_cache:
         hit = _load().get(key)
@@ -91,12 +96,14 @@ def tune(plan, x: Optional[torch.Tensor] = None, reps: int = 3,
             plan.params.fp_batch = int(hit["fp_batch"])
             plan.params.upd_planes = int(hit["upd_planes"])
             plan.params.fp_stage = int(hit.get("fp_stage", 0))
+            plan.params.upd_tile = int(hit.get("upd_tile", 0))
             return plan.params.fp_batch, plan.params.upd_planes, hit
     if x is None:
         x = torch.zeros(plan.geom.n_voxels, dtype=torch.float32, device=plan.ws.device)
     xo = torch.empty_like(x)
     M = plan.params.subset_num
     saved = (plan.params.fp_batch, plan.params.upd_planes, plan.params.fp_stage)
+    one_view = plan.geom.n_angles == M  # the two-voxel tile serves one-view subsets
     fp_ms, up_ms = {}, {}
     for k, st in FP_VARIANTS:
         plan.params.fp_batch = k
@@ -105,18 +112,21 @@ def tune(plan, x: Optional[torch.Tensor] = None, reps: int = 3,
         fp_ms[(k, st)] = _time(lambda: [plan.project(x, a) for a in range(M)], reps)
     plan.params.fp_batch, plan.params.fp_stage = saved[0], saved[2]
     plan.project(x, 0)  # h of subset 0 for the update timings
-    for z in UPD_PLANES:
-        plan.params.upd_planes = z
-        plan.update(x, xo, 0)
-        up_ms[z] = _time(lambda: [plan.update(x, xo, 0) for _ in range(M)], reps)
+    for t in (UPD_TILES if one_view else (0,)):
+        for z in UPD_PLANES:
+            plan.params.upd_tile = t
+            plan.params.upd_planes = z
+            plan.update(x, xo, 0)
+            up_ms[(t, z)] = _time(lambda: [plan.update(x, xo, 0) for _ in range(M)], reps)
     best_k, best_st = min(fp_ms, key=fp_ms.get)
-    best_z = min(up_ms, key=up_ms.get)
+    best_t, best_z = min(up_ms, key=up_ms.get)
     plan.params.fp_batch = best_k
     plan.params.fp_stage = best_st
     plan.params.upd_planes = best_z
-    rec = {"fp_batch": best_k, "fp_stage": best_st, "upd_planes": best_z,
+    plan.params.upd_tile = best_t
+    rec = {"fp_batch": best_k, "fp_stage": best_st, "upd_planes": best_z, "upd_tile": best_t,
            "fp_ms": {f"{k}{'-tma' if st else ''}": v for (k, st), v in fp_ms.items()},
-           "update_ms": {str(k): v for k, v in up_ms.items()}}
+           "update_ms": {f"{z}{'-x2' if t else ''}": v for (t, z), v in up_ms.items()}}
     if use_cache:
         _store(key, rec)
     return best_k, best_z, rec

@@ -29,7 +29,7 @@ nr_status launch_gamma_yry(const nr_geom& g, int gamma_mode, float* out, const f
                            const float* y, const float* r, cudaStream_t st);
 nr_status launch_bp(const nr_geom& g, bool ji, float* vol, const float* prj, const float* angles,
                     const int32_t* index, int a0, int nv, cudaStream_t st);
-nr_status launch_update(const nr_geom& g, int pot, int zc, const float* x, float* x_out,
+nr_status launch_update(const nr_geom& g, int pot, int zc, int tile, const float* x, float* x_out,
                         const float* d, const float* h, const float* angles, const int32_t* index,
                         const BpTab& T, int a0, int nv, float M, float beta, float delta,
                         int* status, cudaStream_t st);
@@ -127,6 +127,7 @@ static nr_status check_params(const nr_geom* g, const nr_ostr_params* p) {
     if (p->upd_planes != 0 && p->upd_planes != 8 && p->upd_planes != 16 && p->upd_planes != 32)
         return NR_ERR_BAD_ARGUMENT;
     if (p->fp_stage != NR_STAGE_OFF && p->fp_stage != NR_STAGE_TMA) return NR_ERR_BAD_ARGUMENT;
+    if (p->upd_tile != NR_TILE_1 && p->upd_tile != NR_TILE_2) return NR_ERR_BAD_ARGUMENT;
     if (g->ny > 65535 || g->nz > 65535 || g->n_angles > 65535) return NR_ERR_BAD_GEOMETRY;
     if (!bp_tables_fit(*g)) return NR_ERR_BAD_GEOMETRY;
     return NR_OK;
@@ -267,7 +268,7 @@ NR_API nr_status nr_ostr_update(const nr_geom* g, const nr_ostr_params* p, const
         return NR_ERR_BAD_ARGUMENT;
     WS w = carve(workspace, L);
     const int M = p->subset_num, Vs = g->n_angles / M;
-    return launch_update(*g, p->potential, p->upd_planes, x, x_out, w.d, w.h, w.angles, w.index, w.tab(), subset * Vs, Vs,
+    return launch_update(*g, p->potential, p->upd_planes, p->upd_tile, x, x_out, w.d, w.h, w.angles, w.index, w.tab(), subset * Vs, Vs,
                          (float)M, p->beta, p->delta, w.status, as_stream(stream));
 }
 
@@ -305,7 +306,7 @@ NR_API nr_status nr_ostr_subiter(const nr_geom* g, const nr_ostr_params* p, floa
     const int a0 = subset * Vs;
     if ((st = launch_fp_h(*g, p->fp_batch, p->fp_stage, x, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, w.status, nullptr, s)) != NR_OK)
         return st;
-    if ((st = launch_update(*g, p->potential, p->upd_planes, x, w.xtmp, w.d, w.h, w.angles, w.index, w.tab(), a0, Vs,
+    if ((st = launch_update(*g, p->potential, p->upd_planes, p->upd_tile, x, w.xtmp, w.d, w.h, w.angles, w.index, w.tab(), a0, Vs,
                             (float)M, p->beta, p->delta, w.status, s)) != NR_OK)
         return st;
     if (cudaMemcpyAsync(x, w.xtmp, N * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
@@ -332,7 +333,7 @@ static nr_status enqueue_iterations(const nr_geom* g, const nr_ostr_params* p, f
                                   staged ? &maps[cur == x ? 0 : 1] : nullptr, s)) !=
                 NR_OK)
                 return st;
-            if ((st = launch_update(*g, p->potential, p->upd_planes, cur, nxt, w.d, w.h, w.angles, w.index, w.tab(), a0, Vs,
+            if ((st = launch_update(*g, p->potential, p->upd_planes, p->upd_tile, cur, nxt, w.d, w.h, w.angles, w.index, w.tab(), a0, Vs,
                                     (float)M, p->beta, p->delta, w.status, s)) != NR_OK)
                 return st;
             float* t = cur;

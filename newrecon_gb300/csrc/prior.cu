@@ -176,14 +176,18 @@ nr_status launch_bp_tables(const nr_geom& g, const float* angles, const int32_t*
 }
 
 template <int POT, int ZC>
-static nr_status launch_update_t(const nr_geom& g, const float* x, float* x_out, const float* d,
+static nr_status launch_update_t(const nr_geom& g, int tile, const float* x, float* x_out, const float* d,
                                  const float* h, const float* angles, const int32_t* index,
                                  const BpTab& T, int a0, int nv, float M, float beta,
                                  float delta, int* status, cudaStream_t st) {
     dim3 blk(UTX, UTY), grd(cdiv(g.nx, UTX), cdiv(g.ny, UTY), cdiv(g.nz, ZC));
     const Geo G = make_geo(g);
     const PriorW5 W = make_w5(g.vz / g.vx, delta);
-    if (nv == 1)
+    if (nv == 1 && tile == NR_TILE_2) {
+        dim3 g2(cdiv(g.nx, U2X), cdiv(g.ny, UTY), cdiv(g.nz, ZC));
+        update_x2_kernel<POT, ZC, 1><<<g2, blk, 0, st>>>(G, W, x, x_out, d, h, angles, index, T, a0,
+                                                       nv, M, beta, delta, status);
+    } else if (nv == 1)
         update_kernel<POT, ZC, 1><<<grd, blk, 0, st>>>(G, W, x, x_out, d, h, angles, index, T, a0,
                                                        nv, M, beta, delta, status);
     else
@@ -193,40 +197,40 @@ static nr_status launch_update_t(const nr_geom& g, const float* x, float* x_out,
 }
 
 template <int POT>
-static nr_status launch_update_z(const nr_geom& g, int zc, const float* x, float* x_out,
+static nr_status launch_update_z(const nr_geom& g, int zc, int tile, const float* x, float* x_out,
                                  const float* d, const float* h, const float* angles,
                                  const int32_t* index, const BpTab& T, int a0, int nv, float M,
                                  float beta, float delta, int* status, cudaStream_t st) {
     switch (zc) {
     case 8:
-        return launch_update_t<POT, 8>(g, x, x_out, d, h, angles, index, T, a0, nv, M, beta, delta,
+        return launch_update_t<POT, 8>(g, tile, x, x_out, d, h, angles, index, T, a0, nv, M, beta, delta,
                                        status, st);
     case 32:
-        return launch_update_t<POT, 32>(g, x, x_out, d, h, angles, index, T, a0, nv, M, beta, delta,
+        return launch_update_t<POT, 32>(g, tile, x, x_out, d, h, angles, index, T, a0, nv, M, beta, delta,
                                         status, st);
     default:
-        return launch_update_t<POT, 16>(g, x, x_out, d, h, angles, index, T, a0, nv, M, beta, delta,
+        return launch_update_t<POT, 16>(g, tile, x, x_out, d, h, angles, index, T, a0, nv, M, beta, delta,
                                         status, st);
     }
 }
 
-nr_status launch_update(const nr_geom& g, int pot, int zc, const float* x, float* x_out,
+nr_status launch_update(const nr_geom& g, int pot, int zc, int tile, const float* x, float* x_out,
                         const float* d, const float* h, const float* angles, const int32_t* index,
                         const BpTab& T, int a0, int nv, float M, float beta, float delta,
                         int* status, cudaStream_t st) {
     if (nv > UPD_VIEWS_SMEM) return NR_ERR_BAD_ARGUMENT;
     switch (pot) {
     case NR_POT_Q2:
-        return launch_update_z<NR_POT_Q2>(g, zc, x, x_out, d, h, angles, index, T, a0, nv, M, beta,
+        return launch_update_z<NR_POT_Q2>(g, zc, tile, x, x_out, d, h, angles, index, T, a0, nv, M, beta,
                                           delta, status, st);
     case NR_POT_LANGE:
-        return launch_update_z<NR_POT_LANGE>(g, zc, x, x_out, d, h, angles, index, T, a0, nv, M, beta,
+        return launch_update_z<NR_POT_LANGE>(g, zc, tile, x, x_out, d, h, angles, index, T, a0, nv, M, beta,
                                              delta, status, st);
     case NR_POT_HYPERBOLA:
-        return launch_update_z<NR_POT_HYPERBOLA>(g, zc, x, x_out, d, h, angles, index, T, a0, nv, M,
+        return launch_update_z<NR_POT_HYPERBOLA>(g, zc, tile, x, x_out, d, h, angles, index, T, a0, nv, M,
                                                  beta, delta, status, st);
     case NR_POT_HUBER:
-        return launch_update_z<NR_POT_HUBER>(g, zc, x, x_out, d, h, angles, index, T, a0, nv, M, beta,
+        return launch_update_z<NR_POT_HUBER>(g, zc, tile, x, x_out, d, h, angles, index, T, a0, nv, M, beta,
                                              delta, status, st);
     default: return NR_ERR_BAD_ARGUMENT;
     }

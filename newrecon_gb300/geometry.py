@@ -44,7 +44,7 @@ class NrOstrParams(ctypes.Structure):
         ("gamma_mode", ctypes.c_int32), ("has_scatter", ctypes.c_int32),
         ("beta", ctypes.c_float), ("delta", ctypes.c_float),
         ("fp_batch", ctypes.c_int32), ("upd_planes", ctypes.c_int32),
-        ("fp_stage", ctypes.c_int32),
+        ("fp_stage", ctypes.c_int32), ("upd_tile", ctypes.c_int32),
     ]
 
 

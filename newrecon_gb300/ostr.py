@@ -366,16 +366,21 @@ class OSTR:
 
     def __init__(self, geom: Geometry, *, subset_num: int, beta: float, delta: float,
                  potential: str = "lange", gamma_mode: str = "length", has_scatter: bool = False,
-                 stage: bool = False):
+                 stage: bool = False, upd_tile: int = 0):
         """stage=True stages the projection's volume slab by slab in shared
         memory by TMA instead of gathering it through L1/L2 (same result;
-        slower on the clinical workload)."""
+        slower on the clinical workload).  upd_tile=1 gives each thread of the
+        update two voxels side by side in x (one-view subsets; same result bit
+        for bit).  autotune() picks both per geometry."""
+        if upd_tile not in (0, 1):
+            raise ValueError("upd_tile must be 0 (one voxel per thread) or 1 (two)")
         geom.validate(subset_num)
         self.geom = geom
         self.params = NrOstrParams(int(subset_num), int(POTENTIALS[potential]),
                                    int(GAMMA_MODES[gamma_mode]), int(bool(has_scatter)),
                                    float(beta), float(delta if potential != "q2" else 1.0))
         self.params.fp_stage = 1 if stage else 0
+        self.params.upd_tile = int(upd_tile)
         self.gc = geom.to_c()
         self.history = None      # objectives of a monotone iterate()
         self.rejected_at = None  # the iteration a monotone iterate() undid

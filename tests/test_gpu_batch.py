@@ -171,11 +171,13 @@ def test_autotune_variants_agree_and_cache(mod, tmp_path, monkeypatch):
     outs = []
     for k, st in autotune.FP_VARIANTS:
         for zc in autotune.UPD_PLANES:
-            plan.params.fp_batch, plan.params.fp_stage, plan.params.upd_planes = k, st, zc
-            xo = torch.empty_like(x)
-            plan.project(x, 3)
-            plan.update(x, xo, 3)
-            outs.append(xo)
+            for t in autotune.UPD_TILES:
+                plan.params.fp_batch, plan.params.fp_stage = k, st
+                plan.params.upd_planes, plan.params.upd_tile = zc, t
+                xo = torch.empty_like(x)
+                plan.project(x, 3)
+                plan.update(x, xo, 3)
+                outs.append(xo)
     torch.cuda.synchronize()
     for o in outs[1:]:
         assert torch.equal(o, outs[0])
@@ -188,3 +190,5 @@ def test_autotune_variants_agree_and_cache(mod, tmp_path, monkeypatch):
     rec2 = plan.autotune(x)  # served from the cache
     assert (plan.params.fp_batch, plan.params.upd_planes) == (rec["fp_batch"], rec["upd_planes"])
     assert plan.params.fp_stage == rec["fp_stage"]
+    assert plan.params.upd_tile == rec["upd_tile"] in autotune.UPD_TILES
+    assert len(rec["update_ms"]) == len(autotune.UPD_PLANES) * len(autotune.UPD_TILES)

@@ -1,0 +1,106 @@
+"""The two-voxel update tile (upd_tile = 1) against the one-voxel tile.
+
+Each voxel's sums are formed in the same order and grouping by both tiles, so
+the bar is bit-identical volumes after whole OSTR iterations, for every
+potential, on shapes that leave partly filled 64-column tiles, odd column
+counts (a thread whose second voxel is outside the volume), a single column,
+and slab chunks cut short in z.  The oracle parity of the one-voxel tile is
+covered by test_gpu_recon.py.
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(203, 77, 13), (65, 9, 5), (1, 1, 3), (2, 3, 4), (64, 8, 16), (130, 17, 33),
+          (127, 40, 7)]
+
+
+@pytest.fixture(scope="module")
+def mod():
+    from newrecon_gb300 import native, ostr
+
+    native.load()
+    return ostr
+
+
+def scan(mod, g, angles, seed, I0=1e4):
+    from newrecon_gb300.phantom import poisson_counts
+
+    rng = np.random.default_rng(seed)
+    x = (rng.random(g.n_voxels, dtype=np.float32) * 0.05).astype(np.float32)
+    mod.set_geometry(g)
+    idx = np.arange(g.n_angles, dtype=np.int32)
+    line = torch.zeros(g.n_angles * g.n_bins, device="cuda")
+    mod.fprojectCB_1R_GPU_OSTR_cos(torch.from_numpy(x).cuda(), line,
+                                   torch.from_numpy(angles).cuda(),
+                                   torch.from_numpy(idx).cuda(), 0, g.n_angles)
+    y = poisson_counts(line.cpu().numpy(), I0, seed)
+    return torch.from_numpy(y).cuda(), torch.full((y.size,), I0, device="cuda")
+
+
+def run(mod, g, angles, y, b, iters, pot, beta, delta, tile, planes=0):
+    plan = mod.OSTR(g, subset_num=g.n_angles, beta=beta, delta=delta, potential=pot,
+                    upd_tile=tile)
+    plan.params.upd_planes = planes
+    plan.setup(angles, y, b)
+    x = torch.zeros(g.n_voxels, dtype=torch.float32, device="cuda")
+    plan.iterate(x, iters)
+    assert plan.check() == 0
+    return x
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+def test_two_voxel_tile_is_bit_identical(mod, shape):
+    from newrecon_gb300.geometry import Geometry, view_angles
+
+    nx, ny, nz = shape
+    g = Geometry.dbt(nx, ny, nz, 0.5, 1.0, max(8, nx + 10), max(8, ny + 6), 0.5, 6)
+    angles = view_angles(6, 15.0)
+    y, b = scan(mod, g, angles, nx * 7 + ny)
+    for pot in ("q2", "lange", "hyperbola", "huber"):
+        for planes in (8, 16, 32):
+            a = run(mod, g, angles, y, b, 2, pot, 20.0, 0.01, 0, planes)
+            c = run(mod, g, angles, y, b, 2, pot, 20.0, 0.01, 1, planes)
+            assert torch.isfinite(a).all()
+            assert torch.equal(a, c), (shape, pot, planes, float((a - c).abs().max()))
+
+
+def test_two_voxel_tile_clinical(mod):
+    """One iteration (25 sub-iterations) of the clinical workload, both tiles."""
+    from newrecon_gb300.geometry import config
+    from newrecon_gb300.phantom import breast_phantom, poisson_counts
+
+    cfg = config("clinical")
+    g = cfg.geom
+    x = breast_phantom(g, 1, cfg.n_glandular, cfg.n_calc, thickness_mm=cfg.thickness_mm)
+    mod.set_geometry(g)
+    idx = np.arange(g.n_angles, dtype=np.int32)
+    line = torch.zeros(g.n_angles * g.n_bins, device="cuda")
+    mod.fprojectCB_1R_GPU_OSTR_cos(torch.from_numpy(x.ravel()).cuda(), line,
+                                   torch.from_numpy(cfg.angles).cuda(),
+                                   torch.from_numpy(idx).cuda(), 0, g.n_angles)
+    y = torch.from_numpy(poisson_counts(line.cpu().numpy(), cfg.I0, 1)).cuda()
+    b = torch.full_like(y, cfg.I0)
+    a = run(mod, g, cfg.angles, y, b, 1, cfg.potential, cfg.beta, cfg.delta, 0)
+    c = run(mod, g, cfg.angles, y, b, 1, cfg.potential, cfg.beta, cfg.delta, 1)
+    assert torch.equal(a, c)
+    assert float(a.abs().max()) > 0
+
+
+def test_two_voxel_tile_falls_back_for_many_view_subsets(mod):
+    """With several views per subset the plan runs the one-voxel tile."""
+    from newrecon_gb300.geometry import Geometry, view_angles
+
+    g = Geometry.dbt(70, 20, 9, 0.5, 1.0, 80, 26, 0.5, 6)
+    angles = view_angles(6, 15.0)
+    y, b = scan(mod, g, angles, 5)
+    out = []
+    for tile in (0, 1):
+        plan = mod.OSTR(g, subset_num=3, beta=20.0, delta=0.01, potential="huber", upd_tile=tile)
+        plan.setup(angles, y, b)
+        x = torch.zeros(g.n_voxels, dtype=torch.float32, device="cuda")
+        plan.iterate(x, 2)
+        out.append(x)
+    assert torch.equal(out[0], out[1])
