@@ -631,12 +631,13 @@ __global__ void __launch_bounds__(256, NV == 1 ? 8 : 0) update_kernel(
                                        delta, status, blockIdx.x, blockIdx.y, blockIdx.z, sm);
 }
 
-// The same update on x2 tiles (64 x 8 columns per block).  Six resident
-// blocks per SM (40 registers, no spills): held to eight (32 registers) it
-// spills 20 bytes and runs slower (0.275 against 0.270 ms on the clinical
-// workload).
+// The same update on x2 tiles (64 x 8 columns per block), five resident
+// blocks per SM (48 registers, no spills).  Measured per 25 updates at 16
+// planes, clinical / full resolution: 5 blocks 6.54 / 17.42 ms, 6 blocks (40
+// registers) 6.71 / 17.46 ms, 4 blocks (64 registers) 6.82 / 18.51 ms; held
+// to 8 blocks (32 registers) it spills 20 bytes (0.275 ms per update).
 template <int POT, int ZC, int NV>
-__global__ void __launch_bounds__(256, NV == 1 ? 6 : 0) update_x2_kernel(
+__global__ void __launch_bounds__(256, NV == 1 ? 5 : 0) update_x2_kernel(
     const __grid_constant__ Geo G, const __grid_constant__ PriorW5 W,
     const float* __restrict__ x, float* __restrict__ x_out, const float* __restrict__ d,
     const float* __restrict__ h, const float* __restrict__ angles,
