@@ -568,7 +568,8 @@ def e2e_ours(args, cfg, y, b):
             "h2d_bytes_per_step": int(y.nbytes + b.nbytes + cfg.angles.nbytes),
             "d2h_bytes_per_step": int(g.n_voxels * 4),
             "step": f"ostr.reconstruct from pinned host buffers: upload, gamma/d setup, "
-                    f"{iters} iterations x {cfg.subset_num} subsets, volume download",
+                    f"{iters} iterations x {cfg.subset_num} subsets (the kernel variants "
+                    f"the tuner cached for this geometry, if any), volume download",
             "seconds_per_call": float(np.mean(ts))}
 
 

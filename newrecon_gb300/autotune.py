@@ -85,18 +85,28 @@ def _time(fn, reps: int) -> float:
     return best
 
 
+def apply_cached(plan) -> Optional[dict]:
+    """Applies the cached choice for the plan's GPU, geometry and parameters;
+    None (and the plan unchanged) when the cache holds none."""
+    hit = _load().get(signature(plan))
+    if not (hit and hit.get("fp_batch") in FP_BATCHES and hit.get("upd_planes") in UPD_PLANES
+            and hit.get("fp_stage", 0) in (0, 1) and hit.get("upd_tile", 0) in UPD_TILES):
+        return None
+    plan.params.fp_batch = int(hit["fp_batch"])
+    plan.params.upd_planes = int(hit["upd_planes"])
+    plan.params.fp_stage = int(hit.get("fp_stage", 0))
+    plan.params.upd_tile = int(hit.get("upd_tile", 0))
+    return hit
+
+
 def tune(plan, x: Optional[torch.Tensor] = None, reps: int = 3,
          use_cache: bool = True) -> Tuple[int, int, dict]:
     """Picks (fp_batch, upd_planes) -- with fp_stage and upd_tile -- for a set-up
     plan and applies them."""
     key = signature(plan)
     if use_cache:
-        hit = _load().get(key)
-        if hit and hit.get("fp_batch") in FP_BATCHES and hit.get("upd_planes") in UPD_PLANES:
-            plan.params.fp_batch = int(hit["fp_batch"])
-            plan.params.upd_planes = int(hit["upd_planes"])
-            plan.params.fp_stage = int(hit.get("fp_stage", 0))
-            plan.params.upd_tile = int(hit.get("upd_tile", 0))
+        hit = apply_cached(plan)
+        if hit is not None:
             return plan.params.fp_batch, plan.params.upd_planes, hit
     if x is None:
         x = torch.zeros(plan.geom.n_voxels, dtype=torch.float32, device=plan.ws.device)

@@ -637,17 +637,30 @@ class BatchGraph:
 
 def reconstruct(geom: Geometry, prj, blank, scatter=None, *, angles, subset_num: int,
                 iter_num: int, beta: float, delta: float, potential: str = "lange",
-                gamma_mode: str = "length", x0=None, monotone: bool = False):
+                gamma_mode: str = "length", x0=None, monotone: bool = False,
+                tune="cached"):
     """OSTR reconstruction: transmission counts in, attenuation (1/mm) out.
 
     prj, blank, scatter: [view][i][j] in original view order (the layout
     load_prj produces).  Returns the volume [z][y][x]; numpy when prj was a
     host array, else a CUDA tensor.  monotone=True stops before the first
-    iteration that would raise the FP64 objective (OSTR.iterate).
+    iteration that would raise the FP64 objective (OSTR.iterate).  tune:
+    "cached" runs the kernel variants the autotuner cached for this GPU and
+    geometry (the defaults when it has none), True tunes first when the
+    cache has none, False runs the defaults.  Every variant gives the same
+    result bit for bit.
     """
+    if not (tune == "cached" or tune is True or tune is False):
+        raise ValueError('tune must be "cached", True or False')
     plan = OSTR(geom, subset_num=subset_num, beta=beta, delta=delta, potential=potential,
                 gamma_mode=gamma_mode, has_scatter=scatter is not None)
     plan.setup(angles, prj, blank, scatter)
+    if tune is True:
+        plan.autotune()
+    elif tune == "cached":
+        from . import autotune
+
+        autotune.apply_cached(plan)
     if x0 is None:
         x = torch.zeros(geom.n_voxels, dtype=torch.float32, device=plan.ws.device)
     else:

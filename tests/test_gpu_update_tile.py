@@ -104,3 +104,34 @@ def test_two_voxel_tile_falls_back_for_many_view_subsets(mod):
         plan.iterate(x, 2)
         out.append(x)
     assert torch.equal(out[0], out[1])
+
+
+def test_reconstruct_applies_the_cached_choice(mod, tmp_path, monkeypatch):
+    """reconstruct(tune="cached") runs the autotuner's cached variants for the
+    geometry; the result is the defaults' result bit for bit."""
+    import json
+
+    from newrecon_gb300 import autotune
+    from newrecon_gb300.geometry import Geometry, view_angles
+
+    cache = tmp_path / "tune.json"
+    monkeypatch.setenv("NR_TUNE_CACHE", str(cache))
+    g = Geometry.dbt(130, 17, 33, 0.5, 1.0, 140, 23, 0.5, 6)
+    angles = view_angles(6, 15.0)
+    y, b = scan(mod, g, angles, 11)
+    kw = dict(angles=angles, subset_num=6, iter_num=2, beta=20.0, delta=0.01, potential="huber")
+    plain = mod.reconstruct(g, y, b, tune=False, **kw)
+    plan = mod.OSTR(g, subset_num=6, beta=20.0, delta=0.01, potential="huber")
+    assert autotune.apply_cached(plan) is None            # nothing cached yet
+    tuned = mod.reconstruct(g, y, b, tune=True, **kw)     # tunes and caches
+    rec = autotune.apply_cached(plan)
+    assert rec is not None
+    assert (plan.params.upd_tile, plan.params.upd_planes) == (rec["upd_tile"], rec["upd_planes"])
+    cached = mod.reconstruct(g, y, b, **kw)
+    assert torch.equal(plain, tuned) and torch.equal(plain, cached)
+    # a cached entry that names no variant is ignored
+    cache.write_text(json.dumps({autotune.signature(plan): {"fp_batch": 3, "upd_planes": 16}}))
+    assert autotune.apply_cached(mod.OSTR(g, subset_num=6, beta=20.0, delta=0.01,
+                                          potential="huber")) is None
+    with pytest.raises(ValueError):
+        mod.reconstruct(g, y, b, tune="always", **kw)
