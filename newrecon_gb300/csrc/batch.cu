@@ -2,7 +2,7 @@
 //
 // A batch step advances every unfinished case by one sub-iteration: one
 // launch of the fused forward projection + gradient of all cases, then one
-// update launch per (potential, one view per subset) class.  Each launch
+// update launch per (potential, update form, slab depth) class.  Each launch
 // walks one flat list of work items -- (case, detector tile, view) or (case,
 // volume tile, z chunk) -- built from per-case prefix offsets, so cases of
 // different sizes, view counts and potentials share the GPU in the same launch
@@ -25,10 +25,11 @@
 // 64 cases: ~19 KB, inside the 32 KB parameter limit).  The item decode then
 // runs on block-uniform constant-bank values and the tile reads its case's
 // geometry from the constant bank as the single-case kernels do, instead of
-// from a shared-memory copy that costs registers: the one-view update fits
-// 32 registers (8 resident blocks per SM) without spills.
+// from a shared-memory copy that costs registers: the one-voxel one-view
+// update fits 32 registers (8 resident blocks per SM; 8 bytes spill).
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 
 #include "project.cuh"
 #include "update.cuh"
@@ -37,7 +38,10 @@ namespace nr {
 
 constexpr int BATCH_MAX = 64;
 constexpr int N_ZC = 3;                      // update slab depths 8, 16, 32 planes
-constexpr int N_CLASSES = 4 * 2 * N_ZC;      // potential x one-view x slab depth
+// update forms: several views per subset; one view, one voxel per thread;
+// one view, two voxels per thread (the case's upd_tile)
+constexpr int N_FORM = 3;
+constexpr int N_CLASSES = 4 * N_FORM * N_ZC; // potential x form x slab depth
 
 struct CaseDev {
     Geo G;
@@ -52,20 +56,24 @@ struct CaseDev {
     int* status;
     BpTab T;               // the case's back-projection tables
     int fp_tx, fp_ty;      // detector tiles of 32 x 4 bins
-    int up_tx, up_ty;      // volume tiles of 32 x 8 columns
+    int up_tx, up_ty;      // volume tiles of 32 x 8 columns (64 x 8 in form 2)
+    int form;              // update form (N_FORM)
     int zc;                // z planes per update item (the plan's upd_planes)
     int64_t N;
 };
 
 __host__ __device__ constexpr int zc_index(int zc) { return zc == 8 ? 0 : (zc == 32 ? 2 : 1); }
-__host__ __device__ constexpr int upd_class(int pot, bool one_view, int zc) {
-    return (2 * pot + one_view) * N_ZC + zc_index(zc);
+__host__ __device__ constexpr int upd_form(bool one_view, int tile) {
+    return one_view ? (tile == NR_TILE_2 ? 2 : 1) : 0;
+}
+__host__ __device__ constexpr int upd_class(int pot, int form, int zc) {
+    return (N_FORM * pot + form) * N_ZC + zc_index(zc);
 }
 
 struct BatchTable {
     int n;
-    // cases c[] are in class order (potential, one view per subset, slab
-    // depth), and by sub-iteration count, longest first, within a class
+    // cases c[] are in class order (potential, update form, slab depth), and
+    // by sub-iteration count, longest first, within a class
     int cls_first[N_CLASSES], cls_end[N_CLASSES];  // cases [first, end) of each class
     int up_off[BATCH_MAX + 1];                     // update items: prefix over c[]
     int fp_case[BATCH_MAX];                        // projection order (longest first)
@@ -101,15 +109,17 @@ __global__ void __launch_bounds__(128, 12) fp_batch_kernel(const __grid_constant
     }
 }
 
-// Update items [lo, hi) of one (potential, NV, ZC) class.  NV = 1 serves the
-// cases whose subsets hold one view (the compile-time view count of
+// Update items [lo, hi) of one (potential, NV, ZC, X2) class.  NV = 1 serves
+// the cases whose subsets hold one view (the compile-time view count of
 // update_tile: 32 registers, 8 resident blocks per SM); NV = 0 the others
-// (no block minimum, as update_kernel: 40 registers).  ZC
-// is the case's slab depth (planes per item), as the autotuner picked it.
-template <int POT, int NV, int ZC>
-__global__ void __launch_bounds__(256, NV ? 8 : 0) update_batch_kernel(
+// (no block minimum, as update_kernel: 40 registers).  X2: the one-view
+// cases that take two voxels per thread (update_tile_x2, 5 blocks per SM as
+// update_x2_kernel).  ZC is the case's slab depth (planes per item), as the
+// autotuner picked it.
+template <int POT, int NV, int ZC, bool X2>
+__global__ void __launch_bounds__(256, NV ? (X2 ? 5 : 8) : 0) update_batch_kernel(
     const __grid_constant__ BatchTable P, int step, int lo, int hi) {
-    __shared__ UpdSmem sm;
+    __shared__ typename std::conditional<X2, UpdSmem2, UpdSmem>::type sm;
     for (int it = lo + blockIdx.x; it < hi; it += gridDim.x) {
         const int c = find_case(P.up_off, P.n, it);
         const CaseDev& cd = P.c[c];
@@ -129,9 +139,14 @@ __global__ void __launch_bounds__(256, NV ? 8 : 0) update_batch_kernel(
         const Geo G = cd.G;
         const PriorW5 W = cd.W;
         const BpTab T = cd.T;
-        update_tile<POT, ZC, UPD_OSTR, NV>(G, W, cur, nxt, cd.d, cd.h, cd.angles, cd.index, T, a0,
-                                            cd.Vs, cd.M, cd.beta, cd.delta, cd.status, bx, by, bz,
-                                            sm);
+        if constexpr (X2)
+            update_tile_x2<POT, ZC, UPD_OSTR, NV>(G, W, cur, nxt, cd.d, cd.h, cd.angles, cd.index,
+                                                  T, a0, cd.Vs, cd.M, cd.beta, cd.delta,
+                                                  cd.status, bx, by, bz, sm);
+        else
+            update_tile<POT, ZC, UPD_OSTR, NV>(G, W, cur, nxt, cd.d, cd.h, cd.angles, cd.index, T,
+                                                a0, cd.Vs, cd.M, cd.beta, cd.delta, cd.status, bx,
+                                                by, bz, sm);
     }
 }
 
@@ -195,14 +210,16 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
         if (k.n_iters < 0 || !k.x || k.p.subset_num < 1 || k.p.potential < NR_POT_Q2 ||
             k.p.potential > NR_POT_HUBER ||
             (k.p.upd_planes != 0 && k.p.upd_planes != 8 && k.p.upd_planes != 16 &&
-             k.p.upd_planes != 32))
+             k.p.upd_planes != 32) ||
+            (k.p.upd_tile != NR_TILE_1 && k.p.upd_tile != NR_TILE_2))
             return NR_ERR_BAD_ARGUMENT;
     }
     auto total_sub = [&](int c) { return cases[c].n_iters * cases[c].p.subset_num; };
     auto zc_of = [&](int c) { return cases[c].p.upd_planes == 0 ? UZC : cases[c].p.upd_planes; };
     auto cls_of = [&](int c) {
         const nr_batch_case& k = cases[c];
-        return upd_class(k.p.potential, k.g.n_angles == k.p.subset_num, zc_of(c));
+        return upd_class(k.p.potential, upd_form(k.g.n_angles == k.p.subset_num, k.p.upd_tile),
+                         zc_of(c));
     };
     // case order: by class, then by sub-iteration count, longest first (stable)
     int order[BATCH_MAX];
@@ -242,7 +259,8 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
         d.x = k.x;
         d.fp_tx = (int)cdiv(g.nbx, 32);
         d.fp_ty = (int)cdiv(g.nby, 4);
-        d.up_tx = (int)cdiv(g.nx, UTX);
+        d.form = upd_form(d.Vs == 1, k.p.upd_tile);
+        d.up_tx = (int)cdiv(g.nx, d.form == 2 ? U2X : UTX);
         d.up_ty = (int)cdiv(g.ny, UTY);
         d.zc = zc_of(order[c]);
         d.N = (int64_t)g.nx * g.ny * g.nz;
@@ -256,7 +274,7 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
     }
     for (int k = 0; k < N_CLASSES; k++) P->cls_first[k] = P->cls_end[k] = 0;
     for (int c = n_cases - 1; c >= 0; c--) {
-        const int k = upd_class(P->c[c].pot, P->c[c].Vs == 1, P->c[c].zc);
+        const int k = upd_class(P->c[c].pot, P->c[c].form, P->c[c].zc);
         if (P->cls_end[k] == 0) P->cls_end[k] = c + 1;
         P->cls_first[k] = c;
     }
@@ -289,33 +307,33 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
 
 namespace {
 
-template <int POT, int NV, int ZC>
+template <int POT, int NV, int ZC, bool X2>
 void launch_class_t(const BatchTable& P, int32_t k, int lo, int hi, cudaStream_t s) {
-    update_batch_kernel<POT, NV, ZC><<<hi - lo, dim3(UTX, UTY), 0, s>>>(P, k, lo, hi);
+    update_batch_kernel<POT, NV, ZC, X2><<<hi - lo, dim3(UTX, UTY), 0, s>>>(P, k, lo, hi);
 }
 
-template <int POT, int NV>
+template <int POT, int NV, bool X2>
 void launch_class_z(int zi, const BatchTable& P, int32_t k, int lo, int hi, cudaStream_t s) {
-    if (zi == 0) return launch_class_t<POT, NV, 8>(P, k, lo, hi, s);
-    if (zi == 2) return launch_class_t<POT, NV, 32>(P, k, lo, hi, s);
-    return launch_class_t<POT, NV, 16>(P, k, lo, hi, s);
+    if (zi == 0) return launch_class_t<POT, NV, 8, X2>(P, k, lo, hi, s);
+    if (zi == 2) return launch_class_t<POT, NV, 32, X2>(P, k, lo, hi, s);
+    return launch_class_t<POT, NV, 16, X2>(P, k, lo, hi, s);
 }
 
 template <int POT>
-void launch_class_nv(bool one, int zi, const BatchTable& P, int32_t k, int lo, int hi,
-                     cudaStream_t s) {
-    if (one) return launch_class_z<POT, 1>(zi, P, k, lo, hi, s);
-    return launch_class_z<POT, 0>(zi, P, k, lo, hi, s);
+void launch_class_form(int form, int zi, const BatchTable& P, int32_t k, int lo, int hi,
+                       cudaStream_t s) {
+    if (form == 2) return launch_class_z<POT, 1, true>(zi, P, k, lo, hi, s);
+    if (form == 1) return launch_class_z<POT, 1, false>(zi, P, k, lo, hi, s);
+    return launch_class_z<POT, 0, false>(zi, P, k, lo, hi, s);
 }
 
 void launch_class(int cls, const BatchTable& P, int32_t k, int lo, int hi, cudaStream_t s) {
-    const int zi = cls % N_ZC, pot = cls / (2 * N_ZC);
-    const bool one = (cls / N_ZC) % 2 == 1;
+    const int zi = cls % N_ZC, form = (cls / N_ZC) % N_FORM, pot = cls / (N_FORM * N_ZC);
     switch (pot) {
-    case NR_POT_Q2: return launch_class_nv<NR_POT_Q2>(one, zi, P, k, lo, hi, s);
-    case NR_POT_LANGE: return launch_class_nv<NR_POT_LANGE>(one, zi, P, k, lo, hi, s);
-    case NR_POT_HYPERBOLA: return launch_class_nv<NR_POT_HYPERBOLA>(one, zi, P, k, lo, hi, s);
-    default: return launch_class_nv<NR_POT_HUBER>(one, zi, P, k, lo, hi, s);
+    case NR_POT_Q2: return launch_class_form<NR_POT_Q2>(form, zi, P, k, lo, hi, s);
+    case NR_POT_LANGE: return launch_class_form<NR_POT_LANGE>(form, zi, P, k, lo, hi, s);
+    case NR_POT_HYPERBOLA: return launch_class_form<NR_POT_HYPERBOLA>(form, zi, P, k, lo, hi, s);
+    default: return launch_class_form<NR_POT_HUBER>(form, zi, P, k, lo, hi, s);
     }
 }
 

@@ -547,7 +547,7 @@ class Batch:
 
     tune=True runs the autotuner on each case's plan first (cached per
     geometry): the batched update then walks each case with its tuned slab
-    depth.  The batched projection always uses 4-step gathers.
+    depth and tile.  The batched projection always uses 4-step gathers.
     """
 
     def __init__(self, cases, tune: bool = False):
@@ -568,6 +568,8 @@ class Batch:
                 plan.autotune(x)
             if "upd_planes" in c:  # an explicit slab depth (8, 16 or 32) wins
                 plan.params.upd_planes = int(c["upd_planes"])
+            if "upd_tile" in c:    # and an explicit update tile (0 or 1)
+                plan.params.upd_tile = int(c["upd_tile"])
             self.plans.append(plan)
             self.x.append(x)
             arr[k] = NrBatchCase(plan.gc, plan.params, int(c["iter_num"]),

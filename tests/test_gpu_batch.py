@@ -118,6 +118,23 @@ def test_batch_slab_depths_match_single(mod):
         assert close(xb, single(mod, c)), (c["potential"], c["upd_planes"])
 
 
+def test_batch_two_voxel_tile_is_bit_identical(mod):
+    """One-view cases on the two-voxel update tile (their own update class)
+    give the one-voxel tile's volumes bit for bit; many-view cases keep the
+    one-voxel tile."""
+    cases = batch_cases()
+    for c in cases:
+        c["subset_num"] = c["geom"].n_angles  # one view per subset
+    cases[3]["subset_num"] = 3                 # except one case
+    ref = [x.clone() for x in mod.Batch(cases).run()]
+    for k, c in enumerate(cases):
+        c["upd_tile"] = 1
+        c["upd_planes"] = (8, 16, 32)[k % 3]
+    out = mod.Batch(cases).run()
+    for a, b in zip(ref, out):
+        assert torch.equal(a, b)
+
+
 def test_batch_graph_matches_run(mod):
     cases = batch_cases()
     b1 = mod.Batch(cases)
