@@ -12,7 +12,8 @@ computes the same result, bit for bit):
   deeper slabs amortise the halo planes, shallower ones give more blocks;
   tried with both update tiles (``upd_tile``: one voxel per thread, or two
   side by side in x with fewer instructions per voxel but fewer resident
-  blocks) when the subsets hold one view each.
+  blocks) when the subsets hold one view each; the two-voxel tile must win
+  by ``TILE_MARGIN``.
 
 The tuner times each variant on the plan's own geometry (CUDA events on the
 launching stream, best of a few repetitions over all subsets) and keeps the
@@ -34,6 +35,10 @@ FP_BATCHES = (2, 4, 8)
 FP_VARIANTS = ((2, 0), (4, 0), (8, 0), (2, 1), (4, 1))
 UPD_PLANES = (8, 16, 32)
 UPD_TILES = (0, 1)  # NR_TILE_1, NR_TILE_2
+# The two-voxel tile is kept only when it beats the best one-voxel variant by
+# this fraction: it holds fewer resident blocks per SM, and near a tie the
+# choice would otherwise follow the timing noise from run to run.
+TILE_MARGIN = 0.02
 
 
 def cache_path() -> str:
@@ -130,6 +135,10 @@ def tune(plan, x: Optional[torch.Tensor] = None, reps: int = 3,
             up_ms[(t, z)] = _time(lambda: [plan.update(x, xo, 0) for _ in range(M)], reps)
     best_k, best_st = min(fp_ms, key=fp_ms.get)
     best_t, best_z = min(up_ms, key=up_ms.get)
+    if best_t == 1:
+        z1 = min(UPD_PLANES, key=lambda z: up_ms[(0, z)])
+        if up_ms[(0, z1)] <= up_ms[(1, best_z)] * (1.0 + TILE_MARGIN):
+            best_t, best_z = 0, z1
     plan.params.fp_batch = best_k
     plan.params.fp_stage = best_st
     plan.params.upd_planes = best_z
