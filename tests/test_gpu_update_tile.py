@@ -135,3 +135,27 @@ def test_reconstruct_applies_the_cached_choice(mod, tmp_path, monkeypatch):
                                           potential="huber")) is None
     with pytest.raises(ValueError):
         mod.reconstruct(g, y, b, tune="always", **kw)
+
+
+@pytest.mark.parametrize("tile", [0, 1])
+def test_nonfinite_input_is_reported_by_both_tiles(mod, tile):
+    """A NaN count reaches the update through h; both tiles flag the
+    non-finite voxels it produces (one-view subsets, so the tile applies)."""
+    from conftest import golden
+    from test_oracle_golden import geom_of
+
+    from newrecon_gb300.native import NrError
+
+    z = golden("tiny")
+    g = geom_of(z)
+    y = z["y"].copy()
+    y[(g.nbx // 2) * g.nby + g.nby // 2] = np.nan
+    plan = mod.OSTR(g, subset_num=g.n_angles, beta=1.0, delta=0.01, potential="huber",
+                    upd_tile=tile)
+    plan.setup(z["angles"], y, z["b"])
+    xt = torch.zeros(g.n_voxels, device="cuda")
+    plan.iterate(xt, 1)
+    with pytest.raises(NrError) as e:
+        plan.check()
+    assert e.value.code == 4
+    assert plan.check() == 0
