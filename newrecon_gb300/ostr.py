@@ -640,7 +640,7 @@ class BatchGraph:
 def reconstruct(geom: Geometry, prj, blank, scatter=None, *, angles, subset_num: int,
                 iter_num: int, beta: float, delta: float, potential: str = "lange",
                 gamma_mode: str = "length", x0=None, monotone: bool = False,
-                tune="cached"):
+                tune="cached", stream=None):
     """OSTR reconstruction: transmission counts in, attenuation (1/mm) out.
 
     prj, blank, scatter: [view][i][j] in original view order (the layout
@@ -650,10 +650,19 @@ def reconstruct(geom: Geometry, prj, blank, scatter=None, *, angles, subset_num:
     "cached" runs the kernel variants the autotuner cached for this GPU and
     geometry (the defaults when it has none), True tunes first when the
     cache has none, False runs the defaults.  Every variant gives the same
-    result bit for bit.
+    result bit for bit.  stream: a torch.cuda.Stream to run every copy and
+    kernel on (default: the current stream).  The call returns once that
+    stream has finished the reconstruction (the status check waits for it).
     """
     if not (tune == "cached" or tune is True or tune is False):
         raise ValueError('tune must be "cached", True or False')
+    if stream is not None:
+        if not isinstance(stream, torch.cuda.Stream):
+            raise TypeError("stream must be a torch.cuda.Stream")
+        with torch.cuda.stream(stream):
+            return reconstruct(geom, prj, blank, scatter, angles=angles, subset_num=subset_num,
+                               iter_num=iter_num, beta=beta, delta=delta, potential=potential,
+                               gamma_mode=gamma_mode, x0=x0, monotone=monotone, tune=tune)
     plan = OSTR(geom, subset_num=subset_num, beta=beta, delta=delta, potential=potential,
                 gamma_mode=gamma_mode, has_scatter=scatter is not None)
     plan.setup(angles, prj, blank, scatter)

@@ -271,3 +271,23 @@ def test_pinned_inputs_return_a_pinned_volume(mod):
     assert torch.equal(vol, ref.cpu())
     pageable = mod.reconstruct(g, torch.from_numpy(z["y"]), torch.from_numpy(z["b"]), **kw)
     assert not pageable.is_pinned() and torch.equal(pageable, vol)
+
+
+def test_reconstruct_on_a_side_stream(mod):
+    """reconstruct(stream=s) runs on s and gives the current stream's result
+    bit for bit, for host and for device inputs."""
+    z = golden("tiny")
+    g = geom_of(z)
+    kw = dict(angles=z["angles"], subset_num=3, iter_num=2, beta=1.0, delta=0.01,
+              potential="lange")
+    ref = mod.reconstruct(g, z["y"], z["b"], **kw)
+    s = torch.cuda.Stream()
+    got = mod.reconstruct(g, z["y"], z["b"], stream=s, **kw)
+    assert isinstance(got, np.ndarray) and np.array_equal(ref, got)
+    yd = torch.from_numpy(z["y"]).cuda()
+    bd = torch.from_numpy(z["b"]).cuda()
+    torch.cuda.synchronize()  # the inputs are written on the current stream
+    dev = mod.reconstruct(g, yd, bd, stream=s, **kw)
+    assert dev.is_cuda and np.array_equal(ref, dev.cpu().numpy())
+    with pytest.raises(TypeError):
+        mod.reconstruct(g, z["y"], z["b"], stream=1, **kw)
