@@ -90,6 +90,18 @@ def _time(fn, reps: int) -> float:
     return best
 
 
+def choose_update(up_ms: Dict[Tuple[int, int], float]) -> Tuple[int, int]:
+    """(upd_tile, upd_planes) from the timings of the update variants: the
+    fastest, except that the two-voxel tile must beat the fastest one-voxel
+    variant by TILE_MARGIN."""
+    best_t, best_z = min(up_ms, key=up_ms.get)
+    if best_t == 1:
+        z1 = min((z for t, z in up_ms if t == 0), key=lambda z: up_ms[(0, z)])
+        if up_ms[(0, z1)] <= up_ms[(1, best_z)] * (1.0 + TILE_MARGIN):
+            best_t, best_z = 0, z1
+    return best_t, best_z
+
+
 def apply_cached(plan) -> Optional[dict]:
     """Applies the cached choice for the plan's GPU, geometry and parameters;
     None (and the plan unchanged) when the cache holds none."""
@@ -134,11 +146,7 @@ def tune(plan, x: Optional[torch.Tensor] = None, reps: int = 3,
             plan.update(x, xo, 0)
             up_ms[(t, z)] = _time(lambda: [plan.update(x, xo, 0) for _ in range(M)], reps)
     best_k, best_st = min(fp_ms, key=fp_ms.get)
-    best_t, best_z = min(up_ms, key=up_ms.get)
-    if best_t == 1:
-        z1 = min(UPD_PLANES, key=lambda z: up_ms[(0, z)])
-        if up_ms[(0, z1)] <= up_ms[(1, best_z)] * (1.0 + TILE_MARGIN):
-            best_t, best_z = 0, z1
+    best_t, best_z = choose_update(up_ms)
     plan.params.fp_batch = best_k
     plan.params.fp_stage = best_st
     plan.params.upd_planes = best_z
