@@ -331,7 +331,9 @@ nr_status nr_ostr_check(void* workspace, size_t ws_bytes, int32_t* flags,
 
 /* The same three entry points under the names of the path's C-ABI contract
  * (fused sub-iteration, FP64 objective, workspace size): identical arguments
- * and behaviour. */
+ * and behaviour.  nr_workspace_size takes the parameters as well as the
+ * geometry: the workspace holds each subset's views (subset_num) and the
+ * scatter counts only when has_scatter is set, so the size depends on both. */
 nr_status nr_ostr_subset(const nr_geom* g, const nr_ostr_params* p, float* x, int32_t subset,
                          void* workspace, size_t ws_bytes, void* stream);
 nr_status nr_objective_fp64(const nr_geom* g, const nr_ostr_params* p, const float* x,
