@@ -76,12 +76,24 @@ def parse():
     return ap.parse_args()
 
 
-def workload_name(cfg):
+def _scan_name(cfg):
     g = cfg.geom
     return (f"{cfg.name}: {g.nx}x{g.ny}x{g.nz} vox @{g.vx:g}x{g.vy:g}x{g.vz:g}mm, "
             f"{g.nbx}x{g.nby} det @{g.bx:g}mm, {g.n_angles} views "
-            f"+-{float(np.degrees(np.abs(cfg.angles).max())):.3g}deg, {cfg.subset_num} subsets, "
-            f"{cfg.potential} d={cfg.delta:g} b={cfg.beta:g}, I0={cfg.I0:g}")
+            f"+-{float(np.degrees(np.abs(cfg.angles).max())):.3g}deg, {cfg.subset_num} subsets")
+
+
+def workload_name(cfg):
+    return (f"{_scan_name(cfg)}, {cfg.potential} d={cfg.delta:g} b={cfg.beta:g}, "
+            f"I0={cfg.I0:g}")
+
+
+def sart_workload_name(cfg, supersample):
+    """The OS-SART workload on a config's scan (both arms print this)."""
+    return (f"{_scan_name(cfg)}, OS-SART lambda 0.8, cos projector"
+            + (" (2x2 sub-rays per bin)" if supersample else "")
+            + f", hyperbola prior beta -0.2 d={cfg.delta:g}, line integrals of "
+              f"Poisson({cfg.I0:g}) counts")
 
 
 def make_scan_gpu(cfg, seed):
@@ -607,8 +619,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded breast phantom, Poisson counts)",
-        "config": {"workload": "clinical: 1024x512x60 vox @0.14x0.14x1mm, 1664x832 det @0.14mm, "
-                               "25 views +-25deg, 25 subsets, Huber d=0.003 b=100, I0=5e3",
+        "config": {"workload": workload_name(cfg),
                    "step": "1 OSTR sub-iteration on the host cores", "parallelism": "host"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{len(times)} sub-iterations (FP32 restatement of the "
@@ -743,18 +754,16 @@ def run_ossart(args):
             parts = ln.split()
             if len(parts) >= 2 and not ln.startswith("#") and parts[0] == dom:
                 traffic = float(parts[1])
-    workload = ("clinical: 1024x512x60 vox @0.14x0.14x1mm, 1664x832 det @0.14mm, 25 views "
-                "+-25deg, 25 subsets, OS-SART lambda 0.8, cos projector"
-                + (" (2x2 sub-rays per bin)" if args.supersample else "")
-                + ", hyperbola prior beta -0.2 d=0.003, line integrals of Poisson(5e3) counts")
+    workload = sart_workload_name(cfg, args.supersample)
     out = {
         "metric": SART_METRIC, "value": n_sub / elapsed, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded breast phantom, Poisson counts, log transform)",
-        "config": {"workload": workload, "step": "1 OS-SART iteration = 25 sub-iterations",
+        "config": {"workload": workload, "step": f"1 OS-SART iteration = {M} sub-iterations",
                    "parallelism": f"replicas x{ws}",
-                   "l2": "inputs larger than L2 (x, x': 2 x 126 MB; p, norm: 2 x 138 MB)"},
+                   "l2": f"inputs larger than L2 (x, x': 2 x {4 * g.n_voxels / 1e6:.0f} MB; "
+                         f"p, norm: 2 x {4 * g.n_angles * g.n_bins / 1e6:.0f} MB)"},
         "gpu_launches": 2 * M * args.steps,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": kern[dom]["gbs"], "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s",
@@ -831,7 +840,7 @@ def run_reference_ossart(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded breast phantom, Poisson counts, log transform)",
-        "config": {"workload": "clinical OS-SART (see --algo ossart)",
+        "config": {"workload": sart_workload_name(cfg, args.supersample),
                    "step": "1 OS-SART sub-iteration on the host cores", "parallelism": "host"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{len(times)} sub-iterations (FP32 restatement of the "
