@@ -78,3 +78,69 @@ def test_ctypes_mirror_matches_the_c_layout(c_layout, cname):
     assert ctypes.sizeof(cls) == c_layout[(cname, "sizeof")], cname
     for fname, _ in cls._fields_:
         assert getattr(cls, fname).offset == c_layout[(cname, fname)], (cname, fname)
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include <string.h>
+#include "nrgb300.h"
+
+/* A C caller of the boundary: geometry validation and workspace sizing run
+ * on the host, so this needs no GPU. */
+int main(void) {
+    nr_geom g;
+    nr_ostr_params p;
+    size_t bytes = 0;
+    memset(&g, 0, sizeof g);
+    memset(&p, 0, sizeof p);
+    g.nx = 256; g.ny = 128; g.nz = 24;
+    g.vx = 0.4f; g.vy = 0.4f; g.vz = 1.0f;
+    g.x_p0 = -51.2f; g.y_p0 = -51.2f; g.z_p0 = 0.0f;
+    g.nbx = 320; g.nby = 160; g.bx = 0.4f; g.by = 0.4f;
+    g.x_d0 = -64.0f; g.y_d0 = -64.0f;
+    g.detectorR = 20.0f; g.sourceR = 640.0f; g.sourceY = 0.0f;
+    g.n_angles = 9;
+    p.subset_num = 9; p.potential = NR_POT_HYPERBOLA; p.beta = 50.0f; p.delta = 0.002f;
+    printf("version %s\n", nr_version());
+    printf("valid %d\n", (int)nr_validate_geometry(&g, 9));
+    printf("bad_subsets %d\n", (int)nr_validate_geometry(&g, 4));
+    printf("ws_status %d\n", (int)nr_ostr_workspace_size(&g, &p, &bytes));
+    printf("ws_bytes %zu\n", bytes);
+    p.upd_tile = NR_TILE_2;
+    printf("ws_tile2 %d\n", (int)nr_ostr_workspace_size(&g, &p, &bytes));
+    return 0;
+}
+"""
+
+
+def test_a_c_program_links_and_calls_the_library(tmp_path, native_lib_path):
+    """Compiled with gcc against the header and linked to libnrgb300.so: the
+    host-side entry points answer as they do through ctypes."""
+    from newrecon_gb300.geometry import Geometry, NrOstrParams
+
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no gcc")
+    src, exe = tmp_path / "caller.c", tmp_path / "caller"
+    src.write_text(C_CALLER)
+    libdir = os.path.dirname(native_lib_path)
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", INCLUDE, str(src), "-o", str(exe),
+                        "-L", libdir, "-lnrgb300", f"-Wl,-rpath,{libdir}"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    vals = dict(ln.split(" ", 1) for ln in out.splitlines())
+    assert "sm_103a" in vals["version"]
+    assert vals["valid"] == "0" and vals["bad_subsets"] != "0"
+    assert vals["ws_status"] == "0" and vals["ws_tile2"] == "0"
+    # the same size through the Python binding
+    from newrecon_gb300 import native
+
+    g = Geometry(256, 128, 24, 0.4, 0.4, 1.0, -51.2, -51.2, 0.0, 320, 160, 0.4, 0.4, -64.0,
+                 -64.0, 20.0, 640.0, 0.0, 9)
+    gc = g.to_c()
+    p = NrOstrParams(9, 2, 0, 0, 50.0, 0.002)
+    size = ctypes.c_size_t(0)
+    assert native.load(native_lib_path).nr_ostr_workspace_size(
+        ctypes.byref(gc), ctypes.byref(p), ctypes.byref(size)) == 0
+    assert int(vals["ws_bytes"]) == size.value
