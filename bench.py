@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--cpu-dtype", default="f32", choices=["f32", "f64"],
                     help="the CPU baseline's arithmetic: the FP32 restatement or the FP64 oracle")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-monotone", action="store_true",
+                    help="skip the cost measurement of the monotone (FP64-checked) loops")
     ap.add_argument("--batch", type=int, default=0,
                     help="also time N batched reconstructions (shared launches, one CUDA graph)")
     ap.add_argument("--batch-steps", type=int, default=0,
@@ -63,8 +65,9 @@ def parse():
                     help="mixed: uneven clinical-pitch cases; fullres: 2048x1024x70 breasts "
                          "at 0.085 mm, 3328x1664 detector, 15 views")
     ap.add_argument("--no-tune", action="store_true")
-    ap.add_argument("--upd-tile", type=int, default=None, choices=[0, 1],
-                    help="force the OSTR update tile (0: one voxel per thread, 1: two) "
+    ap.add_argument("--upd-tile", type=int, default=None, choices=[0, 1, 2],
+                    help="force the OSTR update tile (0: one voxel per thread, 1: two, "
+                         "2: one voxel per thread on a TMA-fed ring) "
                          "instead of the tuner's or the default choice")
     ap.add_argument("--algo", default="ostr", choices=["ostr", "ossart", "dual-energy"],
                     help="ostr (the headline), ossart (the SART family on the same workload) "
@@ -329,6 +332,8 @@ def run_ours(args):
         out["clocks"] = clk
     if not args.no_e2e:
         out["e2e"] = e2e_ours(args, cfg, y, b)
+    if not args.no_monotone:
+        out["monotone"] = monotone_cost(plan, g)
     if rank == 0 and not args.no_cpu_baseline:
         d = plan.section("d").cpu().numpy()
         threads = args.cpu_threads or os.cpu_count() or 1
@@ -348,6 +353,50 @@ def run_ours(args):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def monotone_cost(plan, g):
+    """Wall time of one iteration of the plain loop, of the loop with the
+    FP64 objective check per iteration (monotone=True) and with the subset
+    objective check per sub-iteration (monotone="subset"), from the same
+    start; and of one FP64 objective evaluation."""
+    import torch
+
+    stream = torch.cuda.current_stream()
+    x0 = torch.zeros(g.n_voxels, device="cuda")
+    plan.iterate(x0, 2)  # a start away from zero
+
+    def timed(fn, reps=3):
+        best = float("inf")
+        for _ in range(reps):
+            x = x0.clone()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn(x)
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        return best * 1e3
+
+    plain = timed(lambda x: plan.iterate(x, 1))
+    it = timed(lambda x: plan.iterate(x, 1, monotone=True))
+    sub = timed(lambda x: plan.iterate(x, 1, monotone="subset"))
+    obj = timed(lambda x: plan.objective(x))
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    x = x0.clone()
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    plan.penalty(x, out)
+    a.record(stream)
+    plan.penalty(x, out)
+    b.record(stream)
+    b.synchronize()
+    return {"plain_iteration_ms": plain, "monotone_iteration_ms": it,
+            "monotone_subset_iteration_ms": sub, "objective_ms": obj,
+            "penalty_fp64_ms": a.elapsed_time(b),
+            "overhead_iteration": it / plain - 1.0, "overhead_subset": sub / plain - 1.0,
+            "note": "wall time from a start two iterations in; monotone=True adds one FP64 "
+                    "objective (all views + penalty) per iteration, monotone=\"subset\" one "
+                    "projection of the subset's views and one penalty per sub-iteration"}
 
 
 def batch_bench(args, rank):
@@ -565,18 +614,28 @@ def e2e_ours(args, cfg, y, b):
     ostr.reconstruct(g, y_h, b_h, **kw)  # warm-up
     torch.cuda.synchronize()
     ts = []
+    phases = []
     vol = None
     for _ in range(args.e2e_runs):
         # the caller is done with the previous volume (its pinned block goes
         # back to torch's host cache, as in a stream of reconstructions)
         vol = None
+        ph = {}
         t0 = time.perf_counter()
-        vol = ostr.reconstruct(g, y_h, b_h, **kw)
+        vol = ostr.reconstruct(g, y_h, b_h, timing=ph, **kw)
         torch.cuda.synchronize()
         ts.append(time.perf_counter() - t0)
+        phases.append(ph)
     assert vol.device.type == "cpu"
     sub = iters * cfg.subset_num
-    return {"value": sub / float(np.mean(ts)), "unit": UNIT,
+    # device time of each phase (CUDA events inside reconstruct), averaged over
+    # the runs; "host_s" is the rest of the call's wall time (plan and
+    # workspace creation, Python, launch gaps)
+    ph = {k: float(np.mean([p[k] for p in phases]))
+          for k in ("upload_s", "setup_s", "iterate_s", "download_s")}
+    ph["host_s"] = float(np.mean(ts)) - sum(ph.values())
+    ph["iterate_subiters_per_s"] = sub / ph["iterate_s"]
+    return {"value": sub / float(np.mean(ts)), "unit": UNIT, "phases": ph,
             "h2d_bytes_per_step": int(y.nbytes + b.nbytes + cfg.angles.nbytes),
             "d2h_bytes_per_step": int(g.n_voxels * 4),
             "step": f"ostr.reconstruct from pinned host buffers: upload, gamma/d setup, "

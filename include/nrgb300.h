@@ -6,7 +6,9 @@
  * element counts and a CUDA stream handle (passed as void*), returns an
  * nr_status and never allocates: buffers (including scratch workspace) belong
  * to the caller.  Geometry travels by value into the kernels, so the library
- * holds no global state and calls on different streams may overlap.
+ * holds no global state and calls on different streams may overlap.  The one
+ * exception is nr_penalty_fp64_static, which keeps its scratch in a
+ * per-device array inside the library: calls to it must not overlap.
  *
  * Layouts (the reference's, PranjalSahu/newrecon):
  *   volume       [z][y][x], x fastest            (Tomo_OSTR.cu:538, :1604)
@@ -159,7 +161,11 @@ typedef struct nr_ostr_params {
                                   voxels side by side in x of a 64 x 8-column tile
                                   (one-view subsets; others use NR_TILE_1).  Same
                                   result bit for bit; fewer instructions per voxel,
-                                  fewer resident blocks.                         */
+                                  fewer resident blocks.  NR_TILE_TMA: the
+                                  one-voxel tile with its planes streamed by TMA
+                                  through a shared-memory ring by a producer warp
+                                  (IMGSIZx a multiple of 4 and x 16-byte aligned,
+                                  else NR_TILE_1); same result bit for bit.       */
 } nr_ostr_params;
 
 enum {
@@ -169,7 +175,8 @@ enum {
 
 enum {
     NR_TILE_1 = 0,
-    NR_TILE_2 = 1
+    NR_TILE_2 = 1,
+    NR_TILE_TMA = 2
 };
 
 /* fp_batch, fp_stage, upd_planes and upd_tile select kernel variants only
@@ -329,6 +336,24 @@ nr_status nr_ostr_objective(const nr_geom* g, const nr_ostr_params* p,
 nr_status nr_ostr_check(void* workspace, size_t ws_bytes, int32_t* flags,
                         void* stream);
 
+/* nr_ostr_project (the fused forward projection and gradient h of one subset)
+ * that also returns, in data_out[0] (one device double), the subset's FP64
+ * data term: the sum over its views' bins of ybar + r - y log(ybar + r), each
+ * bin's term formed as in nr_ostr_objective's out[0] (whose views it sums
+ * over), from the same projection that makes h.  For subset-level step
+ * acceptance (the subset objective subset_num * data + beta * penalty).  No
+ * counterpart in the reference, whose gold driver evaluates no objective
+ * (Tomo_OSTR_gold.cpp:724-887).  The projection walks fp_batch steps per
+ * gather round (the direct walk, whatever fp_stage says). */
+nr_status nr_ostr_project_fp64(const nr_geom* g, const nr_ostr_params* p, const float* x,
+                               int32_t subset, double* data_out, void* workspace,
+                               size_t ws_bytes, void* stream);
+
+/* The penalty alone, out[0] = nr_ostr_objective's out[1] (one device double),
+ * over the workspace's partial sums.  No counterpart in the reference. */
+nr_status nr_ostr_penalty(const nr_geom* g, const nr_ostr_params* p, const float* x,
+                          double* out, void* workspace, size_t ws_bytes, void* stream);
+
 /* The same three entry points under the names of the path's C-ABI contract
  * (fused sub-iteration, FP64 objective, workspace size): identical arguments
  * and behaviour.  nr_workspace_size takes the parameters as well as the
@@ -339,6 +364,21 @@ nr_status nr_ostr_subset(const nr_geom* g, const nr_ostr_params* p, float* x, in
 nr_status nr_objective_fp64(const nr_geom* g, const nr_ostr_params* p, const float* x,
                             double* out, void* workspace, size_t ws_bytes, void* stream);
 nr_status nr_workspace_size(const nr_geom* g, const nr_ostr_params* p, size_t* bytes);
+
+/* Test hook for the bounded waits.  The kernels that wait on mbarriers (the
+ * TMA-fed update tile, the TMA-staged projection, the tensor-core
+ * convolutions) read the second status word of their workspace (an OSTR
+ * workspace, or the CNN's): with wait_index >= 0 set there, the wait number
+ * wait_index of every block (the update's ring plane, the projection's slab,
+ * the convolution CTA's tile) reports that it gave up once it has in fact
+ * succeeded.  Nothing is in flight at that point, so the failure path runs
+ * as it would after a real expiry -- the block flags NR_FLAG_TIMEOUT, stops
+ * issuing copies and MMAs, drains, releases its tensor memory -- and the
+ * next check returns NR_ERR_TIMEOUT.  wait_index < 0 turns the hook off;
+ * nr_ostr_check also clears it on an OSTR workspace after a flagged run.
+ * Enqueued on the stream.  No counterpart in the reference, which ignores
+ * CUDA errors (Tomo_OSTR_gold.cpp:460-462). */
+nr_status nr_test_expire_wait(void* workspace, int32_t wait_index, void* stream);
 
 /* The penalty of nr_ostr_objective (out[1] there) computed without any
  * workspace, into out[0] (one device double), for callers that may not
@@ -352,6 +392,10 @@ nr_status nr_workspace_size(const nr_geom* g, const nr_ostr_params* p, size_t* b
  * (1024x512x64 fits); larger volumes return NR_ERR_WORKSPACE.  The first call
  * on each device looks up the array's device address (cudaGetSymbolAddress)
  * with that device current; make that first call before any stream capture.
+ * The address is cached with the id of the CUDA context it belongs to, and
+ * looked up again when a call comes from a new context of that device (after
+ * cudaDeviceReset); make the first call after a reset outside a capture too.
+ * A failed lookup returns NR_ERR_CUDA and leaves CUDA's last error clear.
  * Every call shares the one array: calls that overlap on the GPU (other
  * streams, other host threads) race on it and must be serialised by the
  * caller.  Each call overwrites the partials it uses, so nothing carries over. */

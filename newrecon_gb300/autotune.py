@@ -10,10 +10,12 @@ computes the same result, bit for bit):
   the geometry allows it;
 * ``upd_planes`` -- z planes walked per block by the fused update (8, 16, 32):
   deeper slabs amortise the halo planes, shallower ones give more blocks;
-  tried with both update tiles (``upd_tile``: one voxel per thread, or two
-  side by side in x with fewer instructions per voxel but fewer resident
-  blocks) when the subsets hold one view each; the two-voxel tile must win
-  by ``TILE_MARGIN``.
+  tried with each update tile (``upd_tile``: one voxel per thread; two side
+  by side in x, with fewer instructions per voxel but fewer resident blocks,
+  when the subsets hold one view each; or one voxel per thread with the
+  planes streamed by TMA through a ring filled by a producer warp, where the
+  volume's rows allow TMA); a tile other than the default one voxel per
+  thread must win by ``TILE_MARGIN``.
 
 The tuner times each variant on the plan's own geometry (CUDA events on the
 launching stream, best of a few repetitions over all subsets) and keeps the
@@ -34,10 +36,11 @@ FP_BATCHES = (2, 4, 8)
 # batch, TMA-staged slabs for 2 and 4
 FP_VARIANTS = ((2, 0), (4, 0), (8, 0), (2, 1), (4, 1))
 UPD_PLANES = (8, 16, 32)
-UPD_TILES = (0, 1)  # NR_TILE_1, NR_TILE_2
-# The two-voxel tile is kept only when it beats the best one-voxel variant by
-# this fraction: it holds fewer resident blocks per SM, and near a tie the
-# choice would otherwise follow the timing noise from run to run.
+UPD_TILES = (0, 1, 2)  # NR_TILE_1, NR_TILE_2, NR_TILE_TMA
+TILE_NAMES = {0: "", 1: "-x2", 2: "-tma"}
+# A tile other than the default one-voxel tile is kept only when it beats the
+# best one-voxel variant by this fraction: near a tie the choice would
+# otherwise follow the timing noise from run to run.
 TILE_MARGIN = 0.02
 
 
@@ -51,7 +54,7 @@ def signature(plan) -> str:
     p = plan.params
     dev = torch.cuda.get_device_name(plan.ws.device)
     return (f"{dev}|{g.nx}x{g.ny}x{g.nz}|{g.nbx}x{g.nby}|A{g.n_angles}|M{p.subset_num}"
-            f"|pot{p.potential}|scat{p.has_scatter}|v3")
+            f"|pot{p.potential}|scat{p.has_scatter}|v4")
 
 
 def _load() -> Dict[str, dict]:
@@ -92,12 +95,12 @@ def _time(fn, reps: int) -> float:
 
 def choose_update(up_ms: Dict[Tuple[int, int], float]) -> Tuple[int, int]:
     """(upd_tile, upd_planes) from the timings of the update variants: the
-    fastest, except that the two-voxel tile must beat the fastest one-voxel
-    variant by TILE_MARGIN."""
+    fastest, except that a tile other than the one-voxel tile (0) must beat
+    the fastest one-voxel variant by TILE_MARGIN."""
     best_t, best_z = min(up_ms, key=up_ms.get)
-    if best_t == 1:
+    if best_t != 0:
         z1 = min((z for t, z in up_ms if t == 0), key=lambda z: up_ms[(0, z)])
-        if up_ms[(0, z1)] <= up_ms[(1, best_z)] * (1.0 + TILE_MARGIN):
+        if up_ms[(0, z1)] <= up_ms[(best_t, best_z)] * (1.0 + TILE_MARGIN):
             best_t, best_z = 0, z1
     return best_t, best_z
 
@@ -139,7 +142,7 @@ def tune(plan, x: Optional[torch.Tensor] = None, reps: int = 3,
         fp_ms[(k, st)] = _time(lambda: [plan.project(x, a) for a in range(M)], reps)
     plan.params.fp_batch, plan.params.fp_stage = saved[0], saved[2]
     plan.project(x, 0)  # h of subset 0 for the update timings
-    for t in (UPD_TILES if one_view else (0,)):
+    for t in (UPD_TILES if one_view else (0, 2)):
         for z in UPD_PLANES:
             plan.params.upd_tile = t
             plan.params.upd_planes = z
@@ -153,7 +156,7 @@ def tune(plan, x: Optional[torch.Tensor] = None, reps: int = 3,
     plan.params.upd_tile = best_t
     rec = {"fp_batch": best_k, "fp_stage": best_st, "upd_planes": best_z, "upd_tile": best_t,
            "fp_ms": {f"{k}{'-tma' if st else ''}": v for (k, st), v in fp_ms.items()},
-           "update_ms": {f"{z}{'-x2' if t else ''}": v for (t, z), v in up_ms.items()}}
+           "update_ms": {f"{z}{TILE_NAMES[t]}": v for (t, z), v in up_ms.items()}}
     if use_cache:
         _store(key, rec)
     return best_k, best_z, rec

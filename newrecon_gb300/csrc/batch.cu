@@ -211,7 +211,8 @@ NR_API nr_status nr_batch_prepare(const nr_batch_case* cases, int32_t n_cases, v
             k.p.potential > NR_POT_HUBER ||
             (k.p.upd_planes != 0 && k.p.upd_planes != 8 && k.p.upd_planes != 16 &&
              k.p.upd_planes != 32) ||
-            (k.p.upd_tile != NR_TILE_1 && k.p.upd_tile != NR_TILE_2))
+            (k.p.upd_tile != NR_TILE_1 && k.p.upd_tile != NR_TILE_2 &&
+             k.p.upd_tile != NR_TILE_TMA))
             return NR_ERR_BAD_ARGUMENT;
     }
     auto total_sub = [&](int c) { return cases[c].n_iters * cases[c].p.subset_num; };

@@ -123,7 +123,12 @@ __global__ void __launch_bounds__(128) conv32_kernel(Dims d, const __nv_bfloat16
     const int64_t nt = ntiles(d);
     int64_t qg = 0;  // strips staged so far by this CTA
     int ntile = 0;   // tiles finished so far by this CTA
+    int ncommit = 0; // commits to the "done" barrier so far
     bool ok = true;
+    // test hook: the workspace's second status word k + 1 > 0 makes the wait
+    // for this CTA's tile k report giving up once it has in fact succeeded
+    // (its MMAs are complete), so the failure path runs with nothing in flight
+    const int force_at = status[1] - 1;
     for (int64_t t = blockIdx.x; t < nt; t += gridDim.x) {
         int b, z, y, x0;
         tile_pos(d, t, b, z, y, x0);
@@ -169,8 +174,14 @@ __global__ void __launch_bounds__(128) conv32_kernel(Dims d, const __nv_bfloat16
                 tc::commit(&bars[st]);
             }
         }
+        // uniform from here, so that every thread counts the commits alike
+        ok = __syncthreads_and(ok) != 0;
         if (tid == 0 && ok) tc::commit(&bars[NSTAGE]);
-        if (ok) ok = tc::mbar_wait(&bars[NSTAGE], (uint32_t)(ntile & 1), WAIT_LIMIT);
+        if (ok) {
+            ok = tc::mbar_wait(&bars[NSTAGE], (uint32_t)(ncommit & 1), WAIT_LIMIT) &&
+                 ntile != force_at;
+            ncommit++;
+        }
         ntile++;
         tc::fence_after();
         if (!__syncthreads_and(ok)) {
@@ -187,9 +198,13 @@ __global__ void __launch_bounds__(128) conv32_kernel(Dims d, const __nv_bfloat16
         tc::fence_before();
         __syncthreads();  // TMEM read before the next tile's MMAs overwrite it
     }
-    // drain: nothing may be in flight when TMEM is released
+    // drain: nothing may be in flight when TMEM is released.  The commit
+    // arrives once every MMA this thread issued has completed; a drain that
+    // gives up is retried once (bounded) before TMEM is released regardless,
+    // which the CTA must do before it exits.
     if (tid == 0) tc::commit(&bars[NSTAGE]);
-    tc::mbar_wait(&bars[NSTAGE], (uint32_t)(ntile & 1), WAIT_LIMIT);
+    if (!tc::mbar_wait(&bars[NSTAGE], (uint32_t)(ncommit & 1), WAIT_LIMIT))
+        tc::mbar_wait(&bars[NSTAGE], (uint32_t)(ncommit & 1), WAIT_LIMIT);
     tc::fence_before();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, 32);
@@ -220,7 +235,9 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restr
     constexpr uint32_t idesc = tc::idesc_bf16(TM, C);
     const int64_t nt = ntiles(d);
     int ntile = 0;
+    int ncommit = 0;
     bool ok = true;
+    const int force_at = status[1] - 1;  // test hook, as in conv32_kernel
     for (int64_t t = blockIdx.x; t < nt; t += gridDim.x) {
         int b, z, y, x0;
         tile_pos(d, t, b, z, y, x0);
@@ -241,7 +258,7 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restr
 #pragma unroll
         for (int kc = 0; kc < KCH; kc++) *(uint4*)(sA + kc * TM * 16 + tid * 16) = ((uint4*)row)[kc];
         tc::fence_async_smem();
-        __syncthreads();
+        ok = __syncthreads_and(ok) != 0;  // uniform: every thread counts the commits alike
         if (tid == 0 && ok) {
             tc::fence_after();
             const uint32_t sa = tc::smem_u32(sA), sw = tc::smem_u32(sW);
@@ -251,7 +268,10 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restr
                              tc::sdesc(sw + j * 256, 128, 512), idesc, j != 0);
             tc::commit(&bars[0]);
         }
-        if (ok) ok = tc::mbar_wait(&bars[0], (uint32_t)(ntile & 1), WAIT_LIMIT);
+        if (ok) {
+            ok = tc::mbar_wait(&bars[0], (uint32_t)(ncommit & 1), WAIT_LIMIT) && ntile != force_at;
+            ncommit++;
+        }
         ntile++;
         tc::fence_after();
         if (!__syncthreads_and(ok)) {
@@ -267,8 +287,9 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restr
         tc::fence_before();
         __syncthreads();
     }
-    if (tid == 0) tc::commit(&bars[0]);
-    tc::mbar_wait(&bars[0], (uint32_t)(ntile & 1), WAIT_LIMIT);
+    if (tid == 0) tc::commit(&bars[0]);  // drain, as in conv32_kernel
+    if (!tc::mbar_wait(&bars[0], (uint32_t)(ncommit & 1), WAIT_LIMIT))
+        tc::mbar_wait(&bars[0], (uint32_t)(ncommit & 1), WAIT_LIMIT);
     tc::fence_before();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, 32);

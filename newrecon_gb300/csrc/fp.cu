@@ -129,6 +129,28 @@ __global__ void __launch_bounds__(128, (K >= 8 ? 8 : 12)) fp_h_kernel(const __gr
     fp_h_tile<K>(G, vol, h, angles, index, a0, y, b, r, blockIdx.x, blockIdx.y, blockIdx.z, src);
 }
 
+// fp_h_kernel with the subset's FP64 data term: one partial per block in red
+// (project.cuh, DATA), summed by partials_sum_kernel.
+template <int K>
+__global__ void __launch_bounds__(128) fp_h_data_kernel(const __grid_constant__ Geo G,
+                                                        const float* __restrict__ vol,
+                                                        float* __restrict__ h,
+                                                        const float* __restrict__ angles,
+                                                        const int32_t* __restrict__ index, int a0,
+                                                        const float* __restrict__ y,
+                                                        const float* __restrict__ b,
+                                                        const float* __restrict__ r,
+                                                        double* __restrict__ red) {
+    __shared__ ViewSrc src;
+    fp_h_tile<K, true>(G, vol, h, angles, index, a0, y, b, r, blockIdx.x, blockIdx.y, blockIdx.z,
+                       src, red);
+}
+
+__global__ void __launch_bounds__(1024) partials_sum_kernel(const double* __restrict__ red,
+                                                            int64_t n, double* __restrict__ out) {
+    sum_partials(red, n, out);
+}
+
 // The same with the volume staged slab by slab through shared memory by TMA
 // (slab.cuh); bit-identical to fp_h_kernel.  Measured on the clinical
 // workload it is slower than the direct gathers (0.255 ms with 4-plane slabs,
@@ -306,6 +328,24 @@ bool slab_map(const nr_geom& g, const float* x, CUtensorMap* map) {
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The TMA descriptor of volume x with a box of bx x by x bz voxels (bx a
+// multiple of 4) whose out-of-volume elements read as NaN: the update's
+// planes with their halo (update.cuh), where NaN marks a neighbour outside
+// the volume.  False when the volume cannot be described.
+bool volume_map_nan(const nr_geom& g, const float* x, int bx, int by, int bz, CUtensorMap* map) {
+    if (g.nx % 4 != 0 || bx % 4 != 0 || ((uintptr_t)x & 15) != 0) return false;
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.nx * 4, (cuuint64_t)g.nx * g.ny * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)x, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NAN_REQUEST_ZERO_FMA) == CUDA_SUCCESS;
+}
+
 // premap: x's descriptor when the caller encoded it already (slab_map), else
 // nullptr (encoded here when staging applies).
 nr_status launch_fp_h(const nr_geom& g, int k, int stage, const float* x, float* h,
@@ -340,6 +380,26 @@ nr_status launch_fp_h(const nr_geom& g, int k, int stage, const float* x, float*
         fp_h_kernel<8><<<grd, blk, 0, st>>>(G, x, h, angles, index, a0, y, b, r);
     else
         fp_h_kernel<4><<<grd, blk, 0, st>>>(G, x, h, angles, index, a0, y, b, r);
+    return launch_status();
+}
+
+// The fused projection of launch_fp_h (direct gathers, K steps per round)
+// with the subset's FP64 data term into out[0]; red holds red_n partials.
+nr_status launch_fp_h_data(const nr_geom& g, int k, const float* x, float* h,
+                           const float* angles, const int32_t* index, int a0, int nviews,
+                           const float* y, const float* b, const float* r, double* red,
+                           int64_t red_n, double* out, cudaStream_t st) {
+    dim3 blk(32, 4), grd(cdiv(g.nbx, 32), cdiv(g.nby, 4), nviews);
+    const int64_t n = (int64_t)grd.x * grd.y * grd.z;
+    if (n > red_n) return NR_ERR_WORKSPACE;
+    const Geo G = make_geo(g);
+    if (k == 2)
+        fp_h_data_kernel<2><<<grd, blk, 0, st>>>(G, x, h, angles, index, a0, y, b, r, red);
+    else if (k == 8)
+        fp_h_data_kernel<8><<<grd, blk, 0, st>>>(G, x, h, angles, index, a0, y, b, r, red);
+    else
+        fp_h_data_kernel<4><<<grd, blk, 0, st>>>(G, x, h, angles, index, a0, y, b, r, red);
+    partials_sum_kernel<<<1, 1024, 0, st>>>(red, n, out);
     return launch_status();
 }
 

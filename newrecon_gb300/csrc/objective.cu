@@ -14,31 +14,12 @@
 // fixed order, so the value is deterministic.
 #include <cmath>
 #include <mutex>
+#include <utility>
 
+#include "reduce.cuh"
 #include "siddon.cuh"
 
 namespace nr {
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Block sum of v written to red[blk] by thread 0 (blockDim multiple of 32, <= 1024).
-__device__ __forceinline__ void block_partial(double v, double* red, int64_t blk) {
-    __shared__ double ws[32];
-    const int t = threadIdx.y * blockDim.x + threadIdx.x;
-    const int nt = blockDim.x * blockDim.y;
-    v = warp_sum(v);
-    if ((t & 31) == 0) ws[t >> 5] = v;
-    __syncthreads();
-    if (t < 32) {
-        double s = (t < (nt >> 5)) ? ws[t] : 0.0;
-        s = warp_sum(s);
-        if (t == 0) red[blk] = s;
-    }
-}
 
 __global__ void __launch_bounds__(128) data_term_kernel(
     const __grid_constant__ Geo G, const float* __restrict__ x, const float* __restrict__ angles,
@@ -67,34 +48,36 @@ __global__ void __launch_bounds__(128) data_term_kernel(
     block_partial(term, red, blk);
 }
 
+// psi(t) in double throughout: t is the exact difference of two floats (a
+// double holds it), and the weights are the double values 1/sqrt(...), so the
+// only roundings left are the double operations' own.
 template <int POT>
-__device__ __forceinline__ double psi(float t, float delta) {
-    if (POT == NR_POT_Q2) return 0.5 * (double)t * (double)t;
+__device__ __forceinline__ double psi(double t, double delta) {
+    if (POT == NR_POT_Q2) return 0.5 * t * t;
     if (POT == NR_POT_LANGE) {
-        const double a = fabs((double)t) / (double)delta;
-        return (double)delta * (double)delta * (a - log1p(a));
+        const double a = fabs(t) / delta;
+        return delta * delta * (a - log1p(a));
     }
     if (POT == NR_POT_HYPERBOLA) {
         // d^2 (sqrt(1+u^2) - 1) = d^2 u^2 / (sqrt(1+u^2) + 1): no cancellation
-        const float u = t / delta;
-        const float u2 = u * u;
-        return (double)delta * (double)delta * (double)(u2 / (sqrtf(1.f + u2) + 1.f));
+        const double u = t / delta;
+        const double u2 = u * u;
+        return delta * delta * (u2 / (sqrt(1.0 + u2) + 1.0));
     }
-    const float a = fabsf(t);
-    return a <= delta ? 0.5 * (double)t * (double)t
-                      : (double)delta * (double)a - 0.5 * (double)delta * (double)delta;
+    const double a = fabs(t);
+    return a <= delta ? 0.5 * t * t : delta * a - 0.5 * delta * delta;
 }
 
 struct PairW {
-    float w[13];  // forward neighbours: dz=+1 (9), dz=0 dy=+1 (3), dz=0 dy=0 dx=+1 (1)
+    double w[13];  // forward neighbours: dz=+1 (9), dz=0 dy=+1 (3), dz=0 dy=0 dx=+1 (1)
 };
 
-__host__ inline PairW make_pair_weights(float zxy) {
+// zxy = Vz / Vx, formed in double from the float sizes.
+__host__ inline PairW make_pair_weights(double zxy) {
     PairW p;
     int k = 0;
     auto put = [&](int dx, int dy, int dz) {
-        float dist = std::sqrt((float)(dx * dx + dy * dy) + (float)(dz * dz) * zxy * zxy);
-        p.w[k++] = (float)(1.0 / (double)dist);
+        p.w[k++] = 1.0 / std::sqrt((double)(dx * dx + dy * dy) + (double)(dz * dz) * zxy * zxy);
     };
     for (int dy = -1; dy <= 1; dy++)
         for (int dx = -1; dx <= 1; dx++) put(dx, dy, 1);
@@ -122,8 +105,8 @@ __global__ void __launch_bounds__(128) penalty_kernel(const __grid_constant__ Ge
             const int kx = ix + dx, ky = iy + dy, kz = iz + dz;
             if ((unsigned)kx < (unsigned)g.nx && (unsigned)ky < (unsigned)g.ny &&
                 (unsigned)kz < (unsigned)g.nz) {
-                const float t = xc - __ldg(x + kz * plane + (int64_t)ky * g.nx + kx);
-                acc += (double)W.w[k] * psi<POT>(t, delta);
+                const double t = (double)xc - (double)__ldg(x + kz * plane + (int64_t)ky * g.nx + kx);
+                acc += W.w[k] * psi<POT>(t, (double)delta);
             }
             k++;
         };
@@ -160,6 +143,11 @@ __global__ void __launch_bounds__(1024) final_sum_kernel(const double* __restric
     }
 }
 
+__global__ void __launch_bounds__(1024) penalty_sum_kernel(const double* __restrict__ red,
+                                                           int64_t n, double* __restrict__ out) {
+    sum_partials(red, n, out);
+}
+
 static int64_t data_blocks(const nr_geom& g) {
     return (int64_t)cdiv(g.nbx, 32) * cdiv(g.nby, 4) * g.n_angles;
 }
@@ -168,6 +156,32 @@ static int64_t pen_blocks(const nr_geom& g) {
 }
 
 int64_t objective_partials(const nr_geom& g) { return data_blocks(g) + pen_blocks(g); }
+
+template <int POT>
+static void launch_penalty_t(const nr_geom& g, float delta, const float* x, double* red,
+                             cudaStream_t st) {
+    dim3 blk(32, 4), grd(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz);
+    penalty_kernel<POT><<<grd, blk, 0, st>>>(make_geo(g),
+                                             make_pair_weights((double)g.vz / (double)g.vx), x,
+                                             delta, red);
+}
+
+// The penalty alone into out[0] (out[1] of launch_objective), over red_n partials.
+nr_status launch_penalty(const nr_geom& g, int pot, float delta, const float* x, double* red,
+                         int64_t red_n, double* out, cudaStream_t st) {
+    const int64_t np = pen_blocks(g);
+    if (np > red_n) return NR_ERR_WORKSPACE;
+    const float dl = pot == NR_POT_Q2 ? 1.f : delta;
+    switch (pot) {
+    case NR_POT_Q2: launch_penalty_t<NR_POT_Q2>(g, dl, x, red, st); break;
+    case NR_POT_LANGE: launch_penalty_t<NR_POT_LANGE>(g, dl, x, red, st); break;
+    case NR_POT_HYPERBOLA: launch_penalty_t<NR_POT_HYPERBOLA>(g, dl, x, red, st); break;
+    case NR_POT_HUBER: launch_penalty_t<NR_POT_HUBER>(g, dl, x, red, st); break;
+    default: return NR_ERR_BAD_ARGUMENT;
+    }
+    penalty_sum_kernel<<<1, 1024, 0, st>>>(red, np, out);
+    return launch_status();
+}
 
 nr_status launch_objective(const nr_geom& g, int pot, float delta, const float* x,
                            const float* angles, const int32_t* index, const float* y,
@@ -182,7 +196,7 @@ nr_status launch_objective(const nr_geom& g, int pot, float delta, const float* 
     }
     {
         dim3 blk(32, 4), grd(cdiv(g.nx, 32), cdiv(g.ny, 4), g.nz);
-        const PairW W = make_pair_weights(g.vz / g.vx);
+        const PairW W = make_pair_weights((double)g.vz / (double)g.vx);
         const float dl = pot == NR_POT_Q2 ? 1.f : delta;
         switch (pot) {
         case NR_POT_Q2: penalty_kernel<NR_POT_Q2><<<grd, blk, 0, st>>>(G, W, x, dl, red + nd); break;
@@ -234,25 +248,64 @@ __global__ void __launch_bounds__(1024) static_sum_kernel(const double* __restri
     }
 }
 
+// The unique id of the current context (cuCtxGetCurrent + cuCtxGetId from
+// the driver, looked up once); 0 when it cannot be had.  Ids are never
+// reused within a process, so a context created after cudaDeviceReset has a
+// new one.
+static unsigned long long current_context_id() {
+    typedef int (*get_current_fn)(void**);
+    typedef int (*get_id_fn)(void*, unsigned long long*);
+    static const auto fns = [] {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault,
+                                             &qa) != cudaSuccess ||
+            qa != cudaDriverEntryPointSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) !=
+                cudaSuccess ||
+            qb != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            a = b = nullptr;
+        }
+        return std::make_pair((get_current_fn)a, (get_id_fn)b);
+    }();
+    if (!fns.first || !fns.second) return 0;
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (fns.first(&ctx) != 0 || !ctx || fns.second(ctx, &id) != 0) return 0;
+    return id;
+}
+
 // Device address of g_static_partials on the current device.  The first call
-// on a device looks it up (cudaGetSymbolAddress) with that device current.
+// on a device looks it up (cudaGetSymbolAddress) with that device current and
+// caches it with the context's id; a call from another context of that
+// device (after cudaDeviceReset) looks it up again.  A failed lookup leaves
+// no error behind in CUDA's last-error slot, so it is not charged to a later
+// call.
 static double* static_partials(nr_status* st) {
     constexpr int kMaxDevices = 64;
     static std::mutex mu;
     static double* ptrs[kMaxDevices] = {};
+    static unsigned long long ctx_ids[kMaxDevices] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
         *st = NR_ERR_CUDA;
         return nullptr;
     }
     std::lock_guard<std::mutex> lock(mu);
-    if (!ptrs[dev]) {
+    if (!ptrs[dev] || current_context_id() != ctx_ids[dev]) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_static_partials) != cudaSuccess || !p) {
+            cudaGetLastError();
+            ptrs[dev] = nullptr;
             *st = NR_ERR_CUDA;
             return nullptr;
         }
         ptrs[dev] = (double*)p;
+        // read after the lookup: it is the lookup that makes the context current
+        ctx_ids[dev] = current_context_id();
     }
     return ptrs[dev];
 }
@@ -275,7 +328,7 @@ NR_API nr_status nr_penalty_fp64_static(const nr_geom* g, const float* x, int32_
     if (!red) return st;
     cudaStream_t s = as_stream(stream);
     const Geo G = make_geo(*g);
-    const PairW W = make_pair_weights(g->vz / g->vx);
+    const PairW W = make_pair_weights((double)g->vz / (double)g->vx);
     const float dl = potential == NR_POT_Q2 ? 1.f : delta;
     dim3 blk(32, 4), grd(cdiv(g->nx, 32), cdiv(g->ny, 4), g->nz);
     // every block overwrites its own partial: nothing to clear between calls

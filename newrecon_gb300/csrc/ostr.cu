@@ -32,7 +32,17 @@ nr_status launch_bp(const nr_geom& g, bool ji, float* vol, const float* prj, con
 nr_status launch_update(const nr_geom& g, int pot, int zc, int tile, const float* x, float* x_out,
                         const float* d, const float* h, const float* angles, const int32_t* index,
                         const BpTab& T, int a0, int nv, float M, float beta, float delta,
-                        int* status, cudaStream_t st);
+                        int* status, const CUtensorMap* map, cudaStream_t st);
+bool volume_map_nan(const nr_geom& g, const float* x, int bx, int by, int bz, CUtensorMap* map);
+
+// The TMA descriptor the update's NR_TILE_TMA form reads volume x through
+// (its planes with halo, NaN outside the volume); false when the volume
+// cannot be described (IMGSIZx not a multiple of 4, x not 16-byte aligned),
+// and the update then runs the one-voxel tile instead.
+static bool update_map(const nr_geom& g, const nr_ostr_params& p, const float* x,
+                       CUtensorMap* map) {
+    return p.upd_tile == NR_TILE_TMA && volume_map_nan(g, x, UTW, USH, 1, map);
+}
 nr_status launch_bp_tables(const nr_geom& g, const float* angles, const int32_t* index,
                            float4* tx, float4* ty, cudaStream_t st);
 nr_status launch_transpose(float* out, const float* in, int rows, int cols, int nviews, int M,
@@ -42,6 +52,12 @@ nr_status launch_objective(const nr_geom& g, int pot, float delta, const float* 
                            const float* b, const float* r, double* red, int64_t red_n,
                            double* out, cudaStream_t st);
 int64_t objective_partials(const nr_geom& g);
+nr_status launch_fp_h_data(const nr_geom& g, int k, const float* x, float* h,
+                           const float* angles, const int32_t* index, int a0, int nviews,
+                           const float* y, const float* b, const float* r, double* red,
+                           int64_t red_n, double* out, cudaStream_t st);
+nr_status launch_penalty(const nr_geom& g, int pot, float delta, const float* x, double* red,
+                         int64_t red_n, double* out, cudaStream_t st);
 
 struct Layout {
     size_t status, red, index, angles, y, b, r, d, xtmp, h, bpx, bpy, gc, gr, total;
@@ -127,7 +143,8 @@ static nr_status check_params(const nr_geom* g, const nr_ostr_params* p) {
     if (p->upd_planes != 0 && p->upd_planes != 8 && p->upd_planes != 16 && p->upd_planes != 32)
         return NR_ERR_BAD_ARGUMENT;
     if (p->fp_stage != NR_STAGE_OFF && p->fp_stage != NR_STAGE_TMA) return NR_ERR_BAD_ARGUMENT;
-    if (p->upd_tile != NR_TILE_1 && p->upd_tile != NR_TILE_2) return NR_ERR_BAD_ARGUMENT;
+    if (p->upd_tile != NR_TILE_1 && p->upd_tile != NR_TILE_2 && p->upd_tile != NR_TILE_TMA)
+        return NR_ERR_BAD_ARGUMENT;
     if (g->ny > 65535 || g->nz > 65535 || g->n_angles > 65535) return NR_ERR_BAD_GEOMETRY;
     if (!bp_tables_fit(*g)) return NR_ERR_BAD_GEOMETRY;
     return NR_OK;
@@ -156,6 +173,8 @@ __global__ void index_kernel(int32_t* idx, const float* __restrict__ angles_in,
 __global__ void clear_status_kernel(int* s) {
     if (threadIdx.x < 64) s[threadIdx.x] = 0;
 }
+
+__global__ void set_word_kernel(int* p, int v) { *p = v; }
 
 // The two set-up launches the OS-SART driver (sart.cu) shares.
 nr_status launch_subset_index(int32_t* idx, const float* angles_in, float* angles_out, int A,
@@ -268,8 +287,11 @@ NR_API nr_status nr_ostr_update(const nr_geom* g, const nr_ostr_params* p, const
         return NR_ERR_BAD_ARGUMENT;
     WS w = carve(workspace, L);
     const int M = p->subset_num, Vs = g->n_angles / M;
-    return launch_update(*g, p->potential, p->upd_planes, p->upd_tile, x, x_out, w.d, w.h, w.angles, w.index, w.tab(), subset * Vs, Vs,
-                         (float)M, p->beta, p->delta, w.status, as_stream(stream));
+    CUtensorMap map;
+    const bool mapped = update_map(*g, *p, x, &map);
+    return launch_update(*g, p->potential, p->upd_planes, p->upd_tile, x, x_out, w.d, w.h,
+                         w.angles, w.index, w.tab(), subset * Vs, Vs, (float)M, p->beta, p->delta,
+                         w.status, mapped ? &map : nullptr, as_stream(stream));
 }
 
 NR_API nr_status nr_ostr_workspace_section(const nr_geom* g, const nr_ostr_params* p,
@@ -306,8 +328,11 @@ NR_API nr_status nr_ostr_subiter(const nr_geom* g, const nr_ostr_params* p, floa
     const int a0 = subset * Vs;
     if ((st = launch_fp_h(*g, p->fp_batch, p->fp_stage, x, w.h, w.angles, w.index, a0, Vs, w.y, w.b, w.r, w.status, nullptr, s)) != NR_OK)
         return st;
-    if ((st = launch_update(*g, p->potential, p->upd_planes, p->upd_tile, x, w.xtmp, w.d, w.h, w.angles, w.index, w.tab(), a0, Vs,
-                            (float)M, p->beta, p->delta, w.status, s)) != NR_OK)
+    CUtensorMap map;
+    const bool mapped = update_map(*g, *p, x, &map);
+    if ((st = launch_update(*g, p->potential, p->upd_planes, p->upd_tile, x, w.xtmp, w.d, w.h,
+                            w.angles, w.index, w.tab(), a0, Vs, (float)M, p->beta, p->delta,
+                            w.status, mapped ? &map : nullptr, s)) != NR_OK)
         return st;
     if (cudaMemcpyAsync(x, w.xtmp, N * sizeof(float), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
         return NR_ERR_CUDA;
@@ -326,6 +351,9 @@ static nr_status enqueue_iterations(const nr_geom* g, const nr_ostr_params* p, f
     CUtensorMap maps[2];
     const bool staged = p->fp_stage == NR_STAGE_TMA && p->fp_batch != 8 &&
                         slab_map(*g, x, &maps[0]) && slab_map(*g, w.xtmp, &maps[1]);
+    // and the TMA-fed update's
+    CUtensorMap umaps[2];
+    const bool umapped = update_map(*g, *p, x, &umaps[0]) && update_map(*g, *p, w.xtmp, &umaps[1]);
     for (int it = 0; it < n_iters; it++) {
         for (int a = 0; a < M; a++) {
             const int a0 = a * Vs;
@@ -333,8 +361,10 @@ static nr_status enqueue_iterations(const nr_geom* g, const nr_ostr_params* p, f
                                   staged ? &maps[cur == x ? 0 : 1] : nullptr, s)) !=
                 NR_OK)
                 return st;
-            if ((st = launch_update(*g, p->potential, p->upd_planes, p->upd_tile, cur, nxt, w.d, w.h, w.angles, w.index, w.tab(), a0, Vs,
-                                    (float)M, p->beta, p->delta, w.status, s)) != NR_OK)
+            if ((st = launch_update(*g, p->potential, p->upd_planes, p->upd_tile, cur, nxt, w.d,
+                                    w.h, w.angles, w.index, w.tab(), a0, Vs, (float)M, p->beta,
+                                    p->delta, w.status,
+                                    umapped ? &umaps[cur == x ? 0 : 1] : nullptr, s)) != NR_OK)
                 return st;
             float* t = cur;
             cur = nxt;
@@ -397,6 +427,29 @@ NR_API nr_status nr_ostr_objective(const nr_geom* g, const nr_ostr_params* p, co
                             w.red_n, out, as_stream(stream));
 }
 
+NR_API nr_status nr_ostr_project_fp64(const nr_geom* g, const nr_ostr_params* p, const float* x,
+                                      int32_t subset, double* data_out, void* workspace,
+                                      size_t ws_bytes, void* stream) {
+    Layout L;
+    nr_status st = check_ws(g, p, workspace, ws_bytes, &L);
+    if (st != NR_OK) return st;
+    if (!x || !data_out || subset < 0 || subset >= p->subset_num) return NR_ERR_BAD_ARGUMENT;
+    WS w = carve(workspace, L);
+    const int Vs = g->n_angles / p->subset_num;
+    return launch_fp_h_data(*g, p->fp_batch, x, w.h, w.angles, w.index, subset * Vs, Vs, w.y,
+                            w.b, w.r, w.red, w.red_n, data_out, as_stream(stream));
+}
+
+NR_API nr_status nr_ostr_penalty(const nr_geom* g, const nr_ostr_params* p, const float* x,
+                                 double* out, void* workspace, size_t ws_bytes, void* stream) {
+    Layout L;
+    nr_status st = check_ws(g, p, workspace, ws_bytes, &L);
+    if (st != NR_OK) return st;
+    if (!x || !out) return NR_ERR_BAD_ARGUMENT;
+    WS w = carve(workspace, L);
+    return launch_penalty(*g, p->potential, p->delta, x, w.red, w.red_n, out, as_stream(stream));
+}
+
 NR_API nr_status nr_ostr_check(void* workspace, size_t ws_bytes, int32_t* flags, void* stream) {
     if (!workspace || ws_bytes < 256 || !flags) return NR_ERR_BAD_ARGUMENT;
     cudaStream_t s = as_stream(stream);
@@ -412,6 +465,13 @@ NR_API nr_status nr_ostr_check(void* workspace, size_t ws_bytes, int32_t* flags,
     if (v & NR_FLAG_TIMEOUT) return NR_ERR_TIMEOUT;
     if (v & NR_FLAG_NONFINITE) return NR_ERR_NONFINITE;
     return NR_OK;
+}
+
+NR_API nr_status nr_test_expire_wait(void* workspace, int32_t wait_index, void* stream) {
+    if (!workspace || ((uintptr_t)workspace & 255) != 0) return NR_ERR_BAD_ARGUMENT;
+    set_word_kernel<<<1, 1, 0, as_stream(stream)>>>((int*)workspace + 1,
+                                                   wait_index < 0 ? 0 : wait_index + 1);
+    return launch_status();
 }
 
 NR_API const char* nr_version(void) { return "nrgb300 0.1.0 sm_103a"; }

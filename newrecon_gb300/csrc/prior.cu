@@ -179,11 +179,19 @@ template <int POT, int ZC>
 static nr_status launch_update_t(const nr_geom& g, int tile, const float* x, float* x_out, const float* d,
                                  const float* h, const float* angles, const int32_t* index,
                                  const BpTab& T, int a0, int nv, float M, float beta,
-                                 float delta, int* status, cudaStream_t st) {
+                                 float delta, int* status, const CUtensorMap* map,
+                                 cudaStream_t st) {
     dim3 blk(UTX, UTY), grd(cdiv(g.nx, UTX), cdiv(g.ny, UTY), cdiv(g.nz, ZC));
     const Geo G = make_geo(g);
     const PriorW5 W = make_w5(g.vz / g.vx, delta);
-    if (nv == 1 && tile == NR_TILE_2) {
+    if (tile == NR_TILE_TMA && map) {
+        if (nv == 1)
+            update_tma_kernel<POT, ZC, 1><<<grd, blk, 0, st>>>(
+                G, W, *map, x_out, d, h, angles, index, T, a0, nv, M, beta, delta, status);
+        else
+            update_tma_kernel<POT, ZC, 0><<<grd, blk, 0, st>>>(
+                G, W, *map, x_out, d, h, angles, index, T, a0, nv, M, beta, delta, status);
+    } else if (nv == 1 && tile == NR_TILE_2) {
         dim3 g2(cdiv(g.nx, U2X), cdiv(g.ny, UTY), cdiv(g.nz, ZC));
         update_x2_kernel<POT, ZC, 1><<<g2, blk, 0, st>>>(G, W, x, x_out, d, h, angles, index, T, a0,
                                                        nv, M, beta, delta, status);
@@ -200,38 +208,39 @@ template <int POT>
 static nr_status launch_update_z(const nr_geom& g, int zc, int tile, const float* x, float* x_out,
                                  const float* d, const float* h, const float* angles,
                                  const int32_t* index, const BpTab& T, int a0, int nv, float M,
-                                 float beta, float delta, int* status, cudaStream_t st) {
+                                 float beta, float delta, int* status, const CUtensorMap* map,
+                                 cudaStream_t st) {
     switch (zc) {
     case 8:
         return launch_update_t<POT, 8>(g, tile, x, x_out, d, h, angles, index, T, a0, nv, M, beta, delta,
-                                       status, st);
+                                       status, map, st);
     case 32:
         return launch_update_t<POT, 32>(g, tile, x, x_out, d, h, angles, index, T, a0, nv, M, beta, delta,
-                                        status, st);
+                                        status, map, st);
     default:
         return launch_update_t<POT, 16>(g, tile, x, x_out, d, h, angles, index, T, a0, nv, M, beta, delta,
-                                        status, st);
+                                        status, map, st);
     }
 }
 
 nr_status launch_update(const nr_geom& g, int pot, int zc, int tile, const float* x, float* x_out,
                         const float* d, const float* h, const float* angles, const int32_t* index,
                         const BpTab& T, int a0, int nv, float M, float beta, float delta,
-                        int* status, cudaStream_t st) {
+                        int* status, const CUtensorMap* map, cudaStream_t st) {
     if (nv > UPD_VIEWS_SMEM) return NR_ERR_BAD_ARGUMENT;
     switch (pot) {
     case NR_POT_Q2:
         return launch_update_z<NR_POT_Q2>(g, zc, tile, x, x_out, d, h, angles, index, T, a0, nv, M, beta,
-                                          delta, status, st);
+                                          delta, status, map, st);
     case NR_POT_LANGE:
         return launch_update_z<NR_POT_LANGE>(g, zc, tile, x, x_out, d, h, angles, index, T, a0, nv, M, beta,
-                                             delta, status, st);
+                                             delta, status, map, st);
     case NR_POT_HYPERBOLA:
         return launch_update_z<NR_POT_HYPERBOLA>(g, zc, tile, x, x_out, d, h, angles, index, T, a0, nv, M,
-                                                 beta, delta, status, st);
+                                                 beta, delta, status, map, st);
     case NR_POT_HUBER:
         return launch_update_z<NR_POT_HUBER>(g, zc, tile, x, x_out, d, h, angles, index, T, a0, nv, M, beta,
-                                             delta, status, st);
+                                             delta, status, map, st);
     default: return NR_ERR_BAD_ARGUMENT;
     }
 }

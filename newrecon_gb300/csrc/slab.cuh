@@ -20,14 +20,16 @@
 // are accumulated in the same order with the same arithmetic -- the result is
 // bit-identical to fp_h_kernel's.  Shared-memory indices are kept
 // incrementally with the box's strides and clamped into the buffer, so no
-// access can leave it.  Every mbarrier wait is bounded; a wait that gives up
-// sets NR_FLAG_TIMEOUT and waits once more before the block moves on.
+// access can leave it.  Every mbarrier wait is bounded: when one gives up
+// twice, the block sets NR_FLAG_TIMEOUT, issues no further copy and walks
+// the remaining slabs from global memory (the result is still right), and
+// before it exits it waits, bounded, for the copies it had issued.
 #pragma once
 
 #include <cuda.h>
 
 #include "project.cuh"
-#include "tc.cuh"
+#include "tma.cuh"
 
 namespace nr {
 
@@ -46,25 +48,6 @@ struct SlabCfg {
 struct SlabBox {
     int x0, y0, zlo, zhi, fits;
 };
-
-__device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, int x, int y,
-                                            int z, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(tc::smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(tc::smem_u32(bar))
-        : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(bar)) : "memory");
-}
 
 // Slab q's planes, walking down (dir < 0: from the top) or up.
 template <int SZ>
@@ -221,13 +204,35 @@ __device__ __forceinline__ void fp_h_slab_tile(const Geo& G, const CUtensorMap* 
         ty = R.ay.first;
         tz = R.az.first;
     }
+    // staged: the block still reads slabs from shared memory.  It turns false
+    // (for every thread at once) when a wait gave up twice in some thread;
+    // from then on the walk reads the volume from global memory and no copy
+    // is issued again, so no buffer whose copy is unaccounted for is reused.
+    // Test hook: the workspace's second status word k + 1 > 0 makes the wait
+    // for slab k report giving up once it has in fact succeeded.
+    bool staged = true;
+    int failed_at = nslab;
+    const int force_at = status[1] - 1;
     for (int q = 0; q < nslab; q++) {
         const int buf = q & 1;
-        if (!tc::mbar_wait(&bar[buf], (q >> 1) & 1, SLAB_WAIT)) {
-            if (tid == 0) atomicOr(status, NR_FLAG_TIMEOUT);
-            tc::mbar_wait(&bar[buf], (q >> 1) & 1, SLAB_WAIT);
+        if (staged) {
+            bool got = tc::mbar_wait(&bar[buf], (q >> 1) & 1, SLAB_WAIT) ||
+                       tc::mbar_wait(&bar[buf], (q >> 1) & 1, SLAB_WAIT);
+            if (q == force_at) got = false;
+            staged = __syncthreads_and(got) != 0;
+            if (!staged) {
+                failed_at = q;
+                if (tid == 0) atomicOr(status, NR_FLAG_TIMEOUT);
+            }
         }
-        const SlabBox bx = box[buf];
+        SlabBox bx;
+        if (staged) {
+            bx = box[buf];
+        } else {  // the slab's planes, read from global memory
+            slab_planes<SZ>(q, g.nz, down, &bx.zlo, &bx.zhi);
+            bx.x0 = bx.y0 = 0;
+            bx.fits = 0;
+        }
         if (hit && s < R.smax) {
             // the voxel the walk is in
             const int ix = R.ax.idx + R.ax.dir * (int)cx;
@@ -257,10 +262,17 @@ __device__ __forceinline__ void fp_h_slab_tile(const Geo& G, const CUtensorMap* 
             }
         }
         __syncthreads();  // buffer `buf` is free again
-        if (tid == 0 && q + 2 < nslab) {
+        if (tid == 0 && staged && q + 2 < nslab) {
             tc::fence_async_smem();
             slab_issue<SZ>(g, src, map, q + 2, down, i0, i1, j0, j1, sbuf, box, bar, buf);
         }
+    }
+    if (tid == 0 && failed_at < nslab) {
+        // the copies issued but not waited for (slabs failed_at and
+        // failed_at + 1) must land before the block's shared memory goes
+        for (int q = failed_at; q < min(failed_at + 2, nslab); q++)
+            if (!tc::mbar_wait(&bar[q & 1], (q >> 1) & 1, SLAB_WAIT))
+                tc::mbar_wait(&bar[q & 1], (q >> 1) & 1, SLAB_WAIT);
     }
     if (!active) return;
     const float l = hit ? sum * src.ct : 0.f;

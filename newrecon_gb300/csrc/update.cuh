@@ -10,6 +10,7 @@
 #include <cmath>
 
 #include "common.cuh"
+#include "tma.cuh"
 
 namespace nr {
 
@@ -146,7 +147,7 @@ __device__ __forceinline__ void nb_terms(f32x2 t2, const PriorW5& W, float delta
 // difference, the weight product and both accumulations of every second
 // neighbour (5 instead of 7 instructions per Huber term, 5.5 instead of 8 per
 // hyperbola term; measured 5 % / 8 % off the update).
-template <int POT, bool EDGE, int KA, int KB>
+template <int POT, bool EDGE, int KA, int KB, int RW = USW>
 __device__ __forceinline__ void nb_pair(const float* __restrict__ pb, const float* __restrict__ pc,
                                         const float* __restrict__ pa, int base, f32x2 xc2,
                                         const PriorW5& W, float delta, float inv_delta,
@@ -156,21 +157,23 @@ __device__ __forceinline__ void nb_pair(const float* __restrict__ pb, const floa
     static_assert(nb_class<KA>() == nb_class<KB>(), "one weight class");
     const float* pla = dza < 0 ? pb : (dza == 0 ? pc : pa);
     const float* plb = dzb < 0 ? pb : (dzb == 0 ? pc : pa);
-    const f32x2 t2 = sub2(xc2, pk2(pla[base + dya * USW + dxa], plb[base + dyb * USW + dxb]));
+    const f32x2 t2 = sub2(xc2, pk2(pla[base + dya * RW + dxa], plb[base + dyb * RW + dxb]));
     nb_terms<POT, EDGE, nb_class<KA>()>(t2, W, delta, inv_delta, sdd, sd);
 }
 
 // The 26 neighbours as 13 equal-weight pairs: (dx = -1, dx = +1) of each
-// (dy, dz) row, and the dx = 0 cells paired across dy or dz.
-template <int POT, bool EDGE>
-__device__ __forceinline__ void prior_pairs(const float* __restrict__ pb,
-                                            const float* __restrict__ pc,
-                                            const float* __restrict__ pa, int base, float xc,
-                                            const PriorW5& W, float delta, float inv_delta,
-                                            float* rdd, float* rd) {
+// (dy, dz) row, and the dx = 0 cells paired across dy or dz.  RW: floats per
+// row of the staged planes.
+template <int POT, bool EDGE, int RW>
+__device__ __forceinline__ void prior_pairs_w(const float* __restrict__ pb,
+                                              const float* __restrict__ pc,
+                                              const float* __restrict__ pa, int base, float xc,
+                                              const PriorW5& W, float delta, float inv_delta,
+                                              float* rdd, float* rd) {
     const f32x2 xc2 = pk2(xc, xc);
     f32x2 sdd = pk2(0.f, 0.f), sd = pk2(0.f, 0.f);
-#define NR_PAIR(a, b) nb_pair<POT, EDGE, a, b>(pb, pc, pa, base, xc2, W, delta, inv_delta, sdd, sd)
+#define NR_PAIR(a, b) \
+    nb_pair<POT, EDGE, a, b, RW>(pb, pc, pa, base, xc2, W, delta, inv_delta, sdd, sd)
     NR_PAIR(0, 2); NR_PAIR(3, 5); NR_PAIR(6, 8);      // dz = -1 rows
     NR_PAIR(9, 11); NR_PAIR(12, 14); NR_PAIR(15, 17); // dz = 0 rows
     NR_PAIR(18, 20); NR_PAIR(21, 23); NR_PAIR(24, 26);  // dz = +1 rows
@@ -181,6 +184,15 @@ __device__ __forceinline__ void prior_pairs(const float* __restrict__ pb,
     upk2(sd, b0, b1);
     *rdd = a0 + a1;
     *rd = b0 + b1;
+}
+
+template <int POT, bool EDGE>
+__device__ __forceinline__ void prior_pairs(const float* __restrict__ pb,
+                                            const float* __restrict__ pc,
+                                            const float* __restrict__ pa, int base, float xc,
+                                            const PriorW5& W, float delta, float inv_delta,
+                                            float* rdd, float* rd) {
+    prior_pairs_w<POT, EDGE, USW>(pb, pc, pa, base, xc, W, delta, inv_delta, rdd, rd);
 }
 
 // Kinds of fused update (template argument KIND of update_tile).
@@ -647,6 +659,165 @@ __global__ void __launch_bounds__(256, NV == 1 ? 5 : 0) update_x2_kernel(
     update_tile_x2<POT, ZC, UPD_OSTR, NV>(G, W, x, x_out, d, h, angles, index, T, a0, nv, M,
                                           beta, delta, status, blockIdx.x, blockIdx.y,
                                           blockIdx.z, sm);
+}
+
+
+// ---- TMA-fed ring -----------------------------------------------------------
+// The one-voxel tile with its planes streamed by TMA instead of through the
+// threads' registers: lane 0 of warp 0 loads each plane of the tile with its
+// halo (one cp.async.bulk.tensor.3d box of UTW x USH voxels starting 4 voxels
+// left of the tile, so that the box's x coordinate is a multiple of 4 floats;
+// out-of-volume voxels read as NaN, the ring's convention for "outside") into
+// a ring of UT_SLOTS slots, each with a "full" mbarrier (the copy landed) and
+// an "empty" one (all eight warps are done with the plane).  Each warp runs
+// update_tile's arithmetic on its row of the tile, plane by plane, waiting
+// only for the plane it needs next: there is no block-wide barrier per
+// plane, so a warp held up by its back-projection loads does not hold the
+// others up, and up to UT_SLOTS - 3 planes are in flight ahead of the
+// slowest warp.  Warp 0 refills a slot once every warp is done with it.
+// Results are bit-identical to update_tile's (same sums in the same order).
+//
+// Every wait is bounded.  A wait that gives up flags NR_FLAG_TIMEOUT, after
+// which that thread waits no more (the tile's output is then not to be
+// used; the host reads the flag as NR_ERR_TIMEOUT).  Once the issuing lane
+// has given up it issues no further copy, so no slot whose readers are
+// unaccounted for is refilled, and before it exits it waits (bounded) for
+// every copy it issued, so none is in flight when the block's shared memory
+// is released.  A first version with a ninth, producer-only warp held 7
+// blocks per SM instead of 8 and ran 11 % slower on the clinical workload.
+constexpr int UTW = UTX + 8;            // columns of a staged row: x0 - 4 .. x0 + 35
+constexpr int UT_SLOT = 416;            // floats per slot: UTW x USH = 400, rounded to 128 B
+constexpr int UT_SLOTS = 6;
+constexpr uint32_t UT_BYTES = UTW * USH * 4;
+constexpr int UT_WAIT = 1 << 22;        // polls before a wait gives up
+static_assert(UTW * USH <= UT_SLOT && (UT_SLOT * 4) % 128 == 0, "slot size");
+
+struct UpdSmemT {
+    alignas(128) float ring[UT_SLOTS][UT_SLOT];
+    alignas(8) uint64_t full[UT_SLOTS];
+    uint64_t empty[UT_SLOTS];
+    ViewSrc sv[UPD_VIEWS_SMEM];
+};
+
+template <int POT, int ZC = UZC, int KIND = UPD_OSTR, int NV = 0>
+__device__ __forceinline__ void update_tile_tma(
+    const Geo& G, const PriorW5& W, const CUtensorMap* map, float* __restrict__ x_out,
+    const float* __restrict__ d, const float* __restrict__ h, const float* __restrict__ angles,
+    const int32_t* __restrict__ index, const BpTab& T, int a0, int nv, float M, float beta,
+    float delta, int* __restrict__ status, int bx, int by, int bz, UpdSmemT& sm) {
+    const nr_geom& g = G.g;
+    const int warp = threadIdx.y, lane = threadIdx.x;
+    const int tid = warp * UTX + lane;
+    for (int t = tid; t < (NV ? NV : nv); t += UTX * UTY)
+        sm.sv[t] = view_source(g, angles[index[a0 + t]]);
+    const int x0t = bx * UTX, y0t = by * UTY;
+    const int zb = bz * ZC, ze = min(zb + ZC, g.nz);
+    const int np = ze - zb + 2;  // planes zb - 1 .. ze; plane k is z = zb - 1 + k
+    const bool issuer = tid == 0;
+    bool issuing = true;         // the issuer: false once one of its waits gave up
+    int issued = 0;
+    auto issue = [&](int k) {    // plane k into slot k % UT_SLOTS (its last reader done)
+        const int s = k % UT_SLOTS;
+        tc::fence_async_smem();
+        mbar_arrive_tx(&sm.full[s], UT_BYTES);
+        tma_load_3d(&sm.ring[s][0], map, x0t - 4, y0t - 1, zb - 1 + k, &sm.full[s]);
+        issued = k + 1;
+    };
+    if (issuer) {
+        for (int s = 0; s < UT_SLOTS; s++) {
+            tc::mbar_init(&sm.full[s], 1);
+            tc::mbar_init(&sm.empty[s], UTY);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int k = 0; k < min(np, UT_SLOTS); k++) issue(k);
+    }
+    __syncthreads();
+    bool live = true;  // false after a wait of this thread gave up: it waits no more
+    // test hook: the workspace's second status word k + 1 > 0 makes the wait
+    // for plane k report giving up once it has in fact succeeded
+    const int force_at = status[1] - 1;
+    auto wait_full = [&](int k) {
+        if (live && (!tc::mbar_wait(&sm.full[k % UT_SLOTS], (k / UT_SLOTS) & 1, UT_WAIT) ||
+                     k == force_at)) {
+            if (lane == 0) atomicOr(status, NR_FLAG_TIMEOUT);
+            live = false;
+        }
+    };
+    const int ix = x0t + lane, iy = y0t + warp;
+    const bool active = ix < g.nx && iy < g.ny;
+    const bool edge_xy = x0t == 0 || x0t + UTX >= g.nx || y0t == 0 || y0t + UTY >= g.ny;
+    const float inv_delta = 1.f / delta;
+    const int plane = g.nx * g.ny;
+    const int64_t B = (int64_t)g.nbx * g.nby;
+    const int base = (warp + 1) * UTW + lane + 4;
+    wait_full(0);
+    wait_full(1);
+    for (int z = zb; z < ze; z++) {
+        const int k = z - zb + 1;  // the centre plane's ring index
+        wait_full(k + 1);
+        const float* pb = sm.ring[(k - 1) % UT_SLOTS];
+        const float* pc = sm.ring[k % UT_SLOTS];
+        const float* pa = sm.ring[(k + 1) % UT_SLOTS];
+        if (active) {
+            const int v = z * plane + iy * g.nx + ix;
+            const float dv = KIND == UPD_OSTR ? __ldg(d + v) : 0.f;
+            const float xc = pc[base];
+            float capL = 0.f, sens = 0.f;
+            const float* p = h;
+            int tix = (a0 * g.nz + z) * g.nx + ix;
+            int tiy = (a0 * g.nz + z) * g.ny + iy;
+            const int sx = g.nz * g.nx, sy = g.nz * g.ny;
+            for (int t = 0; t < (NV ? NV : nv); t++, p += B, tix += sx, tiy += sy)
+                bp_view<KIND>(p, __ldg(T.x + tix), __ldg(T.y + tiy), sm.sv[t].s2, g, capL, sens);
+            float rdd = 0.f, rd = 0.f;
+            if (KIND != UPD_SART) {
+                if (edge_xy || z == 0 || z == g.nz - 1)
+                    prior_pairs_w<POT, true, UTW>(pb, pc, pa, base, xc, W, delta, inv_delta, &rdd,
+                                                  &rd);
+                else
+                    prior_pairs_w<POT, false, UTW>(pb, pc, pa, base, xc, W, delta, inv_delta,
+                                                   &rdd, &rd);
+            }
+            upd_store<KIND>(xc, capL, sens, rd, rdd, dv, M, beta, x_out + v, status);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.empty[(k - 1) % UT_SLOTS]);
+        // plane k - 1 + UT_SLOTS goes where plane k - 1 was, once every warp is done with it
+        const int kn = k - 1 + UT_SLOTS;
+        if (issuer && issuing && kn < np) {
+            if (tc::mbar_wait(&sm.empty[(k - 1) % UT_SLOTS], ((k - 1) / UT_SLOTS) & 1, UT_WAIT)) {
+                issue(kn);
+            } else {
+                atomicOr(status, NR_FLAG_TIMEOUT);
+                issuing = false;
+            }
+        }
+    }
+    if (issuer) {
+        // no copy may be in flight when the block exits
+        for (int k = max(0, issued - UT_SLOTS); k < issued; k++) {
+            const int s = k % UT_SLOTS;
+            if (!tc::mbar_wait(&sm.full[s], (k / UT_SLOTS) & 1, UT_WAIT)) {
+                atomicOr(status, NR_FLAG_TIMEOUT);
+                tc::mbar_wait(&sm.full[s], (k / UT_SLOTS) & 1, UT_WAIT);
+            }
+        }
+    }
+}
+
+// One block per (x, y) tile and chunk of ZC planes, 8 warps (one row each);
+// one-view kernels held to 32 registers (8 resident blocks per SM).
+template <int POT, int ZC, int NV>
+__global__ void __launch_bounds__(256, NV == 1 ? 8 : 0) update_tma_kernel(
+    const __grid_constant__ Geo G, const __grid_constant__ PriorW5 W,
+    const __grid_constant__ CUtensorMap map, float* __restrict__ x_out,
+    const float* __restrict__ d, const float* __restrict__ h, const float* __restrict__ angles,
+    const int32_t* __restrict__ index, const __grid_constant__ BpTab T, int a0, int nv,
+    float M, float beta, float delta, int* __restrict__ status) {
+    __shared__ UpdSmemT sm;
+    update_tile_tma<POT, ZC, UPD_OSTR, NV>(G, W, &map, x_out, d, h, angles, index, T, a0, nv, M,
+                                           beta, delta, status, blockIdx.x, blockIdx.y,
+                                           blockIdx.z, sm);
 }
 
 }  // namespace nr

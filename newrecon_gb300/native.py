@@ -55,6 +55,9 @@ SIGNATURES = {
     "nr_objective_fp64": (_I32, [_GP, _PP, _P, _P, _P, ctypes.c_size_t, _P]),
     "nr_workspace_size": (_I32, [_GP, _PP, ctypes.POINTER(ctypes.c_size_t)]),
     "nr_ostr_project": (_I32, [_GP, _PP, _P, _I32, _P, ctypes.c_size_t, _P]),
+    "nr_ostr_project_fp64": (_I32, [_GP, _PP, _P, _I32, _P, _P, ctypes.c_size_t, _P]),
+    "nr_ostr_penalty": (_I32, [_GP, _PP, _P, _P, _P, ctypes.c_size_t, _P]),
+    "nr_test_expire_wait": (_I32, [_P, _I32, _P]),
     "nr_ostr_update": (_I32, [_GP, _PP, _P, _P, _I32, _P, ctypes.c_size_t, _P]),
     "nr_ostr_workspace_section": (_I32, [_GP, _PP, _I32, _P, ctypes.c_size_t,
                                          ctypes.POINTER(ctypes.c_void_p),

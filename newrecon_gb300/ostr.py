@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import time
 from typing import Optional, Tuple
 
 import numpy as np
@@ -370,10 +371,12 @@ class OSTR:
         """stage=True stages the projection's volume slab by slab in shared
         memory by TMA instead of gathering it through L1/L2 (same result;
         slower on the clinical workload).  upd_tile=1 gives each thread of the
-        update two voxels side by side in x (one-view subsets; same result bit
-        for bit).  autotune() picks both per geometry."""
-        if upd_tile not in (0, 1):
-            raise ValueError("upd_tile must be 0 (one voxel per thread) or 1 (two)")
+        update two voxels side by side in x (one-view subsets); upd_tile=2
+        streams the update's planes by TMA through a shared-memory ring filled
+        by a producer warp (where IMGSIZx is a multiple of 4).  Every variant
+        gives the same result bit for bit.  autotune() picks them per geometry."""
+        if upd_tile not in (0, 1, 2):
+            raise ValueError("upd_tile must be 0 (one voxel per thread), 1 (two) or 2 (TMA ring)")
         geom.validate(subset_num)
         self.geom = geom
         self.params = NrOstrParams(int(subset_num), int(POTENTIALS[potential]),
@@ -384,6 +387,8 @@ class OSTR:
         self.gc = geom.to_c()
         self.history = None      # objectives of a monotone iterate()
         self.rejected_at = None  # the iteration a monotone iterate() undid
+        self.subset_history = None  # per sub-iteration record of monotone="subset"
+        self.rejected_steps = 0
         size = ctypes.c_size_t(0)
         native.call("nr_ostr_workspace_size", ctypes.byref(self.gc), ctypes.byref(self.params),
                     ctypes.byref(size))
@@ -407,7 +412,7 @@ class OSTR:
                     _p(y), _p(b), _p(s), ws, n, _stream())
         self._keep = (ang, y, b, s)
 
-    def iterate(self, x: torch.Tensor, n_iters: int, monotone: bool = False) -> torch.Tensor:
+    def iterate(self, x: torch.Tensor, n_iters: int, monotone=False) -> torch.Tensor:
         """n_iters iterations (every subset once each) on x in place.
 
         monotone=True accepts an iteration only if it does not raise the FP64
@@ -417,7 +422,22 @@ class OSTR:
         ``history`` then holds the objectives of the accepted iterates (the
         start included) and ``rejected_at`` the rejected iteration, or None.
         Each check costs one objective evaluation (a projection of all views
-        and the penalty)."""
+        and the penalty).
+
+        monotone="subset" decides every sub-iteration instead: the step of
+        subset a from x to x' is kept only if it does not raise the FP64
+        subset objective M L_a + beta R (L_a the data term of subset a's
+        views, M the subset count, R the penalty); otherwise x stays and the
+        loop goes on with the next subset.  L_a(x) comes from the projection
+        that makes the step's gradient (nr_ostr_project_fp64); each check adds
+        the projection of the subset's views at x' and one penalty
+        evaluation.  ``subset_history`` holds (iteration, subset, before,
+        after, kept) per sub-iteration and ``rejected_steps`` the count of
+        steps not kept."""
+        if monotone == "subset":
+            return self._iterate_subset_monotone(x, n_iters)
+        if monotone not in (False, True):
+            raise ValueError('monotone must be False, True or "subset"')
         ws, n = self._ws()
         if not monotone:
             native.call("nr_ostr_iterate", ctypes.byref(self.gc), ctypes.byref(self.params),
@@ -438,6 +458,59 @@ class OSTR:
             hist.append(f)
         self.history = hist
         return x
+
+    def _iterate_subset_monotone(self, x: torch.Tensor, n_iters: int) -> torch.Tensor:
+        M = int(self.params.subset_num)
+        beta = float(self.params.beta)
+        xn = torch.empty_like(x)
+        vals = torch.zeros(3, dtype=torch.float64, device=x.device)
+        self.penalty(x, vals[2:3])
+        pen_x = float(vals[2].item())
+        log = []
+        for k in range(int(n_iters)):
+            for a in range(M):
+                self.project_fp64(x, a, vals[0:1])      # h and L_a(x)
+                self.update(x, xn, a)
+                self.project_fp64(xn, a, vals[1:2])     # L_a(x')
+                self.penalty(xn, vals[2:3])             # R(x')
+                before_data, after_data, pen_new = (float(v) for v in vals.cpu())
+                before, after = self._subset_values(M * before_data + beta * pen_x,
+                                                    M * after_data + beta * pen_new)
+                kept = after <= before
+                if kept:
+                    x.copy_(xn)
+                    pen_x = pen_new
+                log.append((k, a, before, after, kept))
+        self.subset_history = log
+        self.rejected_steps = sum(1 for e in log if not e[4])
+        return x
+
+    @staticmethod
+    def _subset_values(before: float, after: float) -> Tuple[float, float]:
+        """The subset objectives a monotone="subset" step is judged by (a seam
+        for tests that plant a rising step on the host)."""
+        return before, after
+
+    def project_fp64(self, x: torch.Tensor, subset: int,
+                     out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """Fused FP + h of one subset into the workspace, as project(), and the
+        subset's FP64 data term into out (one device double; returned)."""
+        if out is None:
+            out = torch.zeros(1, dtype=torch.float64, device=x.device)
+        ws, n = self._ws()
+        native.call("nr_ostr_project_fp64", ctypes.byref(self.gc), ctypes.byref(self.params),
+                    _p(x), int(subset), _p(out), ws, n, _stream())
+        return out
+
+    def penalty(self, x: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """The FP64 penalty R(x) (objective()'s second part) into out (one
+        device double; returned)."""
+        if out is None:
+            out = torch.zeros(1, dtype=torch.float64, device=x.device)
+        ws, n = self._ws()
+        native.call("nr_ostr_penalty", ctypes.byref(self.gc), ctypes.byref(self.params), _p(x),
+                    _p(out), ws, n, _stream())
+        return out
 
     def subiter(self, x: torch.Tensor, subset: int) -> torch.Tensor:
         ws, n = self._ws()
@@ -568,7 +641,7 @@ class Batch:
                 plan.autotune(x)
             if "upd_planes" in c:  # an explicit slab depth (8, 16 or 32) wins
                 plan.params.upd_planes = int(c["upd_planes"])
-            if "upd_tile" in c:    # and an explicit update tile (0 or 1)
+            if "upd_tile" in c:    # and an explicit update tile (0, 1 or 2)
                 plan.params.upd_tile = int(c["upd_tile"])
             self.plans.append(plan)
             self.x.append(x)
@@ -639,20 +712,27 @@ class BatchGraph:
 
 def reconstruct(geom: Geometry, prj, blank, scatter=None, *, angles, subset_num: int,
                 iter_num: int, beta: float, delta: float, potential: str = "lange",
-                gamma_mode: str = "length", x0=None, monotone: bool = False,
-                tune="cached", stream=None):
+                gamma_mode: str = "length", x0=None, monotone=False,
+                tune="cached", stream=None, timing: Optional[dict] = None):
     """OSTR reconstruction: transmission counts in, attenuation (1/mm) out.
 
     prj, blank, scatter: [view][i][j] in original view order (the layout
     load_prj produces).  Returns the volume [z][y][x]; numpy when prj was a
     host array, else a CUDA tensor.  monotone=True stops before the first
-    iteration that would raise the FP64 objective (OSTR.iterate).  tune:
+    iteration that would raise the FP64 objective; monotone="subset" keeps
+    only the sub-iteration steps that do not raise the FP64 subset objective
+    (OSTR.iterate).  tune:
     "cached" runs the kernel variants the autotuner cached for this GPU and
     geometry (the defaults when it has none), True tunes first when the
     cache has none, False runs the defaults.  Every variant gives the same
     result bit for bit.  stream: a torch.cuda.Stream to run every copy and
     kernel on (default: the current stream).  The call returns once that
     stream has finished the reconstruction (the status check waits for it).
+    timing: a dict that receives the device time of each phase in seconds
+    (CUDA events on the stream): "upload_s" (host to device copies of the
+    counts, blank scan, angles and x0), "setup_s" (gamma and d), "iterate_s"
+    (the iterations), "download_s" (the status check and the volume's copy
+    back), and "wall_s", the host's clock around the whole call.
     """
     if not (tune == "cached" or tune is True or tune is False):
         raise ValueError('tune must be "cached", True or False')
@@ -662,20 +742,41 @@ def reconstruct(geom: Geometry, prj, blank, scatter=None, *, angles, subset_num:
         with torch.cuda.stream(stream):
             return reconstruct(geom, prj, blank, scatter, angles=angles, subset_num=subset_num,
                                iter_num=iter_num, beta=beta, delta=delta, potential=potential,
-                               gamma_mode=gamma_mode, x0=x0, monotone=monotone, tune=tune)
+                               gamma_mode=gamma_mode, x0=x0, monotone=monotone, tune=tune,
+                               timing=timing)
+    t_wall = time.perf_counter()
+    ev = None
+    if timing is not None:
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
     plan = OSTR(geom, subset_num=subset_num, beta=beta, delta=delta, potential=potential,
                 gamma_mode=gamma_mode, has_scatter=scatter is not None)
-    plan.setup(angles, prj, blank, scatter)
+    if ev:
+        ev[0].record()
+    ang, y, b = _in(angles), _in(prj), _in(blank)
+    s = None if scatter is None else _in(scatter)
+    x = None if x0 is None else _in(x0).clone()
+    if ev:
+        ev[1].record()
+    plan.setup(ang, y, b, s)
     if tune is True:
         plan.autotune()
     elif tune == "cached":
         from . import autotune
 
         autotune.apply_cached(plan)
-    if x0 is None:
+    if x is None:
         x = torch.zeros(geom.n_voxels, dtype=torch.float32, device=plan.ws.device)
-    else:
-        x = _in(x0).clone()
+    if ev:
+        ev[2].record()
     plan.iterate(x, iter_num, monotone=monotone)
+    if ev:
+        ev[3].record()
     plan.check()
-    return _like_input(prj, x)
+    out = _like_input(prj, x)
+    if ev:
+        ev[4].record()
+        ev[4].synchronize()
+        for k, name in enumerate(("upload_s", "setup_s", "iterate_s", "download_s")):
+            timing[name] = ev[k].elapsed_time(ev[k + 1]) / 1e3
+        timing["wall_s"] = time.perf_counter() - t_wall
+    return out

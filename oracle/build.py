@@ -14,7 +14,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 ORACLE_SO = os.path.join(BUILD_DIR, "libostr_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libostr_ref.so")
-REFERENCE_DIR = os.environ.get("NR_REFERENCE_DIR", "/root/reference")
+# The reference sources: NR_REFERENCE_DIR, else a checkout named "reference"
+# beside this repository.
+REFERENCE_DIR = os.environ.get(
+    "NR_REFERENCE_DIR", os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 
 def oracle_cmd():

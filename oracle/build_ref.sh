@@ -21,8 +21,10 @@
 # helper_cuda.h are absent from the reference, so their includes (the first
 # lines of each file) are skipped.
 set -euo pipefail
-REF="${NR_REFERENCE_DIR:-/root/reference}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
+# the reference sources: NR_REFERENCE_DIR, else a checkout named "reference"
+# beside this repository
+REF="${NR_REFERENCE_DIR:-$(dirname "$(dirname "$HERE")")/reference}"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/Tomo_OSTR.cu" ] || [ ! -f "$REF/Tomo_OSTR_gold.cpp" ]; then
     echo "build_ref: reference sources not found under $REF" >&2

@@ -477,7 +477,11 @@ inline double psi(int pot, double t, double delta) {
     switch (pot) {
     case NR_POT_Q2: return 0.5 * t * t;
     case NR_POT_LANGE: return delta * delta * (a / delta - std::log1p(a / delta));
-    case NR_POT_HYPERBOLA: return delta * delta * (std::sqrt(1.0 + (t / delta) * (t / delta)) - 1.0);
+    case NR_POT_HYPERBOLA: {
+        // d^2 (sqrt(1+u^2) - 1) in the form without cancellation for small u
+        const double u2 = (t / delta) * (t / delta);
+        return delta * delta * (u2 / (std::sqrt(1.0 + u2) + 1.0));
+    }
     default: return a <= delta ? 0.5 * t * t : delta * a - 0.5 * delta * delta;
     }
 }

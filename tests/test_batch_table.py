@@ -98,7 +98,7 @@ def test_prepare_rejects_bad_cases(native):
                     None)
     assert e.value.code == 2
     arr[1].p.upd_planes = 32
-    arr[1].p.upd_tile = 2  # not an update tile
+    arr[1].p.upd_tile = 3  # not an update tile
     with pytest.raises(NrError) as e:
         native.call("nr_batch_prepare", arr, 2, ctypes.c_void_p(ptr), size, ctypes.byref(steps),
                     None)

@@ -98,13 +98,14 @@ def test_contract_names_alias_the_fused_entry_points(native):
 
 
 def test_update_tile_choice_is_checked(native):
-    """upd_tile takes NR_TILE_1 (0) or NR_TILE_2 (1); anything else is refused."""
+    """upd_tile takes NR_TILE_1 (0), NR_TILE_2 (1) or NR_TILE_TMA (2); anything
+    else is refused."""
     from newrecon_gb300.geometry import NrOstrParams, config
 
     lib = native.load()
     gc = config("small").geom.to_c()
     size = ctypes.c_size_t(0)
-    for tile, ok in ((0, True), (1, True), (2, False), (-1, False)):
+    for tile, ok in ((0, True), (1, True), (2, True), (3, False), (-1, False)):
         p = NrOstrParams(9, 2, 0, 0, 50.0, 0.002)
         p.upd_tile = tile
         st = lib.nr_ostr_workspace_size(ctypes.byref(gc), ctypes.byref(p), ctypes.byref(size))

@@ -1,10 +1,13 @@
-"""The two-voxel update tile (upd_tile = 1) against the one-voxel tile.
+"""The alternative update tiles against the one-voxel tile: the two-voxel tile
+(upd_tile = 1) and the TMA-fed ring (upd_tile = 2, a producer warp streaming
+the planes into shared memory, consumer warps synchronised by mbarriers).
 
-Each voxel's sums are formed in the same order and grouping by both tiles, so
+Each voxel's sums are formed in the same order and grouping by every tile, so
 the bar is bit-identical volumes after whole OSTR iterations, for every
-potential, on shapes that leave partly filled 64-column tiles, odd column
-counts (a thread whose second voxel is outside the volume), a single column,
-and slab chunks cut short in z.  The oracle parity of the one-voxel tile is
+potential, on shapes that leave partly filled tiles, odd column counts (a
+thread whose second voxel is outside the volume; a row the TMA form cannot
+describe, where it falls back to the one-voxel tile), a single column, and
+slab chunks cut short in z.  The oracle parity of the one-voxel tile is
 covered by test_gpu_recon.py.
 """
 import numpy as np
@@ -14,7 +17,7 @@ import torch
 pytestmark = pytest.mark.gpu
 
 SHAPES = [(203, 77, 13), (65, 9, 5), (1, 1, 3), (2, 3, 4), (64, 8, 16), (130, 17, 33),
-          (127, 40, 7)]
+          (127, 40, 7), (128, 40, 7), (36, 9, 5), (4, 3, 4), (100, 17, 33)]
 
 
 @pytest.fixture(scope="module")
@@ -51,8 +54,9 @@ def run(mod, g, angles, y, b, iters, pot, beta, delta, tile, planes=0):
     return x
 
 
+@pytest.mark.parametrize("tile", [1, 2])
 @pytest.mark.parametrize("shape", SHAPES)
-def test_two_voxel_tile_is_bit_identical(mod, shape):
+def test_alternative_tile_is_bit_identical(mod, shape, tile):
     from newrecon_gb300.geometry import Geometry, view_angles
 
     nx, ny, nz = shape
@@ -62,12 +66,13 @@ def test_two_voxel_tile_is_bit_identical(mod, shape):
     for pot in ("q2", "lange", "hyperbola", "huber"):
         for planes in (8, 16, 32):
             a = run(mod, g, angles, y, b, 2, pot, 20.0, 0.01, 0, planes)
-            c = run(mod, g, angles, y, b, 2, pot, 20.0, 0.01, 1, planes)
+            c = run(mod, g, angles, y, b, 2, pot, 20.0, 0.01, tile, planes)
             assert torch.isfinite(a).all()
             assert torch.equal(a, c), (shape, pot, planes, float((a - c).abs().max()))
 
 
-def test_two_voxel_tile_clinical(mod):
+@pytest.mark.parametrize("tile", [1, 2])
+def test_alternative_tile_clinical(mod, tile):
     """One iteration (25 sub-iterations) of the clinical workload, both tiles."""
     from newrecon_gb300.geometry import config
     from newrecon_gb300.phantom import breast_phantom, poisson_counts
@@ -84,26 +89,29 @@ def test_two_voxel_tile_clinical(mod):
     y = torch.from_numpy(poisson_counts(line.cpu().numpy(), cfg.I0, 1)).cuda()
     b = torch.full_like(y, cfg.I0)
     a = run(mod, g, cfg.angles, y, b, 1, cfg.potential, cfg.beta, cfg.delta, 0)
-    c = run(mod, g, cfg.angles, y, b, 1, cfg.potential, cfg.beta, cfg.delta, 1)
+    c = run(mod, g, cfg.angles, y, b, 1, cfg.potential, cfg.beta, cfg.delta, tile)
     assert torch.equal(a, c)
     assert float(a.abs().max()) > 0
 
 
-def test_two_voxel_tile_falls_back_for_many_view_subsets(mod):
-    """With several views per subset the plan runs the one-voxel tile."""
+@pytest.mark.parametrize("nx", [70, 72])
+def test_many_view_subsets(mod, nx):
+    """With several views per subset the two-voxel tile falls back to the
+    one-voxel tile, and the TMA-fed ring runs its view loop (nx = 72) or
+    falls back too (nx = 70: rows of 280 bytes cannot be described)."""
     from newrecon_gb300.geometry import Geometry, view_angles
 
-    g = Geometry.dbt(70, 20, 9, 0.5, 1.0, 80, 26, 0.5, 6)
+    g = Geometry.dbt(nx, 20, 9, 0.5, 1.0, 80, 26, 0.5, 6)
     angles = view_angles(6, 15.0)
     y, b = scan(mod, g, angles, 5)
     out = []
-    for tile in (0, 1):
+    for tile in (0, 1, 2):
         plan = mod.OSTR(g, subset_num=3, beta=20.0, delta=0.01, potential="huber", upd_tile=tile)
         plan.setup(angles, y, b)
         x = torch.zeros(g.n_voxels, dtype=torch.float32, device="cuda")
         plan.iterate(x, 2)
         out.append(x)
-    assert torch.equal(out[0], out[1])
+    assert torch.equal(out[0], out[1]) and torch.equal(out[0], out[2])
 
 
 def test_reconstruct_applies_the_cached_choice(mod, tmp_path, monkeypatch):
@@ -137,10 +145,11 @@ def test_reconstruct_applies_the_cached_choice(mod, tmp_path, monkeypatch):
         mod.reconstruct(g, y, b, tune="always", **kw)
 
 
-@pytest.mark.parametrize("tile", [0, 1])
-def test_nonfinite_input_is_reported_by_both_tiles(mod, tile):
-    """A NaN count reaches the update through h; both tiles flag the
-    non-finite voxels it produces (one-view subsets, so the tile applies)."""
+@pytest.mark.parametrize("tile", [0, 1, 2])
+def test_nonfinite_input_is_reported_by_every_tile(mod, tile):
+    """A NaN count reaches the update through h; every tile flags the
+    non-finite voxels it produces (one-view subsets, so the tile applies;
+    the tiny volume's 40 columns allow the TMA form)."""
     from conftest import golden
     from test_oracle_golden import geom_of
 
