@@ -715,13 +715,11 @@ __device__ __forceinline__ void update_tile_tma(
     const int np = ze - zb + 2;  // planes zb - 1 .. ze; plane k is z = zb - 1 + k
     const bool issuer = tid == 0;
     bool issuing = true;         // the issuer: false once one of its waits gave up
-    int issued = 0;
-    auto issue = [&](int k) {    // plane k into slot k % UT_SLOTS (its last reader done)
-        const int s = k % UT_SLOTS;
+    int issued = np;             // planes issued: all of them unless the issuer gave up
+    auto issue = [&](int k, int s) {  // plane k into slot s = k % UT_SLOTS (its last reader done)
         tc::fence_async_smem();
         mbar_arrive_tx(&sm.full[s], UT_BYTES);
         tma_load_3d(&sm.ring[s][0], map, x0t - 4, y0t - 1, zb - 1 + k, &sm.full[s]);
-        issued = k + 1;
     };
     if (issuer) {
         for (int s = 0; s < UT_SLOTS; s++) {
@@ -729,16 +727,15 @@ __device__ __forceinline__ void update_tile_tma(
             tc::mbar_init(&sm.empty[s], UTY);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        for (int k = 0; k < min(np, UT_SLOTS); k++) issue(k);
+        for (int k = 0; k < min(np, UT_SLOTS); k++) issue(k, k);
     }
     __syncthreads();
     bool live = true;  // false after a wait of this thread gave up: it waits no more
     // test hook: the workspace's second status word k + 1 > 0 makes the wait
     // for plane k report giving up once it has in fact succeeded
     const int force_at = status[1] - 1;
-    auto wait_full = [&](int k) {
-        if (live && (!tc::mbar_wait(&sm.full[k % UT_SLOTS], (k / UT_SLOTS) & 1, UT_WAIT) ||
-                     k == force_at)) {
+    auto wait_full = [&](int k, int s, uint32_t parity) {  // plane k, in slot s
+        if (live && (!tc::mbar_wait(&sm.full[s], parity, UT_WAIT) || k == force_at)) {
             if (lane == 0) atomicOr(status, NR_FLAG_TIMEOUT);
             live = false;
         }
@@ -750,14 +747,19 @@ __device__ __forceinline__ void update_tile_tma(
     const int plane = g.nx * g.ny;
     const int64_t B = (int64_t)g.nbx * g.nby;
     const int base = (warp + 1) * UTW + lane + 4;
-    wait_full(0);
-    wait_full(1);
+    // ring slot and barrier parity of planes k - 1, k and k + 1, carried from
+    // plane to plane (slot p % UT_SLOTS, parity (p / UT_SLOTS) & 1 of plane p)
+    int sb = 0, sc = 1, sa = 2;
+    uint32_t qb = 0, qa = 0;
+    static_assert(UT_SLOTS > 3, "planes 0..2 share the first pass of the ring");
+    wait_full(0, 0, 0);
+    wait_full(1, 1, 0);
     for (int z = zb; z < ze; z++) {
         const int k = z - zb + 1;  // the centre plane's ring index
-        wait_full(k + 1);
-        const float* pb = sm.ring[(k - 1) % UT_SLOTS];
-        const float* pc = sm.ring[k % UT_SLOTS];
-        const float* pa = sm.ring[(k + 1) % UT_SLOTS];
+        wait_full(k + 1, sa, qa);
+        const float* pb = sm.ring[sb];
+        const float* pc = sm.ring[sc];
+        const float* pa = sm.ring[sa];
         if (active) {
             const int v = z * plane + iy * g.nx + ix;
             const float dv = KIND == UPD_OSTR ? __ldg(d + v) : 0.f;
@@ -781,16 +783,25 @@ __device__ __forceinline__ void update_tile_tma(
             upd_store<KIND>(xc, capL, sens, rd, rdd, dv, M, beta, x_out + v, status);
         }
         __syncwarp();
-        if (lane == 0) mbar_arrive(&sm.empty[(k - 1) % UT_SLOTS]);
+        if (lane == 0) mbar_arrive(&sm.empty[sb]);
         // plane k - 1 + UT_SLOTS goes where plane k - 1 was, once every warp is done with it
         const int kn = k - 1 + UT_SLOTS;
         if (issuer && issuing && kn < np) {
-            if (tc::mbar_wait(&sm.empty[(k - 1) % UT_SLOTS], ((k - 1) / UT_SLOTS) & 1, UT_WAIT)) {
-                issue(kn);
+            if (tc::mbar_wait(&sm.empty[sb], qb, UT_WAIT)) {
+                issue(kn, sb);
             } else {
                 atomicOr(status, NR_FLAG_TIMEOUT);
                 issuing = false;
+                issued = kn;
             }
+        }
+        // rotate: k - 1 <- k, k <- k + 1, k + 1 <- k + 2
+        qb = (sc < sb) ? qb ^ 1u : qb;  // plane k's parity: plane k - 1's, flipped on a wrap
+        sb = sc;
+        sc = sa;
+        if (++sa == UT_SLOTS) {
+            sa = 0;
+            qa ^= 1u;
         }
     }
     if (issuer) {

@@ -147,16 +147,32 @@ class TrainConfig:
     seed: int = 10_000               # training seeds seed .. seed+n_train-1, validation after
     workers: int = 8                 # processes generating phantoms
     last_scale: float = 0.1          # initial scale of the last layer (x He)
+    workload: str = "batch"          # "batch": the batched workload's statistics (hyperbola,
+                                     # delta 0.002, beta 50); "clinical": the clinical
+                                     # workload's (25 views over +-25 deg, I0 5e3, 60 slices,
+                                     # Huber delta 0.003, beta 100)
 
 
-def case_configs(n: int, seed: int, crop: Tuple[int, int]):
-    """Batched-workload cases (uneven thickness / views / dose) on a cropped
-    in-plane field with the detector fitted to the volume's shadow."""
+def case_configs(n: int, seed: int, crop: Tuple[int, int], workload: str = "batch"):
+    """Cases on a cropped in-plane field with the detector fitted to the
+    volume's shadow: the batched workload's statistics (uneven thickness /
+    views / dose; hyperbola) or the clinical workload's (Huber)."""
     from .geometry import Geometry, ReconConfig, view_angles
 
+    if workload not in ("batch", "clinical"):
+        raise ValueError(f"unknown workload {workload!r}")
     out = []
     for c in range(n):
         rng = np.random.default_rng(seed + c)
+        if workload == "clinical":
+            nx, ny = crop
+            gland = float(rng.uniform(0.10, 0.50))
+            g0 = Geometry.dbt(nx, ny, 60, 0.14, 1.0, 8, 8, 0.14, 25)
+            angles = view_angles(25, 25.0)
+            g = fit_detector(g0, angles)
+            out.append(ReconConfig(f"case{seed + c}", g, angles, 5e3, 25, 50, "huber", 100.0,
+                                   0.003, int(round(100 * gland)), 10, 60.0, seed + c))
+            continue
         nz = int(round(rng.uniform(30, 80)))
         views = int(rng.choice([9, 15, 25]))
         span = float(rng.uniform(7.5, 25.0))
@@ -220,6 +236,7 @@ class Pair:
     x_full: torch.Tensor
     y: np.ndarray
     b: np.ndarray
+    x_true: Optional[np.ndarray] = None  # the phantom
 
 
 def make_pairs(cfgs, phantom_vols, early: int, full: int) -> List[Pair]:
@@ -246,7 +263,7 @@ def make_pairs(cfgs, phantom_vols, early: int, full: int) -> List[Pair]:
         x_early = x.clone()
         plan.iterate(x, full - early)
         plan.check()
-        out.append(Pair(c, x_early, x.clone(), y, b))
+        out.append(Pair(c, x_early, x.clone(), y, b, xt))
     return out
 
 
@@ -348,7 +365,70 @@ def evaluate(cnn: WarmStartCNN, pair: Pair, after: int, early: int = 2,
     out.update(rmse_tol=rmse_tol, iters_to_tol_plain=it_plain, seconds_to_tol_plain=t_plain,
                iters_to_tol_warm=None if it_warm is None else early + it_warm,
                seconds_to_tol_warm=t_warm)
+    if max_iters > 0 and pair.x_true is not None:
+        out.update(criteria(cnn, plan, pair, early, full=max_iters))
     return out
+
+
+def criteria(cnn: WarmStartCNN, plan, pair: Pair, early: int, full: int = 50,
+             frac: float = 0.01) -> dict:
+    """The warm start against plain OSTR on the two criteria of the target:
+    (a) the FP64 objective within `frac` of plain OSTR's objective gap after
+    `full` iterations: f(x) - f_full <= frac (f(0) - f_full); (b) RMSE
+    against the phantom within `frac` of plain OSTR's after `full`
+    iterations: rmse(x) <= (1 + frac) rmse_full.  Iterations to each (early
+    iterations and the network counted for the warm start), and wall times:
+    the measured time of one iteration times the iterations, plus the
+    network's measured time for the warm start."""
+    g = pair.cfg.geom
+    truth = torch.from_numpy(np.asarray(pair.x_true, np.float32)).cuda()
+    dims = (g.nx, g.ny, g.nz, 1)
+
+    def track(x, n):
+        fs, rs = [plan.total_objective(x)], [_rmse(x, truth)]
+        for _ in range(n):
+            plan.iterate(x, 1)
+            fs.append(plan.total_objective(x))
+            rs.append(_rmse(x, truth))
+        return fs, rs
+
+    fp, rp = track(torch.zeros(g.n_voxels, device="cuda"), full)
+    f0, f_full, r_full = fp[0], fp[-1], rp[-1]
+    xw = torch.zeros(g.n_voxels, device="cuda")
+    plan.iterate(xw, early)
+    xw = warm_start_volume(cnn, xw, g)
+    fw, rw = track(xw, full - early)
+
+    def first(vals, ok, offset):
+        for k, v in enumerate(vals):
+            if ok(v):
+                return offset + k
+        return None
+
+    obj_ok = lambda f: f - f_full <= frac * (f0 - f_full)
+    rmse_ok = lambda r: r <= (1.0 + frac) * r_full
+    # timings: one plain iteration and one network pass, on this volume
+    x = torch.zeros(g.n_voxels, device="cuda")
+    plan.iterate(x, 1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plan.iterate(x, 2)
+    torch.cuda.synchronize()
+    t_it = (time.perf_counter() - t0) / 2
+    t0 = time.perf_counter()
+    cnn.forward(x, dims)
+    torch.cuda.synchronize()
+    t_cnn = time.perf_counter() - t0
+    res = {"criteria_frac": frac, "objective_gap_full": f0 - f_full, "rmse_phantom_full": r_full,
+           "seconds_per_iteration": t_it, "seconds_cnn": t_cnn}
+    for name, ok, vp, vw in (("objective", obj_ok, fp, fw), ("rmse_phantom", rmse_ok, rp, rw)):
+        kp = first(vp, ok, 0)
+        kw = first(vw, ok, early)
+        tp = None if kp is None else kp * t_it
+        tw = None if kw is None else kw * t_it + t_cnn
+        res[name] = {"iters_plain": kp, "iters_warm": kw, "seconds_plain": tp,
+                     "seconds_warm": tw, "speedup": (tp / tw) if (tp and tw) else None}
+    return res
 
 
 def warm_reconstruct(cnn: WarmStartCNN, geom, prj, blank, *, angles, subset_num: int,
@@ -378,8 +458,8 @@ def run(cfg: TrainConfig, out_params: Optional[str] = None, n_time: int = 4,
         log=print) -> dict:
     """The whole recipe: data, training, held-out evaluation.  Returns a report."""
     t0 = time.perf_counter()
-    tr_cfgs = case_configs(cfg.n_train, cfg.seed, cfg.crop)
-    va_cfgs = case_configs(cfg.n_val, cfg.seed + cfg.n_train, cfg.crop)
+    tr_cfgs = case_configs(cfg.n_train, cfg.seed, cfg.crop, cfg.workload)
+    va_cfgs = case_configs(cfg.n_val, cfg.seed + cfg.n_train, cfg.crop, cfg.workload)
     vols = phantoms(tr_cfgs + va_cfgs, cfg.workers)
     t1 = time.perf_counter()
     pairs = make_pairs(tr_cfgs, vols[:cfg.n_train], cfg.early_iters, cfg.full_iters)
@@ -413,9 +493,16 @@ def run(cfg: TrainConfig, out_params: Optional[str] = None, n_time: int = 4,
         "mean_rmse_plain": float(np.mean([e["rmse_plain"] for e in evals])),
         "mean_rmse_warm": float(np.mean([e["rmse_warm"] for e in evals])),
     }
+    timed = [e for e in evals if "objective" in e]
+    for name in ("objective", "rmse_phantom"):
+        sp = [e[name]["speedup"] for e in timed if e[name]["speedup"] is not None]
+        rep[f"speedup_{name}"] = {"cases": len(timed), "reached_by_both": len(sp),
+                                  "mean": float(np.mean(sp)) if sp else None,
+                                  "min": float(np.min(sp)) if sp else None,
+                                  "max": float(np.max(sp)) if sp else None}
     if out_params:
         np.savez_compressed(out_params, params=cnn.state(), scale=cnn.scale,
-                            early_iters=cfg.early_iters)
+                            early_iters=cfg.early_iters, workload=cfg.workload)
     return rep
 
 
@@ -436,6 +523,8 @@ def main(argv=None) -> int:
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--n-time", type=int, default=4)
+    ap.add_argument("--workload", default="batch", choices=["batch", "clinical"])
+    ap.add_argument("--crop", type=int, nargs=2, default=[256, 128])
     ap.add_argument("--out", default=None, help="write the trained parameters (.npz)")
     ap.add_argument("--report", default=None, help="write the JSON report")
     a = ap.parse_args(argv)
@@ -443,14 +532,15 @@ def main(argv=None) -> int:
 
     _n.load()
     cfg = TrainConfig(n_train=a.n_train, n_val=a.n_val, steps=a.steps, batch=a.batch, lr=a.lr,
-                      workers=a.workers)
+                      workers=a.workers, workload=a.workload, crop=tuple(a.crop))
     rep = run(cfg, a.out, n_time=a.n_time)
     txt = json.dumps(rep, indent=1, default=float)
     if a.report:
         with open(a.report, "w") as f:
             f.write(txt)
     summary = {k: rep[k] for k in ("accept_rate", "mean_objective_gain", "mean_rmse_plain",
-                                   "mean_rmse_warm", "seconds")}
+                                   "mean_rmse_warm", "seconds", "speedup_objective",
+                                   "speedup_rmse_phantom")}
     print(json.dumps(summary, default=float))
     return 0
 
