@@ -306,6 +306,9 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     return fn;
 }
 
+// The same entry point for the other translation units (cnn.cu).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encode_fn() { return tensor_map_encoder(); }
+
 #ifndef NR_SLAB_Z
 #define NR_SLAB_Z 4
 #endif

@@ -150,7 +150,9 @@ class TrainConfig:
     workload: str = "batch"          # "batch": the batched workload's statistics (hyperbola,
                                      # delta 0.002, beta 50); "clinical": the clinical
                                      # workload's (25 views over +-25 deg, I0 5e3, 60 slices,
-                                     # Huber delta 0.003, beta 100)
+                                     # Huber delta 0.003, beta 100); "fullres": the
+                                     # full-resolution workload's (0.085 mm, 70 slices, 15
+                                     # views over +-7.5 deg, I0 4e3, hyperbola 0.002 / 200)
 
 
 def case_configs(n: int, seed: int, crop: Tuple[int, int], workload: str = "batch"):
@@ -159,11 +161,22 @@ def case_configs(n: int, seed: int, crop: Tuple[int, int], workload: str = "batc
     views / dose; hyperbola) or the clinical workload's (Huber)."""
     from .geometry import Geometry, ReconConfig, view_angles
 
-    if workload not in ("batch", "clinical"):
+    if workload not in ("batch", "clinical", "fullres"):
         raise ValueError(f"unknown workload {workload!r}")
     out = []
     for c in range(n):
         rng = np.random.default_rng(seed + c)
+        if workload == "fullres":
+            # the full-resolution workload: 0.085 mm, 70 slices, 15 views over
+            # +-7.5 deg, I0 4e3, hyperbola delta 0.002, beta 200
+            nx, ny = crop
+            gland = float(rng.uniform(0.10, 0.50))
+            g0 = Geometry.dbt(nx, ny, 70, 0.085, 1.0, 8, 8, 0.085, 15)
+            angles = view_angles(15, 7.5)
+            g = fit_detector(g0, angles)
+            out.append(ReconConfig(f"case{seed + c}", g, angles, 4e3, 15, 50, "hyperbola", 200.0,
+                                   0.002, int(round(100 * gland)), 10, 70.0, seed + c))
+            continue
         if workload == "clinical":
             nx, ny = crop
             gland = float(rng.uniform(0.10, 0.50))
@@ -523,7 +536,7 @@ def main(argv=None) -> int:
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--n-time", type=int, default=4)
-    ap.add_argument("--workload", default="batch", choices=["batch", "clinical"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "clinical", "fullres"])
     ap.add_argument("--crop", type=int, nargs=2, default=[256, 128])
     ap.add_argument("--out", default=None, help="write the trained parameters (.npz)")
     ap.add_argument("--report", default=None, help="write the JSON report")
