@@ -48,9 +48,9 @@ __global__ void __launch_bounds__(128) data_term_kernel(
     block_partial(term, red, blk);
 }
 
-// psi(t) in double throughout: t is the exact difference of two floats (a
-// double holds it), and the weights are the double values 1/sqrt(...), so the
-// only roundings left are the double operations' own.
+// psi(t) in double (Lange, hyperbola): t is the exact difference of two
+// floats (a double holds it), and the weights are the double values
+// 1/sqrt(...), so the only roundings left are the double operations' own.
 template <int POT>
 __device__ __forceinline__ double psi(double t, double delta) {
     if (POT == NR_POT_Q2) return 0.5 * t * t;
@@ -70,7 +70,46 @@ __device__ __forceinline__ double psi(double t, double delta) {
 
 struct PairW {
     double w[13];  // forward neighbours: dz=+1 (9), dz=0 dy=+1 (3), dz=0 dy=0 dx=+1 (1)
+    float wh[13], wl[13];  // the same as float pairs: w = wh + wl to double precision
 };
+
+// Float-float arithmetic for the quadratic potentials: a value is hi + lo
+// with |lo| far below ulp(hi).  GB300 issues FP64 at 1/64 of its FP32 rate;
+// these error-free transforms keep the penalty of Q2 and Huber exact to
+// about 2^-44 per term in FP32 instructions, with one conversion to double
+// per voxel.  The _rn intrinsics are never contracted into FMAs, which
+// would break the transforms.
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp))};
+}
+__device__ __forceinline__ FF two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+// psi(t) for t = th + tl (the exact difference of two floats): Q2 t^2/2;
+// Huber t^2/2 for |t| <= delta, else delta |t| - delta^2/2.
+template <int POT>
+__device__ __forceinline__ FF psi_ff(float th, float tl, float delta) {
+    const float at = fabsf(th);
+    const bool quad = POT == NR_POT_Q2 || at < delta ||
+                      (at == delta && __fmul_rn(th, tl) <= 0.f);
+    if (quad) {  // (th^2 + 2 th tl) / 2
+        const FF p = two_prod(th, th);
+        return {__fmul_rn(0.5f, p.hi),
+                __fmul_rn(0.5f, __fadd_rn(p.lo, __fmul_rn(__fmul_rn(2.f, th), tl)))};
+    }
+    const float atl = th < 0.f ? -tl : tl;              // |t| = at + atl
+    const FF a = two_prod(delta, at);                  // delta |th|
+    const FF d2 = two_prod(delta, delta);
+    const FF s = two_sum(a.hi, __fmul_rn(-0.5f, d2.hi));
+    return {s.hi, __fadd_rn(s.lo, __fadd_rn(__fadd_rn(a.lo, __fmul_rn(delta, atl)),
+                                             __fmul_rn(-0.5f, d2.lo)))};
+}
 
 // zxy = Vz / Vx, formed in double from the float sizes.
 __host__ inline PairW make_pair_weights(double zxy) {
@@ -83,6 +122,10 @@ __host__ inline PairW make_pair_weights(double zxy) {
         for (int dx = -1; dx <= 1; dx++) put(dx, dy, 1);
     for (int dx = -1; dx <= 1; dx++) put(dx, 1, 0);
     put(1, 0, 0);
+    for (int q = 0; q < 13; q++) {
+        p.wh[q] = (float)p.w[q];
+        p.wl[q] = (float)(p.w[q] - (double)p.wh[q]);
+    }
     return p;
 }
 
@@ -101,12 +144,25 @@ __global__ void __launch_bounds__(128) penalty_kernel(const __grid_constant__ Ge
         const int64_t v = iz * plane + (int64_t)iy * g.nx + ix;
         const float xc = x[v];
         int k = 0;
+        FF sum = {0.f, 0.f};  // Q2 / Huber: float-float sum of the voxel's terms
         auto pair = [&](int dx, int dy, int dz) {
             const int kx = ix + dx, ky = iy + dy, kz = iz + dz;
             if ((unsigned)kx < (unsigned)g.nx && (unsigned)ky < (unsigned)g.ny &&
                 (unsigned)kz < (unsigned)g.nz) {
-                const double t = (double)xc - (double)__ldg(x + kz * plane + (int64_t)ky * g.nx + kx);
-                acc += W.w[k] * psi<POT>(t, (double)delta);
+                const float xn = __ldg(x + kz * plane + (int64_t)ky * g.nx + kx);
+                if (POT == NR_POT_Q2 || POT == NR_POT_HUBER) {
+                    const FF t = two_sum(xc, -xn);
+                    const FF ps = psi_ff<POT>(t.hi, t.lo, delta);
+                    // w psi: (wh + wl)(ps.hi + ps.lo), then into the sum
+                    const FF pr = two_prod(W.wh[k], ps.hi);
+                    const float lo = __fadd_rn(pr.lo, __fadd_rn(__fmul_rn(W.wh[k], ps.lo),
+                                                                 __fmul_rn(W.wl[k], ps.hi)));
+                    const FF s2 = two_sum(sum.hi, pr.hi);
+                    sum = {s2.hi, __fadd_rn(sum.lo, __fadd_rn(s2.lo, lo))};
+                } else {
+                    const double t = (double)xc - (double)xn;
+                    acc += W.w[k] * psi<POT>(t, (double)delta);
+                }
             }
             k++;
         };
@@ -117,6 +173,7 @@ __global__ void __launch_bounds__(128) penalty_kernel(const __grid_constant__ Ge
 #pragma unroll
         for (int dx = -1; dx <= 1; dx++) pair(dx, 1, 0);
         pair(1, 0, 0);
+        if (POT == NR_POT_Q2 || POT == NR_POT_HUBER) acc = (double)sum.hi + (double)sum.lo;
     }
     const int64_t blk = ((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
     block_partial(acc, red, blk);

@@ -519,6 +519,28 @@ def run(cfg: TrainConfig, out_params: Optional[str] = None, n_time: int = 4,
     return rep
 
 
+def time_forward(dims: Tuple[int, int, int], reps: int = 5) -> dict:
+    """Wall time of the network's forward pass on a seeded volume of dims =
+    (nx, ny, nz) with seeded weights: 3 warm-up passes, then `reps` timed."""
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    gen = torch.Generator(device="cuda").manual_seed(1)
+    x = torch.rand(n, device="cuda", generator=gen) * 0.1
+    cnn = WarmStartCNN(init_params(3, last_scale=0.5), scale=20.0)
+    shape = (nx, ny, nz, 1)
+    for _ in range(3):
+        cnn.forward(x, shape)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        cnn.forward(x, shape)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+    cnn.check()
+    flops = n * 2 * 27 * (32 + 4 * 32 * 32 + 32)
+    return {"dims": list(dims), "ms": dt * 1e3, "tflops": flops / dt / 1e12}
+
+
 def load(path: str) -> WarmStartCNN:
     z = np.load(path)
     return WarmStartCNN(z["params"], scale=float(z["scale"]))
@@ -537,6 +559,10 @@ def main(argv=None) -> int:
     ap.add_argument("--workers", type=int, default=8)
     ap.add_argument("--n-time", type=int, default=4)
     ap.add_argument("--workload", default="batch", choices=["batch", "clinical", "fullres"])
+    ap.add_argument("--time-forward", type=int, nargs=3, metavar=("NX", "NY", "NZ"),
+                    default=None,
+                    help="only time the network's forward pass on a seeded NX x NY x NZ "
+                         "volume (3 warm-up and 5 timed passes) and exit")
     ap.add_argument("--crop", type=int, nargs=2, default=[256, 128])
     ap.add_argument("--out", default=None, help="write the trained parameters (.npz)")
     ap.add_argument("--report", default=None, help="write the JSON report")
@@ -544,6 +570,9 @@ def main(argv=None) -> int:
     from . import native as _n
 
     _n.load()
+    if a.time_forward:
+        print(json.dumps(time_forward(tuple(a.time_forward))))
+        return 0
     cfg = TrainConfig(n_train=a.n_train, n_val=a.n_val, steps=a.steps, batch=a.batch, lr=a.lr,
                       workers=a.workers, workload=a.workload, crop=tuple(a.crop))
     rep = run(cfg, a.out, n_time=a.n_time)
