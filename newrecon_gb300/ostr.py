@@ -412,7 +412,8 @@ class OSTR:
                     _p(y), _p(b), _p(s), ws, n, _stream())
         self._keep = (ang, y, b, s)
 
-    def iterate(self, x: torch.Tensor, n_iters: int, monotone=False) -> torch.Tensor:
+    def iterate(self, x: torch.Tensor, n_iters: int, monotone=False,
+                check_every: int = 1) -> torch.Tensor:
         """n_iters iterations (every subset once each) on x in place.
 
         monotone=True accepts an iteration only if it does not raise the FP64
@@ -422,7 +423,12 @@ class OSTR:
         ``history`` then holds the objectives of the accepted iterates (the
         start included) and ``rejected_at`` the rejected iteration, or None.
         Each check costs one objective evaluation (a projection of all views
-        and the penalty).
+        and the penalty).  check_every=k checks after every k-th iteration
+        only (and after the last): a checkpoint whose objective rose, or is
+        NaN, is undone back to the previous accepted checkpoint and the loop
+        stops there, so the objective decreases from checkpoint to checkpoint
+        and the checks cost 1/k as much; ``rejected_at`` is then the first
+        iteration of the undone block.
 
         monotone="subset" decides every sub-iteration instead: the step of
         subset a from x to x' is kept only if it does not raise the FP64
@@ -443,19 +449,24 @@ class OSTR:
             native.call("nr_ostr_iterate", ctypes.byref(self.gc), ctypes.byref(self.params),
                         _p(x), int(n_iters), ws, n, _stream())
             return x
+        if int(check_every) < 1:
+            raise ValueError("check_every must be at least 1")
         prev = torch.empty_like(x)
         hist = [self.total_objective(x)]
         self.rejected_at = None
-        for k in range(int(n_iters)):
+        k = 0
+        while k < int(n_iters):
+            block = min(int(check_every), int(n_iters) - k)
             prev.copy_(x)
             native.call("nr_ostr_iterate", ctypes.byref(self.gc), ctypes.byref(self.params),
-                        _p(x), 1, ws, n, _stream())
+                        _p(x), block, ws, n, _stream())
             f = self.total_objective(x)
             if not f <= hist[-1]:
                 x.copy_(prev)
                 self.rejected_at = k
                 break
             hist.append(f)
+            k += block
         self.history = hist
         return x
 
@@ -712,7 +723,7 @@ class BatchGraph:
 
 def reconstruct(geom: Geometry, prj, blank, scatter=None, *, angles, subset_num: int,
                 iter_num: int, beta: float, delta: float, potential: str = "lange",
-                gamma_mode: str = "length", x0=None, monotone=False,
+                gamma_mode: str = "length", x0=None, monotone=False, check_every: int = 1,
                 tune="cached", stream=None, timing: Optional[dict] = None):
     """OSTR reconstruction: transmission counts in, attenuation (1/mm) out.
 
@@ -721,7 +732,8 @@ def reconstruct(geom: Geometry, prj, blank, scatter=None, *, angles, subset_num:
     host array, else a CUDA tensor.  monotone=True stops before the first
     iteration that would raise the FP64 objective; monotone="subset" keeps
     only the sub-iteration steps that do not raise the FP64 subset objective
-    (OSTR.iterate).  tune:
+    (OSTR.iterate; check_every=k checks the iteration-level objective every
+    k iterations).  tune:
     "cached" runs the kernel variants the autotuner cached for this GPU and
     geometry (the defaults when it has none), True tunes first when the
     cache has none, False runs the defaults.  Every variant gives the same
@@ -742,8 +754,8 @@ def reconstruct(geom: Geometry, prj, blank, scatter=None, *, angles, subset_num:
         with torch.cuda.stream(stream):
             return reconstruct(geom, prj, blank, scatter, angles=angles, subset_num=subset_num,
                                iter_num=iter_num, beta=beta, delta=delta, potential=potential,
-                               gamma_mode=gamma_mode, x0=x0, monotone=monotone, tune=tune,
-                               timing=timing)
+                               gamma_mode=gamma_mode, x0=x0, monotone=monotone,
+                               check_every=check_every, tune=tune, timing=timing)
     t_wall = time.perf_counter()
     ev = None
     if timing is not None:
@@ -768,7 +780,7 @@ def reconstruct(geom: Geometry, prj, blank, scatter=None, *, angles, subset_num:
         x = torch.zeros(geom.n_voxels, dtype=torch.float32, device=plan.ws.device)
     if ev:
         ev[2].record()
-    plan.iterate(x, iter_num, monotone=monotone)
+    plan.iterate(x, iter_num, monotone=monotone, check_every=check_every)
     if ev:
         ev[3].record()
     plan.check()

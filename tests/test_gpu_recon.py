@@ -259,6 +259,30 @@ def test_monotone_undoes_a_rising_iteration(mod, monkeypatch):
     assert torch.equal(x, xr)
 
 
+def test_monotone_checkpoints_undo_a_rising_block(mod, monkeypatch):
+    """check_every=2: the objective is checked after every second iteration;
+    a checkpoint whose objective rises (planted on the host) is undone back to
+    the previous checkpoint and the loop stops."""
+    z = golden("tiny")
+    g = geom_of(z)
+    kw = dict(subset_num=3, beta=float(z["beta"]), delta=float(z["delta"]), potential="lange")
+    plan = mod.OSTR(g, **kw)
+    plan.setup(z["angles"], z["y"], z["b"])
+    values = iter([10.0, 5.0, 7.0, 1.0])
+    monkeypatch.setattr(plan, "total_objective", lambda x: next(values))
+    x = torch.zeros(g.n_voxels, device="cuda")
+    plan.iterate(x, 6, monotone=True, check_every=2)
+    assert plan.history == [10.0, 5.0] and plan.rejected_at == 2
+    ref = mod.OSTR(g, **kw)
+    ref.setup(z["angles"], z["y"], z["b"])
+    xr = torch.zeros(g.n_voxels, device="cuda")
+    ref.iterate(xr, 2)
+    torch.cuda.synchronize()
+    assert torch.equal(x, xr)
+    with pytest.raises(ValueError):
+        plan.iterate(x, 1, monotone=True, check_every=0)
+
+
 def test_subset_data_terms_add_up_to_the_objective(mod, small_case):
     """nr_ostr_project_fp64: the same h as nr_ostr_project, and its per-subset
     FP64 data terms add up to the objective's data term (the same per-bin
