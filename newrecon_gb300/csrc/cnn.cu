@@ -19,8 +19,10 @@
 // strip's K chunk is one contiguous block); a producer warp, an MMA warp and
 // four epilogue warps overlap staging, MMAs and stores (conv32_tma_kernel).
 // Weights of all 27 taps stay in shared memory.  1-channel inputs gather the
-// 27 neighbours into one K = 32 row instead.  Weight gradients run on the
-// CUDA cores (per-tap outer products with a fixed-order reduction).
+// 27 neighbours into one K = 32 row instead.  Weight gradients of the 32 -> 32
+// layers are a GEMM over voxels on the tensor cores (wgrad32_tc_kernel); those
+// of the 1-channel layers are per-tap outer products on the CUDA cores.  Both
+// end in the same fixed-order reduction of per-block partials.
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
@@ -515,6 +517,191 @@ __global__ void __launch_bounds__(32) wgrad_thin_kernel(Dims d, const void* __re
     partial[((int64_t)tap * 32 + oi) * gridDim.x + blockIdx.x] = acc;
 }
 
+// ---- Weight gradient of the 32 -> 32 layers on the tensor cores -------------
+// dW[tap][o][i] = sum_v g[v][o] a[v + off(tap)][i] as a GEMM with M = (tap, i),
+// N = o, K = voxels: C[(tap, i)][o] = sum_v A[(tap, i)][v] B[o][v] with
+// A = the input activations shifted by the tap and B = the output gradient.
+// Per block of 128 consecutive voxels of a (patch, z, y) row (the K block),
+// one lane loads by TMA the nine input strips (rows z+dz, y+dy; x0-1 ..
+// x0+128) and the gradient strip; the four warps transpose 8 x 8 blocks
+// (ldmatrix .trans, stmatrix) from the activations' plane layout [x][8 channels]
+// into the K-major operand layout [channel][8 x], the tap's x shift being the
+// source row offset; and one lane issues, per M block of 4 taps (7 blocks: 27
+// taps and a block of ones whose row sums give the bias gradient), 8 MMAs of
+// K = 16 into that block's TMEM accumulator (32 columns).  A and B buffers are
+// double-buffered against the MMAs by tcgen05.commit barriers.  Each CTA adds
+// its K blocks into TMEM and writes one partial per weight, in the layout of
+// wgrad32_kernel, for the same fixed-order reduction.  Out-of-volume strips
+// are zeros.  Every wait is bounded; a wait that gives up flags
+// NR_FLAG_TIMEOUT, stops further copies and MMAs, and the MMAs issued and the
+// copies in flight are waited for before TMEM is released.
+constexpr int WT_GROUP = 2048;                        // bytes per 8-row group of a K-major operand (16 K chunks)
+constexpr int WT_ABUF = 16 * WT_GROUP;                // A: 4 taps x 32 channels x 128 voxels
+constexpr int WT_BBUF = 4 * WT_GROUP;                 // B: 32 channels x 128 voxels
+constexpr int WT_PLANE = 2176;                        // staged plane: 130 rows x 16 B, 128-B aligned
+constexpr int WT_STRIP = KCH * WT_PLANE;
+constexpr uint32_t WT_STRIP_TX = (uint32_t)KCH * SROWS * 16;
+constexpr int WT_SMEM = 10 * WT_STRIP + 2 * WT_ABUF + 2 * WT_BBUF + 128;
+
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t addr, uint32_t* r) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(addr));
+}
+__device__ __forceinline__ void stsm_x4(uint32_t addr, const uint32_t* r) {
+    asm volatile("stmatrix.sync.aligned.m8n8.x4.shared.b16 [%0], {%1, %2, %3, %4};" ::"r"(addr),
+                 "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3])
+                 : "memory");
+}
+
+// One warp transposes a staged strip (rows = x, 4 planes of 8 channels) into
+// slot `slot` (32 rows) of a K-major operand: operand row 8p + c, K chunk b
+// (x = 8b .. 8b+7) <- strip plane p, rows shift + 8b .. shift + 8b + 7.  The
+// warp does units u0, u0 + step, ... of the 16 units (plane p = u / 4, chunks
+// 4 (u % 4) .. + 3; one x4 instruction pair each).
+__device__ __forceinline__ void wt_transpose(const uint8_t* strip, int shift, uint8_t* op,
+                                             int slot, int u0, int step, int lane) {
+    for (int u = u0; u < 16; u += step) {
+        const int p = u >> 2, b = 4 * (u & 3) + (lane >> 3), rr = lane & 7;
+        uint32_t r[4];
+        ldsm_x4_trans(tc::smem_u32(strip + p * WT_PLANE + (shift + 8 * b + rr) * 16), r);
+        stsm_x4(tc::smem_u32(op + (slot * 4 + p) * WT_GROUP + b * 128 + rr * 16), r);
+    }
+}
+// The same slot filled with a constant 16-bit pattern (0: zeros, 0x3F80: ones).
+__device__ __forceinline__ void wt_fill(uint8_t* op, int slot, uint32_t pat, int t0, int nt) {
+    const uint4 v = make_uint4(pat * 0x10001u, pat * 0x10001u, pat * 0x10001u, pat * 0x10001u);
+    uint4* q = (uint4*)(op + slot * 4 * WT_GROUP);
+    for (int k = t0; k < 4 * WT_GROUP / 16; k += nt) q[k] = v;
+}
+
+__global__ void __launch_bounds__(128, 1) wgrad32_tc_kernel(Dims d,
+                                                            const __grid_constant__ CUtensorMap amap,
+                                                            const __grid_constant__ CUtensorMap gmap,
+                                                            float* __restrict__ partial,
+                                                            int* status) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* stg = smem;                                   // 9 input strips + the gradient strip
+    uint8_t* abuf = smem + 10 * WT_STRIP;                   // 2 x A
+    uint8_t* bbuf = abuf + 2 * WT_ABUF;                     // 2 x B
+    uint64_t* bars = (uint64_t*)(bbuf + 2 * WT_BBUF);       // sbar, abar[2], drain
+    uint32_t* tslot = (uint32_t*)(bars + 4);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        for (int k = 0; k < 4; k++) tc::mbar_init(&bars[k], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tc::tmem_alloc(tslot, 256);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = *tslot;
+    const int64_t nt = ntiles(d);
+    const int force_at = status[1] - 1;  // test hook: the wait for K block k gives up
+    constexpr uint32_t idesc = tc::idesc_bf16(TM, C);
+    bool ok = true;
+    int kb = 0, c = 0;
+    int64_t staged = -1;  // the K block whose copies were issued and not yet waited for
+    for (int64_t t = blockIdx.x; t < nt; t += gridDim.x, kb++) {
+        int b, z, y, x0;
+        tile_pos(d, t, b, z, y, x0);
+        if (tid == 0) {
+            uint32_t bytes = WT_STRIP_TX;  // the gradient strip
+            for (int q = 0; q < 9; q++) {
+                const int zz = z + q / 3 - 1, yy = y + q % 3 - 1;
+                if (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny) bytes += WT_STRIP_TX;
+            }
+            tc::fence_async_smem();
+            mbar_arrive_tx(&bars[0], bytes);
+            const int grow = (b * d.nz + z) * d.ny + y;
+            for (int kc = 0; kc < KCH; kc++)
+                tma_load_4d(stg + 9 * WT_STRIP + kc * WT_PLANE, &gmap, 0, x0 - 1, kc, grow, &bars[0]);
+            for (int q = 0; q < 9; q++) {
+                const int zz = z + q / 3 - 1, yy = y + q % 3 - 1;
+                if (!(zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny)) continue;
+                const int row = (b * d.nz + zz) * d.ny + yy;
+                for (int kc = 0; kc < KCH; kc++)
+                    tma_load_4d(stg + q * WT_STRIP + kc * WT_PLANE, &amap, 0, x0 - 1, kc, row,
+                                &bars[0]);
+            }
+        }
+        staged = kb;
+        bool got = tc::mbar_wait(&bars[0], (uint32_t)(kb & 1), WAIT_LIMIT) && kb != force_at;
+        if (!__syncthreads_and(got)) {
+            ok = false;
+            break;
+        }
+        staged = -1;
+        for (int mb = 0; mb < 7; mb++, c++) {
+            const int j = c & 1;
+            // the MMAs of use c - 2 of this A buffer (and, at mb 0, every MMA
+            // of K block kb - 2, the last reader of this B buffer) are done;
+            // a warp in which a wait gave up writes nothing (the transposes are
+            // warp-collective, so the decision is the warp's)
+            if (c >= 2 &&
+                !__all_sync(0xffffffffu,
+                            tc::mbar_wait(&bars[1 + j], (uint32_t)(((c >> 1) - 1) & 1), WAIT_LIMIT)))
+                ok = false;
+            uint8_t* A = abuf + j * WT_ABUF;
+            uint8_t* Bm = bbuf + (kb & 1) * WT_BBUF;
+            if (ok && mb == 0) wt_transpose(stg + 9 * WT_STRIP, 1, Bm, 0, warp, 4, lane);
+            for (int sl = 0; sl < 4 && ok; sl++) {
+                const int tap = 4 * mb + sl;
+                if (tap == 27) {
+                    wt_fill(A, sl, 0x3F80u, tid, 128);  // ones: the bias gradient
+                    continue;
+                }
+                const int q = tap / 3, dx = tap % 3;
+                const int zz = z + q / 3 - 1, yy = y + q % 3 - 1;
+                if (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny)
+                    wt_transpose(stg + q * WT_STRIP, dx, A, sl, warp, 4, lane);
+                else
+                    wt_fill(A, sl, 0u, tid, 128);
+            }
+            tc::fence_async_smem();
+            if (!__syncthreads_and(ok)) {
+                ok = false;
+                break;
+            }
+            if (tid == 0) {
+                tc::fence_after();
+                const uint32_t sa = tc::smem_u32(A), sb = tc::smem_u32(Bm);
+#pragma unroll
+                for (int st = 0; st < TM / 16; st++)
+                    tc::mma_bf16(tmem + (uint32_t)(mb * 32), tc::sdesc(sa + st * 256, 128, WT_GROUP),
+                                 tc::sdesc(sb + st * 256, 128, WT_GROUP), idesc,
+                                 (kb > 0 || st > 0) ? 1u : 0u);
+                tc::commit(&bars[1 + j]);
+            }
+        }
+        if (!ok) break;
+        tc::fence_async_smem();  // this block's reads of the staging precede the next copies
+        __syncthreads();
+    }
+    if (!ok && tid == 0) atomicOr(status, NR_FLAG_TIMEOUT);
+    // copies still in flight land, and every MMA issued completes, before TMEM goes
+    if (tid == 0 && staged >= 0 && !tc::mbar_wait(&bars[0], (uint32_t)(staged & 1), WAIT_LIMIT))
+        tc::mbar_wait(&bars[0], (uint32_t)(staged & 1), WAIT_LIMIT);
+    if (tid == 0) tc::commit(&bars[3]);
+    if (!tc::mbar_wait(&bars[3], 0, WAIT_LIMIT)) tc::mbar_wait(&bars[3], 0, WAIT_LIMIT);
+    tc::fence_after();
+    if (ok && kb > 0) {
+        // TMEM lane 32 w + l = (tap 4 mb + w, input channel l), column o
+        const int64_t nchunk = gridDim.x;
+        for (int mb = 0; mb < 7; mb++) {
+            uint32_t acc[32];
+            tc::ld32(tmem, (uint32_t)(warp * 32), (uint32_t)(mb * 32), acc);
+            const int tap = 4 * mb + warp;
+            for (int o = 0; o < C; o++)
+                partial[(((int64_t)tap * C + o) * C + lane) * nchunk + blockIdx.x] =
+                    __uint_as_float(acc[o]);
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 256);
+}
+
 // grad[tap][o][i] (and grad_b[o] from tap 27, i = 0) = sum over chunks, in order.
 __global__ void wgrad_reduce_kernel(const float* __restrict__ partial, int64_t nchunk, int nout,
                                     int ni, float* __restrict__ gw, float* __restrict__ gb) {
@@ -784,7 +971,7 @@ __global__ void target_kernel(const float* __restrict__ x, const float* __restri
 }
 
 static nr_status wgrad(const Dims& d, int l, const void* g, const void* in, float s, char* ws,
-                       const WSL& L, float* grad, cudaStream_t st) {
+                       const WSL& L, float* grad, int* status, cudaStream_t st) {
     int64_t wo[6], bo[6], P;
     param_offsets(wo, bo, &P);
     float* part = (float*)(ws + L.part);
@@ -799,10 +986,20 @@ static nr_status wgrad(const Dims& d, int l, const void* g, const void* in, floa
         nout = C;
         ni = C;
     } else {
-        wgrad32_kernel<<<grid, 256, 0, st>>>(d, (const __nv_bfloat16*)g, (const __nv_bfloat16*)in,
-                                              part);
-        nout = C * C;
-        ni = C;
+        // the tensor-core form: one partial per CTA (at most L.nchunk CTAs)
+        CUtensorMap am, gm;
+        if (!act_map(d, (const __nv_bfloat16*)in, &am) || !act_map(d, (const __nv_bfloat16*)g, &gm))
+            return NR_ERR_CUDA;
+        if (cudaFuncSetAttribute(wgrad32_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 WT_SMEM) != cudaSuccess)
+            return NR_ERR_CUDA;
+        const int64_t nt = ntiles(d);
+        int64_t nch = nt < (int64_t)sm_count() ? nt : (int64_t)sm_count();
+        if (nch > L.nchunk) nch = L.nchunk;
+        wgrad32_tc_kernel<<<(unsigned)nch, 128, WT_SMEM, st>>>(d, am, gm, part, status);
+        wgrad_reduce_kernel<<<(28 * C * C + 255) / 256, 256, 0, st>>>(part, nch, C * C, C,
+                                                                      grad + wo[l], grad + bo[l]);
+        return launch_status();
     }
     wgrad_reduce_kernel<<<(28 * nout + 255) / 256, 256, 0, st>>>(part, L.nchunk, nout, ni,
                                                                  grad + wo[l], grad + bo[l]);
@@ -830,18 +1027,18 @@ static nr_status loss_grad(const Dims& d, const float* params, const float* x, c
     for (int l = 1; l < 5; l++) pack(params + wo[l], 1, C, C, C, pkb(l), st);
     pack(params + wo[5], 3, C, 1, C, pkb(5), st);
     // layer 6: weight gradient and the masked input gradient dpre5
-    if ((e = wgrad(d, 5, g6, act(4), 1.f, ws, L, grad, st)) != NR_OK) return e;
+    if ((e = wgrad(d, 5, g6, act(4), 1.f, ws, L, grad, status, st)) != NR_OK) return e;
     if ((e = launch_conv1<EPI_MASK>(d, g6, 1.f, pkb(5), nullptr, dpre(4), act(4), status, st)) !=
         NR_OK)
         return e;
     // layers 5..2: dpre_l lives in dpre(l-1)
     for (int l = 4; l >= 1; l--) {
-        if ((e = wgrad(d, l, dpre(l), act(l - 1), 1.f, ws, L, grad, st)) != NR_OK) return e;
+        if ((e = wgrad(d, l, dpre(l), act(l - 1), 1.f, ws, L, grad, status, st)) != NR_OK) return e;
         if ((e = launch_conv32<C, EPI_MASK>(d, dpre(l), pkb(l), nullptr, dpre(l - 1), act(l - 1),
                                             status, st)) != NR_OK)
             return e;
     }
-    return wgrad(d, 0, dpre(0), x, s, ws, L, grad, st);
+    return wgrad(d, 0, dpre(0), x, s, ws, L, grad, status, st);
 }
 
 }  // namespace cnn

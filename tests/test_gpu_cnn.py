@@ -54,7 +54,12 @@ def test_forward_matches_reference(ws, dims):
     assert rel(out - x.ravel(), (ref - x).ravel()) < 2e-3
 
 
-@pytest.mark.parametrize("dims", DIMS[:2], ids=["partial", "two_tiles"])
+# 512 row blocks: every CTA of the tensor-core weight gradient accumulates 3 or 4
+# of them in TMEM, through both halves of its double-buffered operands
+MANY = (160, 16, 8, 2)
+
+
+@pytest.mark.parametrize("dims", DIMS[:2] + [MANY], ids=["partial", "two_tiles", "many_blocks"])
 def test_gradients_match_reference(ws, dims):
     from oracle import cnn_oracle as co
 
@@ -74,6 +79,21 @@ def test_gradients_match_reference(ws, dims):
         sb = slice(bo[l], bo[l] + no)
         assert rel(grad[sw], gref[sw]) < 1e-2, ("W", l, rel(grad[sw], gref[sw]))
         assert rel(grad[sb], gref[sb]) < 1e-2, ("b", l, rel(grad[sb], gref[sb]))
+
+
+def test_gradients_are_deterministic(ws):
+    """A fixed grid, a fixed order of row blocks per CTA and a fixed-order
+    reduction: the same inputs give the same gradient bit for bit."""
+    from oracle import cnn_oracle as co
+
+    x, t = data(MANY, 3)
+    net = ws.WarmStartCNN(co.init_params(5, last_scale=0.5), scale=20.0)
+    xd, td = torch.from_numpy(x.ravel()).cuda(), torch.from_numpy(t.ravel()).cuda()
+    _, g1 = net.loss_grad(xd, td, MANY)
+    g1 = g1.clone()
+    _, g2 = net.loss_grad(xd, td, MANY)
+    net.check()
+    assert torch.equal(g1, g2)
 
 
 def test_adam_matches_reference(ws):

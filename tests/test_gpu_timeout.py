@@ -139,3 +139,38 @@ def test_convolution_expiry_releases_tensor_memory(mod):
     net.check()
     torch.cuda.synchronize()
     assert torch.equal(out, ref)
+
+
+def test_weight_gradient_expiry_is_reported_and_recovers(mod):
+    """The training pass (convolutions and the tensor-core weight gradient):
+    with the hook on, the gradient's staging wait of K block 0 or 1 gives up,
+    the block drains its MMAs and copies and releases TMEM; the check reports
+    the timeout, and with the hook off the gradient on the same workspace is
+    the first one's bit for bit."""
+    from newrecon_gb300 import native, warmstart
+    from newrecon_gb300.native import NrError
+    from oracle import cnn_oracle as co
+
+    dims = (160, 16, 8, 2)  # 512 row blocks: 3 or 4 per CTA
+    rng = np.random.default_rng(6)
+    n = int(np.prod(dims))
+    x = torch.from_numpy(rng.uniform(0.0, 0.1, size=n).astype(np.float32)).cuda()
+    t = (x + 0.01).contiguous()
+    net = warmstart.WarmStartCNN(co.init_params(3, last_scale=0.5), scale=20.0)
+    _, ref = net.loss_grad(x, t, dims)
+    ref = ref.clone()
+    net.check()
+    _, ws = net._workspace(dims, True)
+    for at in (0, 1):
+        expire(ws, at)
+        net.loss_grad(x, t, dims)
+        flags = ctypes.c_int32(0)
+        with pytest.raises(NrError) as e:
+            native.call("nr_cnn_check", ctypes.c_void_p(ws.data_ptr()), ctypes.byref(flags),
+                        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        assert e.value.code == NR_ERR_TIMEOUT and flags.value & 2
+    expire(ws, -1)
+    _, g = net.loss_grad(x, t, dims)
+    net.check()
+    torch.cuda.synchronize()
+    assert torch.equal(g, ref)
