@@ -113,9 +113,9 @@ __device__ __forceinline__ void tile_pos(const Dims& d, int64_t t, int& b, int& 
 // 32-channel input, NOUT = 32 (hidden / dgrad) or 16 (the last layer, output
 // channel 0 real) outputs; weights: 27 packed taps of NOUT x 32.  The work is
 // split between warps so that staging, MMAs and the epilogue overlap:
-//   warp 4 (one lane)  producer: loads each strip by TMA -- four boxes of
-//                      8 channels x 130 rows, one per 16-byte K chunk, each a
-//                      contiguous block of the plane layout -- so the strip
+//   warp 4 (one lane)  producer: loads each strip by TMA -- per 16-byte K
+//                      chunk one contiguous block of the plane layout, in two
+//                      boxes (load_strip) -- so the strip
 //                      lands in the K-major core-matrix layout with zeros
 //                      outside the volume in x, into a ring of TSTAGE stages
 //                      ("full": the bytes landed); strips outside the volume
@@ -148,6 +148,22 @@ struct TmaCtl {
     int abort;
 };
 
+// One strip (130 rows x 4 K-chunk planes, plane stride `pstride`) of row
+// `row` from x0 - 1 by TMA.  The activation tensor is mapped as (2 nx 8-byte
+// units, 4 K chunks, R rows), so one plane is one contiguous run; it is loaded
+// as two boxes, rows 0-63 (map lo, 128 units) and rows 64-129 (map hi, 132
+// units), both 128-byte aligned in shared memory.  Out-of-range units (x < 0,
+// x >= nx, row < 0) arrive as zeros; 4 x 2080 bytes complete on `bar`.
+__device__ __forceinline__ void load_strip(uint8_t* dst, int pstride, const CUtensorMap* lo,
+                                           const CUtensorMap* hi, int x0, int row, uint64_t* bar) {
+    const int u0 = 2 * (x0 - 1);
+#pragma unroll
+    for (int kc = 0; kc < KCH; kc++) {
+        tma_load_3d(dst + kc * pstride, lo, u0, kc, row, bar);
+        tma_load_3d(dst + kc * pstride + 1024, hi, u0 + 128, kc, row, bar);
+    }
+}
+
 // A bounded wait that also gives up once the block has aborted.
 __device__ __forceinline__ bool wait_live(uint64_t* bar, uint32_t parity, volatile int* abort) {
     for (int round = 0; round < WAIT_LIMIT / 1024; round++) {
@@ -159,7 +175,8 @@ __device__ __forceinline__ bool wait_live(uint64_t* bar, uint32_t parity, volati
 
 template <int NOUT, int EPI>
 __global__ void __launch_bounds__(T_THREADS) conv32_tma_kernel(
-    Dims d, const __grid_constant__ CUtensorMap amap, const __nv_bfloat16* __restrict__ wpk,
+    Dims d, const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap amap_hi,
+    const __nv_bfloat16* __restrict__ wpk,
     const float* __restrict__ bias, void* out, const __nv_bfloat16* __restrict__ mask,
     int* status) {
     constexpr int WBYTES = 27 * NOUT * C * 2;
@@ -216,8 +233,7 @@ __global__ void __launch_bounds__(T_THREADS) conv32_tma_kernel(
                         uint8_t* st = sA + s * TSTRIP;
                         tc::fence_async_smem();
                         mbar_arrive_tx(&K->full[s], STRIP_TX);
-                        for (int kc = 0; kc < KCH; kc++)
-                            tma_load_4d(st + kc * PLANE, &amap, 0, x0 - 1, kc, row, &K->full[s]);
+                        load_strip(st, PLANE, &amap, &amap_hi, x0, row, &K->full[s]);
                     } else {
                         mbar_arrive(&K->full[s]);
                     }
@@ -409,311 +425,423 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restr
 }
 
 // ---------------------------------------------------------------------------
-// Weight gradients (CUDA cores).  dW[tap][o][i] = sum_v g[v][o] in[v+off(tap)][i]
-// over the stacked patches (zero outside each patch), db[o] = sum_v g[v][o].
-// Grid: (chunk of WG_CHUNK voxels, tap 0..27; tap 27 = bias).  Each block
-// writes one partial per output; wgrad_reduce_kernel adds the chunks in order.
-constexpr int WG_CHUNK = 2048;
-constexpr int WG_SUB = 64;
+// Weight gradients on the tensor cores.  dW[tap][o][i] = sum_v g[v][o]
+// in[v + off(tap)][i] over the stacked patches (zero outside each patch) and
+// db[o] = sum_v g[v][o]: per layer one GEMM with the voxels as K, in K blocks
+// of one tile (128 consecutive x of a (patch, z, y) row).
+//
+// The activations' plane layout makes staged strips operands as they land: a
+// strip plane is [x][8 channels], i.e. MN-major core matrices (8 channels x 8
+// consecutive x in 16-byte rows), and strips staged one after another sit at
+// one uniform plane stride, so several strips form one operand whose rows are
+// (strip, channel), and a shift along x is a 16-byte start offset.
+//   WG_HID   (32 -> 32)  The shift moves to the gradient: per row of the
+//                        volume, sum_x g[x] a[x + dx - 1] = sum_x' g[x' + 1 - dx]
+//                        a[x'] (both zero outside the row), so with K = x' the
+//                        nine input strips are B unshifted (N = 9 x 32 = 288,
+//                        two MMAs of N = 144) and A (M = 128) is the gradient
+//                        strip staged three times, copy c from x0 + 1 - c (rows
+//                        (c, o); copy 3 is zeros).  D[(dx, o)][(strip, i)]: 16
+//                        MMAs per K block, each reading 8.6 KB of operands.
+//   WG_LAST  (32 -> 1)   A = four input strips (rows (strip, i)) at the tap's
+//                        x shift: blocks {0-3}, {4-7}, {5-8} (of the last only
+//                        strip 8's rows are kept) x dx = 9 MMA blocks; B = the
+//                        FP32 gradient of the one output split as hi + lo BF16
+//                        (rows 0, 1 of an N = 16 K-major operand): dW = column
+//                        0 + column 1.
+//   WG_FIRST (1 -> 32)   A = the FP32 input u = s x at the 27 shifts split as
+//                        hi (rows 0-26) + lo (rows 32-58) of a K-major M = 128
+//                        operand; B = the gradient strip.
+// The split keeps the FP32 operand to 2^-17 relative: hi = bf16(u), lo =
+// bf16(u - hi), and the products of BF16 values are exact in the FP32
+// accumulator.  The bias gradient is summed on the CUDA cores (FP32 per
+// thread, then in a fixed order).
+//
+// Roles (6 warps): warp 0 lane 0 loads each K block's strips by TMA into one
+// of two stages (a strip outside the patch in z or y is loaded from row -1,
+// i.e. zero-filled); warp 1 lane 0 issues the MMAs and frees the stage by
+// tcgen05.commit; warps 2-5 (x - x0 in 32 h .. 32 h + 31 for warp 2 + h) build
+// the split operand from global data fetched one block ahead and sum the
+// bias.  Every wait is bounded and gives up once another role has aborted; a
+// role that gives up flags NR_FLAG_TIMEOUT and aborts the block.  Before TMEM
+// is released the issuer's MMAs are drained and the producer waits for every
+// copy it issued.  Each CTA writes one partial per weight (row blockIdx.x of
+// partial[CTA][28 x weights per tap]); wgrad_reduce_kernel adds the rows in
+// order.
+enum { WG_HID = 0, WG_LAST = 1, WG_FIRST = 2 };
+constexpr int WG_MAXCTA = 256;  // partial slots per weight
+constexpr int WG_GROUP = 2048;  // K-major built operand: bytes per 8-row group (16 K chunks)
+constexpr int WG_PLANE = 2176;  // staged plane: 130 rows x 16 B, 128-B aligned
+constexpr int WG_STRIP = KCH * WG_PLANE;
+constexpr int WG_THREADS = 192;
+constexpr int WG_WIN = 34;      // WG_FIRST: input window per builder warp and row
 
-__device__ __forceinline__ float ld_act(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+struct WgCtl {
+    uint64_t tfull[2], bfull[2], empty[2], drain;
+    uint32_t tslot;
+    int abort;
+    float bsum[4][C];
+};
 
-// Loads the shifted input (tap) and the output gradient of voxels s .. s+WG_SUB-1
-// into shared memory as FP32 (zero outside each patch / past the end).
-template <int NI, int NO, int GP, int XP>
-__device__ __forceinline__ void wg_stage(const Dims& d, int tap, int64_t s, int64_t V,
-                                         const void* __restrict__ g_, const void* __restrict__ in_,
-                                         float in_scale, float (*gs)[GP], float (*xs)[XP]) {
-    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-    for (int e = threadIdx.x; e < WG_SUB * NO; e += blockDim.x) {
-        const int vi = e / NO, o = e % NO;
-        const int64_t v = s + vi;
-        float gv = 0.f;
-        if (v < V)
-            gv = NO == 1 ? ((const float*)g_)[v]
-                         : ld_act((const __nv_bfloat16*)g_ + act_off(v, o, d.nx));
-        gs[vi][o] = gv;
-    }
-    for (int e = threadIdx.x; e < WG_SUB * NI; e += blockDim.x) {
-        const int vi = e / NI, i = e % NI;
-        const int64_t v = s + vi;
-        float xv = 0.f;
-        if (v < V) {
-            if (tap == 27) {
-                xv = 1.f;  // the bias "tap"
-            } else {
-                int64_t r = v;
-                const int x = (int)(r % d.nx);
-                r /= d.nx;
-                const int y = (int)(r % d.ny);
-                r /= d.ny;
-                const int z = (int)(r % d.nz);
-                const int b = (int)(r / d.nz);
-                const int xx = x + dx, yy = y + dy, zz = z + dz;
-                if (xx >= 0 && xx < d.nx && yy >= 0 && yy < d.ny && zz >= 0 && zz < d.nz) {
-                    const int64_t u = (((int64_t)b * d.nz + zz) * d.ny + yy) * d.nx + xx;
-                    xv = NI == 1 ? ((const float*)in_)[u] * in_scale
-                                 : ld_act((const __nv_bfloat16*)in_ + act_off(u, i, d.nx));
-                }
-            }
+template <int MODE>
+struct WgCfg {
+    // one stage: [input strips 0..8 | gradient strip copies | built operand]
+    static constexpr int NSTRIP = MODE == WG_FIRST ? 0 : 9;
+    static constexpr int NCOPY = MODE == WG_HID ? 4 : (MODE == WG_FIRST ? 1 : 0);
+    static constexpr int NLOAD = MODE == WG_HID ? 3 : NCOPY;  // copies loaded (HID copy 3: zeros)
+    static constexpr int OFF_G = NSTRIP * WG_STRIP;
+    static constexpr int OFF_X = OFF_G + NCOPY * WG_STRIP;
+    static constexpr int XBYTES =
+        MODE == WG_LAST ? 2 * WG_GROUP : (MODE == WG_FIRST ? 16 * WG_GROUP : 0);
+    static constexpr int STAGE = OFF_X + XBYTES;
+    static constexpr uint32_t TX = (uint32_t)(NSTRIP + NLOAD) * KCH * SROWS * 16;
+    static constexpr int N = MODE == WG_HID ? 144 : (MODE == WG_LAST ? 16 : C);
+    static constexpr uint32_t NCOL = MODE == WG_FIRST ? 32 : 512;
+    // WG_FIRST: each builder warp's window of the input, 9 rows x WG_WIN x
+    static constexpr int XS = MODE == WG_FIRST ? 4 * 9 * WG_WIN * 4 : 0;
+    static constexpr int SMEM = 2 * STAGE + XS + (int)sizeof(WgCtl);
+    // bit 15 / 16: A / B MN-major
+    static constexpr uint32_t IDESC = tc::idesc_bf16(TM, N) |
+                                      (MODE != WG_FIRST ? 1u << 15 : 0u) |
+                                      (MODE != WG_LAST ? 1u << 16 : 0u);
+    // arrivals that free a stage: the MMA commit, and the bias warps after
+    // reading the gradient strip
+    static constexpr int EMPTY_COUNT = MODE == WG_LAST ? 1 : 5;
+};
+
+// Stores the BF16 pair hi + lo of u at rows (mh, ml), K index k of a K-major
+// built operand (8-row groups WG_GROUP apart, K chunks 128 B apart).
+__device__ __forceinline__ void wg_split_store(uint8_t* op, int mh, int ml, int k, float u) {
+    const __nv_bfloat16 hi = __float2bfloat16_rn(u);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(u - __bfloat162float(hi));
+    const int kk = (k >> 3) * 128 + (k & 7) * 2;
+    *(__nv_bfloat16*)(op + (mh >> 3) * WG_GROUP + kk + (mh & 7) * 16) = hi;
+    *(__nv_bfloat16*)(op + (ml >> 3) * WG_GROUP + kk + (ml & 7) * 16) = lo;
+}
+
+// The global data one builder lane needs for the K block of tile t: WG_LAST
+// the gradient at x = x0 + 32 h + lane; WG_FIRST its share of the warp's
+// window u = s x at x0 - 1 + 32 h + j (j < WG_WIN) of the nine rows.
+template <int MODE>
+__device__ __forceinline__ void wg_fetch(const Dims& d, int64_t t, int h, int lane,
+                                         const float* __restrict__ gvec,
+                                         const float* __restrict__ xin, float s, float* r) {
+    int b, z, y, x0;
+    tile_pos(d, t, b, z, y, x0);
+    if (MODE == WG_LAST) {
+        const int x = x0 + 32 * h + lane;
+        r[0] = x < d.nx ? __ldg(gvec + (((int64_t)b * d.nz + z) * d.ny + y) * d.nx + x) : 0.f;
+    } else if (MODE == WG_FIRST) {
+#pragma unroll
+        for (int k = 0; k < (9 * WG_WIN + 31) / 32; k++) {
+            const int e = lane + 32 * k;
+            const int q = e / WG_WIN, j = e - q * WG_WIN;
+            const int zz = z + q / 3 - 1, yy = y + q % 3 - 1;
+            const int xx = x0 - 1 + 32 * h + j;
+            r[k] = 0.f;
+            if (e < 9 * WG_WIN && zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny && xx >= 0 &&
+                xx < d.nx)
+                r[k] = __ldg(xin + (((int64_t)b * d.nz + zz) * d.ny + yy) * d.nx + xx) * s;
         }
-        xs[vi][i] = xv;
     }
 }
 
-// 32 x 32 layers: thread -> output channel o = tid/8 and inputs i0..i0+3.
-__global__ void __launch_bounds__(256) wgrad32_kernel(Dims d, const __nv_bfloat16* __restrict__ g,
-                                                      const __nv_bfloat16* __restrict__ in,
-                                                      float* __restrict__ partial) {
-    __shared__ __align__(16) float gs[WG_SUB][C + 1];
-    __shared__ __align__(16) float xs[WG_SUB][C + 4];
-    const int tap = blockIdx.y;
-    const int64_t V = nvox(d);
-    const int64_t v0 = (int64_t)blockIdx.x * WG_CHUNK;
-    const int o = threadIdx.x >> 3, i0 = (threadIdx.x & 7) * 4;
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-    for (int64_t s = v0; s < v0 + WG_CHUNK && s < V; s += WG_SUB) {
-        wg_stage<C, C, C + 1, C + 4>(d, tap, s, V, g, in, 1.f, gs, xs);
-        __syncthreads();
-#pragma unroll 8
-        for (int vi = 0; vi < WG_SUB; vi++) {
-            const float gv = gs[vi][o];
-            const float4 xv = *(const float4*)&xs[vi][i0];
-            a0 = fmaf(gv, xv.x, a0);
-            a1 = fmaf(gv, xv.y, a1);
-            a2 = fmaf(gv, xv.z, a2);
-            a3 = fmaf(gv, xv.w, a3);
-        }
-        __syncthreads();
-    }
-    const int64_t nchunk = gridDim.x;
-    const int64_t base = ((int64_t)tap * C * C + o * C + i0) * nchunk + blockIdx.x;
-    partial[base] = a0;
-    partial[base + nchunk] = a1;
-    partial[base + 2 * nchunk] = a2;
-    partial[base + 3 * nchunk] = a3;
-}
-
-// Thin layers (NI = 1 or NO = 1): 32 outputs per tap, one per thread of 32.
-template <int NI, int NO>
-__global__ void __launch_bounds__(32) wgrad_thin_kernel(Dims d, const void* __restrict__ g_,
-                                                        const void* __restrict__ in_,
-                                                        float in_scale,
-                                                        float* __restrict__ partial) {
-    __shared__ float gs[WG_SUB][NO + 1];
-    __shared__ float xs[WG_SUB][NI + 1];
-    const int tap = blockIdx.y;
-    const int64_t V = nvox(d);
-    const int64_t v0 = (int64_t)blockIdx.x * WG_CHUNK;
-    const int oi = threadIdx.x;  // NI * NO == 32
-    const int o = oi / NI, i = oi % NI;
-    float acc = 0.f;
-    for (int64_t s = v0; s < v0 + WG_CHUNK && s < V; s += WG_SUB) {
-        wg_stage<NI, NO, NO + 1, NI + 1>(d, tap, s, V, g_, in_, in_scale, gs, xs);
-        __syncthreads();
-        for (int vi = 0; vi < WG_SUB; vi++) acc = fmaf(gs[vi][o], xs[vi][i], acc);
-        __syncthreads();
-    }
-    partial[((int64_t)tap * 32 + oi) * gridDim.x + blockIdx.x] = acc;
-}
-
-// ---- Weight gradient of the 32 -> 32 layers on the tensor cores -------------
-// dW[tap][o][i] = sum_v g[v][o] a[v + off(tap)][i] as a GEMM with M = (tap, i),
-// N = o, K = voxels: C[(tap, i)][o] = sum_v A[(tap, i)][v] B[o][v] with
-// A = the input activations shifted by the tap and B = the output gradient.
-// Per block of 128 consecutive voxels of a (patch, z, y) row (the K block),
-// one lane loads by TMA the nine input strips (rows z+dz, y+dy; x0-1 ..
-// x0+128) and the gradient strip; the four warps transpose 8 x 8 blocks
-// (ldmatrix .trans, stmatrix) from the activations' plane layout [x][8 channels]
-// into the K-major operand layout [channel][8 x], the tap's x shift being the
-// source row offset; and one lane issues, per M block of 4 taps (7 blocks: 27
-// taps and a block of ones whose row sums give the bias gradient), 8 MMAs of
-// K = 16 into that block's TMEM accumulator (32 columns).  A and B buffers are
-// double-buffered against the MMAs by tcgen05.commit barriers.  Each CTA adds
-// its K blocks into TMEM and writes one partial per weight, in the layout of
-// wgrad32_kernel, for the same fixed-order reduction.  Out-of-volume strips
-// are zeros.  Every wait is bounded; a wait that gives up flags
-// NR_FLAG_TIMEOUT, stops further copies and MMAs, and the MMAs issued and the
-// copies in flight are waited for before TMEM is released.
-constexpr int WT_GROUP = 2048;                        // bytes per 8-row group of a K-major operand (16 K chunks)
-constexpr int WT_ABUF = 16 * WT_GROUP;                // A: 4 taps x 32 channels x 128 voxels
-constexpr int WT_BBUF = 4 * WT_GROUP;                 // B: 32 channels x 128 voxels
-constexpr int WT_PLANE = 2176;                        // staged plane: 130 rows x 16 B, 128-B aligned
-constexpr int WT_STRIP = KCH * WT_PLANE;
-constexpr uint32_t WT_STRIP_TX = (uint32_t)KCH * SROWS * 16;
-constexpr int WT_SMEM = 10 * WT_STRIP + 2 * WT_ABUF + 2 * WT_BBUF + 128;
-
-__device__ __forceinline__ void ldsm_x4_trans(uint32_t addr, uint32_t* r) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(addr));
-}
-__device__ __forceinline__ void stsm_x4(uint32_t addr, const uint32_t* r) {
-    asm volatile("stmatrix.sync.aligned.m8n8.x4.shared.b16 [%0], {%1, %2, %3, %4};" ::"r"(addr),
-                 "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3])
-                 : "memory");
-}
-
-// One warp transposes a staged strip (rows = x, 4 planes of 8 channels) into
-// slot `slot` (32 rows) of a K-major operand: operand row 8p + c, K chunk b
-// (x = 8b .. 8b+7) <- strip plane p, rows shift + 8b .. shift + 8b + 7.  The
-// warp does units u0, u0 + step, ... of the 16 units (plane p = u / 4, chunks
-// 4 (u % 4) .. + 3; one x4 instruction pair each).
-__device__ __forceinline__ void wt_transpose(const uint8_t* strip, int shift, uint8_t* op,
-                                             int slot, int u0, int step, int lane) {
-    for (int u = u0; u < 16; u += step) {
-        const int p = u >> 2, b = 4 * (u & 3) + (lane >> 3), rr = lane & 7;
-        uint32_t r[4];
-        ldsm_x4_trans(tc::smem_u32(strip + p * WT_PLANE + (shift + 8 * b + rr) * 16), r);
-        stsm_x4(tc::smem_u32(op + (slot * 4 + p) * WT_GROUP + b * 128 + rr * 16), r);
-    }
-}
-// The same slot filled with a constant 16-bit pattern (0: zeros, 0x3F80: ones).
-__device__ __forceinline__ void wt_fill(uint8_t* op, int slot, uint32_t pat, int t0, int nt) {
-    const uint4 v = make_uint4(pat * 0x10001u, pat * 0x10001u, pat * 0x10001u, pat * 0x10001u);
-    uint4* q = (uint4*)(op + slot * 4 * WT_GROUP);
-    for (int k = t0; k < 4 * WT_GROUP / 16; k += nt) q[k] = v;
-}
-
-__global__ void __launch_bounds__(128, 1) wgrad32_tc_kernel(Dims d,
-                                                            const __grid_constant__ CUtensorMap amap,
-                                                            const __grid_constant__ CUtensorMap gmap,
-                                                            float* __restrict__ partial,
-                                                            int* status) {
+template <int MODE>
+__global__ void __launch_bounds__(WG_THREADS, 1) wgrad_tc_kernel(
+    Dims d, const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap amap_hi,
+    const __grid_constant__ CUtensorMap gmap, const __grid_constant__ CUtensorMap gmap_hi,
+    const float* __restrict__ gvec, const float* __restrict__ xin, float s,
+    float* __restrict__ partial, int* status) {
+    using Cfg = WgCfg<MODE>;
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t* stg = smem;                                   // 9 input strips + the gradient strip
-    uint8_t* abuf = smem + 10 * WT_STRIP;                   // 2 x A
-    uint8_t* bbuf = abuf + 2 * WT_ABUF;                     // 2 x B
-    uint64_t* bars = (uint64_t*)(bbuf + 2 * WT_BBUF);       // sbar, abar[2], drain
-    uint32_t* tslot = (uint32_t*)(bars + 4);
+    WgCtl* K = (WgCtl*)(smem + 2 * Cfg::STAGE + Cfg::XS);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // regions the copies and the builders never write stay zero
+    constexpr int ZOFF = MODE == WG_HID ? Cfg::OFF_G + 3 * WG_STRIP : Cfg::OFF_X;
+    constexpr int ZBYTES = MODE == WG_HID ? WG_STRIP : Cfg::XBYTES;
+    for (int k = tid; k < ZBYTES / 16; k += WG_THREADS) {
+        ((uint4*)(smem + ZOFF))[k] = make_uint4(0, 0, 0, 0);
+        ((uint4*)(smem + Cfg::STAGE + ZOFF))[k] = make_uint4(0, 0, 0, 0);
+    }
+    tc::fence_async_smem();
     if (tid == 0) {
-        for (int k = 0; k < 4; k++) tc::mbar_init(&bars[k], 1);
+        for (int k = 0; k < 2; k++) {
+            tc::mbar_init(&K->tfull[k], 1);
+            tc::mbar_init(&K->bfull[k], 4);
+            tc::mbar_init(&K->empty[k], Cfg::EMPTY_COUNT);
+        }
+        tc::mbar_init(&K->drain, 1);
+        K->abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) tc::tmem_alloc(tslot, 256);
+    if (warp == 0) tc::tmem_alloc(&K->tslot, Cfg::NCOL);
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
-    const uint32_t tmem = *tslot;
+    const uint32_t tmem = K->tslot;
     const int64_t nt = ntiles(d);
-    const int force_at = status[1] - 1;  // test hook: the wait for K block k gives up
-    constexpr uint32_t idesc = tc::idesc_bf16(TM, C);
-    bool ok = true;
-    int kb = 0, c = 0;
-    int64_t staged = -1;  // the K block whose copies were issued and not yet waited for
-    for (int64_t t = blockIdx.x; t < nt; t += gridDim.x, kb++) {
-        int b, z, y, x0;
-        tile_pos(d, t, b, z, y, x0);
-        if (tid == 0) {
-            uint32_t bytes = WT_STRIP_TX;  // the gradient strip
-            for (int q = 0; q < 9; q++) {
-                const int zz = z + q / 3 - 1, yy = y + q % 3 - 1;
-                if (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny) bytes += WT_STRIP_TX;
-            }
-            tc::fence_async_smem();
-            mbar_arrive_tx(&bars[0], bytes);
-            const int grow = (b * d.nz + z) * d.ny + y;
-            for (int kc = 0; kc < KCH; kc++)
-                tma_load_4d(stg + 9 * WT_STRIP + kc * WT_PLANE, &gmap, 0, x0 - 1, kc, grow, &bars[0]);
-            for (int q = 0; q < 9; q++) {
-                const int zz = z + q / 3 - 1, yy = y + q % 3 - 1;
-                if (!(zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny)) continue;
-                const int row = (b * d.nz + zz) * d.ny + yy;
-                for (int kc = 0; kc < KCH; kc++)
-                    tma_load_4d(stg + q * WT_STRIP + kc * WT_PLANE, &amap, 0, x0 - 1, kc, row,
-                                &bars[0]);
-            }
-        }
-        staged = kb;
-        bool got = tc::mbar_wait(&bars[0], (uint32_t)(kb & 1), WAIT_LIMIT) && kb != force_at;
-        if (!__syncthreads_and(got)) {
-            ok = false;
-            break;
-        }
-        staged = -1;
-        for (int mb = 0; mb < 7; mb++, c++) {
-            const int j = c & 1;
-            // the MMAs of use c - 2 of this A buffer (and, at mb 0, every MMA
-            // of K block kb - 2, the last reader of this B buffer) are done;
-            // a warp in which a wait gave up writes nothing (the transposes are
-            // warp-collective, so the decision is the warp's)
-            if (c >= 2 &&
-                !__all_sync(0xffffffffu,
-                            tc::mbar_wait(&bars[1 + j], (uint32_t)(((c >> 1) - 1) & 1), WAIT_LIMIT)))
-                ok = false;
-            uint8_t* A = abuf + j * WT_ABUF;
-            uint8_t* Bm = bbuf + (kb & 1) * WT_BBUF;
-            if (ok && mb == 0) wt_transpose(stg + 9 * WT_STRIP, 1, Bm, 0, warp, 4, lane);
-            for (int sl = 0; sl < 4 && ok; sl++) {
-                const int tap = 4 * mb + sl;
-                if (tap == 27) {
-                    wt_fill(A, sl, 0x3F80u, tid, 128);  // ones: the bias gradient
-                    continue;
+    volatile int* abort = &K->abort;
+    auto fail = [&]() {
+        if (!*abort) atomicOr(status, NR_FLAG_TIMEOUT);
+        *abort = 1;
+        __threadfence_block();
+    };
+    if (warp == 0) {
+        if (lane == 0) {
+            // producer
+            int64_t kb = 0, issued = 0;
+            for (int64_t t = blockIdx.x; t < nt && !*abort; t += gridDim.x, kb++) {
+                const int sg = (int)(kb & 1);
+                if (kb >= 2 &&
+                    !wait_live(&K->empty[sg], (uint32_t)(((kb >> 1) - 1) & 1), abort)) {
+                    fail();
+                    break;
                 }
-                const int q = tap / 3, dx = tap % 3;
-                const int zz = z + q / 3 - 1, yy = y + q % 3 - 1;
-                if (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny)
-                    wt_transpose(stg + q * WT_STRIP, dx, A, sl, warp, 4, lane);
-                else
-                    wt_fill(A, sl, 0u, tid, 128);
+                int b, z, y, x0;
+                tile_pos(d, t, b, z, y, x0);
+                uint8_t* st = smem + sg * Cfg::STAGE;
+                mbar_arrive_tx(&K->tfull[sg], Cfg::TX);
+                const int grow = (b * d.nz + z) * d.ny + y;
+                // gradient copy c starts at x0 + 1 - c (HID) / x0 - 1 (FIRST)
+                for (int c = 0; c < Cfg::NLOAD; c++)
+                    load_strip(st + Cfg::OFF_G + c * WG_STRIP, WG_PLANE, &gmap, &gmap_hi,
+                               MODE == WG_HID ? x0 + 2 - c : x0, grow, &K->tfull[sg]);
+                for (int q = 0; q < Cfg::NSTRIP; q++) {
+                    const int zz = z + q / 3 - 1, yy = y + q % 3 - 1;
+                    const int row = (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny)
+                                        ? (b * d.nz + zz) * d.ny + yy
+                                        : -1;
+                    load_strip(st + q * WG_STRIP, WG_PLANE, &amap, &amap_hi, x0, row,
+                               &K->tfull[sg]);
+                }
+                issued = kb + 1;
             }
-            tc::fence_async_smem();
-            if (!__syncthreads_and(ok)) {
-                ok = false;
-                break;
-            }
-            if (tid == 0) {
-                tc::fence_after();
-                const uint32_t sa = tc::smem_u32(A), sb = tc::smem_u32(Bm);
-#pragma unroll
-                for (int st = 0; st < TM / 16; st++)
-                    tc::mma_bf16(tmem + (uint32_t)(mb * 32), tc::sdesc(sa + st * 256, 128, WT_GROUP),
-                                 tc::sdesc(sb + st * 256, 128, WT_GROUP), idesc,
-                                 (kb > 0 || st > 0) ? 1u : 0u);
-                tc::commit(&bars[1 + j]);
+            // no copy may be in flight when the block exits
+            for (int64_t k = issued > 2 ? issued - 2 : 0; k < issued; k++) {
+                uint64_t* bar = &K->tfull[k & 1];
+                if (!tc::mbar_wait(bar, (uint32_t)((k >> 1) & 1), WAIT_LIMIT))
+                    tc::mbar_wait(bar, (uint32_t)((k >> 1) & 1), WAIT_LIMIT);
             }
         }
-        if (!ok) break;
-        tc::fence_async_smem();  // this block's reads of the staging precede the next copies
-        __syncthreads();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer.  Test hook: the workspace's second status word k + 1
+            // > 0 makes the wait for this CTA's K block k report giving up
+            // once it has in fact succeeded.
+            const int force_at = status[1] - 1;
+            int64_t kb = 0;
+            for (int64_t t = blockIdx.x; t < nt && !*abort; t += gridDim.x, kb++) {
+                const int sg = (int)(kb & 1);
+                const uint32_t par = (uint32_t)((kb >> 1) & 1);
+                bool got = wait_live(&K->tfull[sg], par, abort);
+                if (MODE != WG_HID && got) got = wait_live(&K->bfull[sg], par, abort);
+                if (kb == force_at) got = false;
+                if (!got) {
+                    fail();
+                    break;
+                }
+                tc::fence_after();
+                const uint32_t sb = tc::smem_u32(smem + sg * Cfg::STAGE);
+                if (MODE == WG_HID) {
+                    // columns 0-143: strips 0-3 and channels 0-15 of strip 4;
+                    // columns 144-287: the rest (from plane 2 of strip 4)
+#pragma unroll
+                    for (int k = 0; k < TM / 16; k++) {
+                        const uint64_t ad = tc::sdesc(sb + Cfg::OFF_G + k * 256, 128, WG_PLANE);
+                        const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
+                        tc::mma_bf16(tmem, ad, tc::sdesc(sb + 16 + k * 256, 128, WG_PLANE),
+                                     Cfg::IDESC, acc);
+                        tc::mma_bf16(tmem + 144, ad,
+                                     tc::sdesc(sb + 4 * WG_STRIP + 2 * WG_PLANE + 16 + k * 256,
+                                               128, WG_PLANE),
+                                     Cfg::IDESC, acc);
+                    }
+                } else if (MODE == WG_FIRST) {
+#pragma unroll
+                    for (int k = 0; k < TM / 16; k++)
+                        tc::mma_bf16(tmem, tc::sdesc(sb + Cfg::OFF_X + k * 256, 128, WG_GROUP),
+                                     tc::sdesc(sb + Cfg::OFF_G + 16 + k * 256, 128, WG_PLANE),
+                                     Cfg::IDESC, (kb > 0 || k > 0) ? 1u : 0u);
+                } else {
+                    for (int gi = 0; gi < 3; gi++) {
+                        const int g0 = gi == 0 ? 0 : (gi == 1 ? 4 : 5);
+#pragma unroll
+                        for (int dx = 0; dx < 3; dx++) {
+                            const uint32_t dacc = tmem + (uint32_t)((gi * 3 + dx) * 32);
+#pragma unroll
+                            for (int k = 0; k < TM / 16; k++)
+                                tc::mma_bf16(
+                                    dacc,
+                                    tc::sdesc(sb + g0 * WG_STRIP + dx * 16 + k * 256, 128, WG_PLANE),
+                                    tc::sdesc(sb + Cfg::OFF_X + k * 256, 128, WG_GROUP),
+                                    Cfg::IDESC, (kb > 0 || k > 0) ? 1u : 0u);
+                        }
+                    }
+                }
+                tc::commit(&K->empty[sg]);
+            }
+        }
+    } else {
+        // warps 2-5: the built operand and the bias sum
+        const int h = warp - 2;
+        float* xs = (float*)(smem + 2 * Cfg::STAGE) + h * 9 * WG_WIN;  // WG_FIRST
+        constexpr int NR = MODE == WG_FIRST ? (9 * WG_WIN + 31) / 32 : 1;
+        float r[NR];  // the next block's global data, in flight
+        float bacc = 0.f;
+        int64_t t = blockIdx.x;
+        if (MODE != WG_HID && t < nt) wg_fetch<MODE>(d, t, h, lane, gvec, xin, s, r);
+        for (int64_t kb = 0; t < nt && !*abort; t += gridDim.x, kb++) {
+            const int sg = (int)(kb & 1);
+            uint8_t* st = smem + sg * Cfg::STAGE;
+            if (MODE != WG_HID) {
+                if (!__all_sync(0xffffffffu,
+                                kb < 2 || wait_live(&K->empty[sg],
+                                                    (uint32_t)(((kb >> 1) - 1) & 1), abort))) {
+                    if (lane == 0) fail();
+                    break;
+                }
+                float cur[NR];
+#pragma unroll
+                for (int k = 0; k < NR; k++) cur[k] = r[k];
+                if (t + gridDim.x < nt) wg_fetch<MODE>(d, t + gridDim.x, h, lane, gvec, xin, s, r);
+                const int k = 32 * h + lane;
+                if (MODE == WG_LAST) {
+                    bacc += cur[0];
+                    wg_split_store(st + Cfg::OFF_X, 0, 1, k, cur[0]);
+                } else {
+                    __syncwarp();  // the previous block's reads of the window are done
+#pragma unroll
+                    for (int e = 0; e < NR; e++)
+                        if (lane + 32 * e < 9 * WG_WIN) xs[lane + 32 * e] = cur[e];
+                    __syncwarp();
+#pragma unroll
+                    for (int q = 0; q < 9; q++)
+#pragma unroll
+                        for (int dx = 0; dx < 3; dx++)
+                            wg_split_store(st + Cfg::OFF_X, 3 * q + dx, 32 + 3 * q + dx, k,
+                                           xs[q * WG_WIN + lane + dx]);
+                }
+                tc::fence_async_smem();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&K->bfull[sg]);
+            }
+            if (MODE != WG_LAST) {
+                if (!__all_sync(0xffffffffu,
+                                wait_live(&K->tfull[sg], (uint32_t)((kb >> 1) & 1), abort))) {
+                    if (lane == 0) fail();
+                    break;
+                }
+                // channel o = lane of x = 32 h .. 32 h + 31, in the gradient
+                // copy staged from x0 - 1 (row x + 1)
+                const uint8_t* gp = st + Cfg::OFF_G + (MODE == WG_HID ? 2 * WG_STRIP : 0) +
+                                    (lane >> 3) * WG_PLANE + (lane & 7) * 2;
+#pragma unroll 8
+                for (int x = 32 * h; x < 32 * h + 32; x++)
+                    bacc += __bfloat162float(*(const __nv_bfloat16*)(gp + (x + 1) * 16));
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&K->empty[sg]);
+            }
+        }
+        K->bsum[h][lane] = bacc;
     }
-    if (!ok && tid == 0) atomicOr(status, NR_FLAG_TIMEOUT);
-    // copies still in flight land, and every MMA issued completes, before TMEM goes
-    if (tid == 0 && staged >= 0 && !tc::mbar_wait(&bars[0], (uint32_t)(staged & 1), WAIT_LIMIT))
-        tc::mbar_wait(&bars[0], (uint32_t)(staged & 1), WAIT_LIMIT);
-    if (tid == 0) tc::commit(&bars[3]);
-    if (!tc::mbar_wait(&bars[3], 0, WAIT_LIMIT)) tc::mbar_wait(&bars[3], 0, WAIT_LIMIT);
+    // drain: every MMA issued has completed before TMEM is read or released
+    __syncthreads();
+    if (warp == 1 && lane == 0) tc::commit(&K->drain);
+    if (!tc::mbar_wait(&K->drain, 0, WAIT_LIMIT)) tc::mbar_wait(&K->drain, 0, WAIT_LIMIT);
     tc::fence_after();
-    if (ok && kb > 0) {
-        // TMEM lane 32 w + l = (tap 4 mb + w, input channel l), column o
-        const int64_t nchunk = gridDim.x;
-        for (int mb = 0; mb < 7; mb++) {
-            uint32_t acc[32];
-            tc::ld32(tmem, (uint32_t)(warp * 32), (uint32_t)(mb * 32), acc);
-            const int tap = 4 * mb + warp;
-            for (int o = 0; o < C; o++)
-                partial[(((int64_t)tap * C + o) * C + lane) * nchunk + blockIdx.x] =
-                    __uint_as_float(acc[o]);
+    const bool ok = *abort == 0;
+    float* prow = partial + (int64_t)blockIdx.x * 28 * (MODE == WG_HID ? C * C : C);
+    auto bias_of = [&](int o) {
+        return ((K->bsum[0][o] + K->bsum[1][o]) + K->bsum[2][o]) + K->bsum[3][o];
+    };
+    if (MODE == WG_HID) {
+        // TMEM lane 32 dx + o, column 32 q + i: dW[3 q + dx][o][i]
+        if (ok && warp < 3) {
+            for (int q = 0; q < 9; q++) {
+                uint32_t acc[32];
+                tc::ld32(tmem, (uint32_t)(warp * 32), (uint32_t)(q * 32), acc);
+                float4* dst = (float4*)(prow + ((3 * q + warp) * C + lane) * C);
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    dst[j] = make_float4(__uint_as_float(acc[4 * j]), __uint_as_float(acc[4 * j + 1]),
+                                         __uint_as_float(acc[4 * j + 2]),
+                                         __uint_as_float(acc[4 * j + 3]));
+            }
+        }
+        if (ok && warp == 3) prow[(27 * C + lane) * C] = bias_of(lane);
+    } else if (MODE == WG_FIRST) {
+        // rows 32 + tap (lo) of warp 1 meet rows tap (hi) of warp 0
+        float* lo = (float*)smem;  // the stages are idle now
+        uint32_t acc[32];
+        if (ok && warp == 1) {
+            tc::ld32(tmem, 32, 0, acc);
+            for (int o = 0; o < C; o++) lo[lane * C + o] = __uint_as_float(acc[o]);
+        }
+        __syncthreads();
+        if (ok && warp == 0) {
+            tc::ld32(tmem, 0, 0, acc);
+            if (lane < 27)
+                for (int o = 0; o < C; o++)
+                    prow[lane * C + o] = __uint_as_float(acc[o]) + lo[lane * C + o];
+        }
+        if (ok && warp == 2) prow[27 * C + lane] = bias_of(lane);
+    } else if (ok && warp < 4) {
+        // TMEM lane 32 w + i of block (gi, dx): strip g0 + w
+        for (int gi = 0; gi < 3; gi++) {
+            if (gi == 2 && warp < 3) continue;  // strips 5-7 again
+            const int q = (gi == 0 ? 0 : (gi == 1 ? 4 : 5)) + warp;
+            for (int dx = 0; dx < 3; dx++) {
+                uint32_t acc[32];
+                tc::ld32(tmem, (uint32_t)(warp * 32), (uint32_t)((gi * 3 + dx) * 32), acc);
+                prow[(3 * q + dx) * C + lane] = __uint_as_float(acc[0]) + __uint_as_float(acc[1]);
+            }
+        }
+        if (tid == 0) {
+            float sacc = 0.f;
+            for (int k = 0; k < 4 * C; k++) sacc += K->bsum[k >> 5][k & 31];
+            prow[27 * C] = sacc;
         }
     }
     tc::fence_before();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 256);
+    if (warp == 0) tc::tmem_dealloc(tmem, Cfg::NCOL);
 }
 
-// grad[tap][o][i] (and grad_b[o] from tap 27, i = 0) = sum over chunks, in order.
-__global__ void wgrad_reduce_kernel(const float* __restrict__ partial, int64_t nchunk, int nout,
-                                    int ni, float* __restrict__ gw, float* __restrict__ gb) {
+// grad[tap][o][i] (and grad_b[o] from tap 27, i = 0) = the sum of the CTAs'
+// partials (partial[cta][e], e = tap nout + o ni + i).  A block of 8 warps
+// takes 32 consecutive e: warp w adds, in CTA order, the CTAs of its eighth of
+// the range for the lane's e (coalesced rows), and warp 0 adds the eight
+// subtotals in warp order -- a fixed order for a given CTA count.
+__global__ void __launch_bounds__(256) wgrad_reduce_kernel(const float* __restrict__ partial,
+                                                           int64_t nchunk, int nout, int ni,
+                                                           float* __restrict__ gw,
+                                                           float* __restrict__ gb) {
+    __shared__ double sub[8][32];
     const int64_t n = 28LL * nout;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        const float* p = partial + e * nchunk;
-        double s = 0.0;
-        for (int64_t c = 0; c < nchunk; c++) s += p[c];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t e = (int64_t)blockIdx.x * 32 + lane;
+    const int64_t c0 = nchunk * w / 8, c1 = nchunk * (w + 1) / 8;
+    double s = 0.0;
+    if (e < n) {
+        int64_t c = c0;
+        for (; c + 4 <= c1; c += 4) {
+            const float a0 = partial[c * n + e], a1 = partial[(c + 1) * n + e];
+            const float a2 = partial[(c + 2) * n + e], a3 = partial[(c + 3) * n + e];
+            s += a0;
+            s += a1;
+            s += a2;
+            s += a3;
+        }
+        for (; c < c1; c++) s += partial[c * n + e];
+    }
+    sub[w][lane] = s;
+    __syncthreads();
+    if (w == 0 && e < n) {
+        double t = 0.0;
+        for (int k = 0; k < 8; k++) t += sub[k][lane];
         const int tap = (int)(e / nout), oi = (int)(e % nout);
-        if (tap < 27) gw[e] = (float)s;
-        else if (oi % ni == 0) gb[oi / ni] = (float)s;
+        if (tap < 27) gw[e] = (float)t;
+        else if (oi % ni == 0) gb[oi / ni] = (float)t;
     }
 }
 
@@ -774,13 +902,14 @@ __global__ void loss_kernel(const float* __restrict__ f, const float* __restrict
     }
 }
 
+// One warp: lane l adds partials l, l + 32, ...; then a fixed shuffle tree.
 __global__ void loss_final_kernel(const double* __restrict__ partial, int n, int64_t V,
                                   double* __restrict__ out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double t = 0.0;
-        for (int k = 0; k < n; k++) t += partial[k];
-        out[0] = t / (double)V;
-    }
+    const int lane = threadIdx.x & 31;
+    double t = 0.0;
+    for (int k = lane; k < n; k += 32) t += partial[k];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) out[0] = t / (double)V;
 }
 
 // Adam (Kingma & Ba 2015) with bias correction, FP32 master parameters.
@@ -860,7 +989,7 @@ static WSL layout(const Dims& d, bool training) {
     const int nact = training ? 5 : 2;
     for (int k = 0; k < nact; k++) L.act[k] = take((size_t)V * C * 2);
     L.f = take((size_t)V * 4);
-    L.nchunk = (V + WG_CHUNK - 1) / WG_CHUNK;
+    L.nchunk = ntiles(d) < WG_MAXCTA ? ntiles(d) : WG_MAXCTA;  // CTAs of a weight gradient
     L.lblocks = 1024;
     if (training) {
         for (int l = 1; l < 5; l++) L.pk_bwd[l] = take(PK_HID);
@@ -889,37 +1018,44 @@ static int sm_count() {
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encode_fn();
 namespace cnn {
 
-// The TMA map of an activation tensor (act_off's layout) seen as (8 channels,
-// nx, 4 K chunks, R rows): one box is one K chunk of 130 consecutive x, a
-// contiguous 2080-byte block away from the row ends (zeros outside them).
-static bool act_map(const Dims& d, const __nv_bfloat16* in, CUtensorMap* map) {
+// The TMA maps of an activation tensor (act_off's layout) seen as (2 nx
+// 8-byte units, 4 K chunks, R rows): one K chunk of a row is one contiguous
+// run; `lo` boxes are 128 units (strip rows 0-63), `hi` boxes 132 units (rows
+// 64-129).  Zeros outside the tensor.
+struct ActMaps {
+    CUtensorMap lo, hi;
+};
+static bool act_maps(const Dims& d, const __nv_bfloat16* in, ActMaps* m) {
     auto enc = tensor_map_encode_fn();
     if (!enc || ((uintptr_t)in & 15) != 0) return false;
     const cuuint64_t rows = (cuuint64_t)d.ny * d.nz * d.nb;
-    const cuuint64_t dims[4] = {8, (cuuint64_t)d.nx, (cuuint64_t)KCH, rows};
-    const cuuint64_t strides[3] = {16, (cuuint64_t)d.nx * 16, (cuuint64_t)d.nx * C * 2};
-    const cuuint32_t box[4] = {8, (cuuint32_t)SROWS, 1, 1};
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
-    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)in, dims, strides, box, estr,
-               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-               CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    const cuuint64_t dims[3] = {(cuuint64_t)d.nx * 2, (cuuint64_t)KCH, rows};
+    const cuuint64_t strides[2] = {(cuuint64_t)d.nx * 16, (cuuint64_t)d.nx * C * 2};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const cuuint32_t box_lo[3] = {128, 1, 1}, box_hi[3] = {132, 1, 1};
+    auto one = [&](CUtensorMap* map, const cuuint32_t* box) {
+        return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, (void*)in, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    };
+    return one(&m->lo, box_lo) && one(&m->hi, box_hi);
 }
 
 template <int NOUT, int EPI>
 static nr_status launch_conv32(const Dims& d, const __nv_bfloat16* in, const __nv_bfloat16* wpk,
                                const float* bias, void* out, const __nv_bfloat16* mask,
                                int* status, cudaStream_t s) {
-    CUtensorMap map;
-    if (!act_map(d, in, &map)) return NR_ERR_CUDA;  // the input cannot be described for TMA
+    ActMaps map;
+    if (!act_maps(d, in, &map)) return NR_ERR_CUDA;  // the input cannot be described for TMA
     const size_t smem = (size_t)TSTAGE * TSTRIP + 27 * NOUT * C * 2 + sizeof(TmaCtl);
     if (cudaFuncSetAttribute(conv32_tma_kernel<NOUT, EPI>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return NR_ERR_CUDA;
     const int64_t nt = ntiles(d);
     const int grid = (int)(nt < (int64_t)sm_count() * 2 ? nt : (int64_t)sm_count() * 2);
-    conv32_tma_kernel<NOUT, EPI><<<grid, T_THREADS, smem, s>>>(d, map, wpk, bias, out, mask,
-                                                               status);
+    conv32_tma_kernel<NOUT, EPI><<<grid, T_THREADS, smem, s>>>(d, map.lo, map.hi, wpk, bias, out,
+                                                               mask, status);
     return launch_status();
 }
 
@@ -970,39 +1106,46 @@ __global__ void target_kernel(const float* __restrict__ x, const float* __restri
         r[v] = s * (t[v] - x[v]);
 }
 
+template <int MODE>
+static nr_status launch_wgrad(const Dims& d, const ActMaps& am, const ActMaps& gm,
+                              const float* gvec, const float* xin, float s, float* part,
+                              int* status, int64_t nch, cudaStream_t st) {
+    if (cudaFuncSetAttribute(wgrad_tc_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             WgCfg<MODE>::SMEM) != cudaSuccess)
+        return NR_ERR_CUDA;
+    wgrad_tc_kernel<MODE><<<(unsigned)nch, WG_THREADS, WgCfg<MODE>::SMEM, st>>>(
+        d, am.lo, am.hi, gm.lo, gm.hi, gvec, xin, s, part, status);
+    return launch_status();
+}
+
+// Weight and bias gradients of layer l (0-based) into grad: the tensor-core
+// GEMM (one partial per CTA), then the fixed-order reduction.  Layer 0 reads
+// the FP32 input volume (times s), layer 5 the FP32 gradient of the output.
 static nr_status wgrad(const Dims& d, int l, const void* g, const void* in, float s, char* ws,
                        const WSL& L, float* grad, int* status, cudaStream_t st) {
     int64_t wo[6], bo[6], P;
     param_offsets(wo, bo, &P);
     float* part = (float*)(ws + L.part);
-    const dim3 grid((unsigned)L.nchunk, 28);
-    int nout, ni;
+    const int64_t nt = ntiles(d);
+    int64_t nch = nt < (int64_t)sm_count() ? nt : (int64_t)sm_count();
+    if (nch > L.nchunk) nch = L.nchunk;
+    ActMaps am{}, gm{};  // a map a mode does not read stays zero
+    if (l > 0 && !act_maps(d, (const __nv_bfloat16*)in, &am)) return NR_ERR_CUDA;
+    if (l < 5 && !act_maps(d, (const __nv_bfloat16*)g, &gm)) return NR_ERR_CUDA;
+    nr_status e;
+    int nout = C, ni = C;
     if (l == 0) {
-        wgrad_thin_kernel<1, C><<<grid, 32, 0, st>>>(d, g, in, s, part);
-        nout = C;
+        e = launch_wgrad<WG_FIRST>(d, am, gm, nullptr, (const float*)in, s, part, status, nch, st);
         ni = 1;
     } else if (l == 5) {
-        wgrad_thin_kernel<C, 1><<<grid, 32, 0, st>>>(d, g, in, 1.f, part);
-        nout = C;
-        ni = C;
+        e = launch_wgrad<WG_LAST>(d, am, gm, (const float*)g, nullptr, 1.f, part, status, nch, st);
     } else {
-        // the tensor-core form: one partial per CTA (at most L.nchunk CTAs)
-        CUtensorMap am, gm;
-        if (!act_map(d, (const __nv_bfloat16*)in, &am) || !act_map(d, (const __nv_bfloat16*)g, &gm))
-            return NR_ERR_CUDA;
-        if (cudaFuncSetAttribute(wgrad32_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 WT_SMEM) != cudaSuccess)
-            return NR_ERR_CUDA;
-        const int64_t nt = ntiles(d);
-        int64_t nch = nt < (int64_t)sm_count() ? nt : (int64_t)sm_count();
-        if (nch > L.nchunk) nch = L.nchunk;
-        wgrad32_tc_kernel<<<(unsigned)nch, 128, WT_SMEM, st>>>(d, am, gm, part, status);
-        wgrad_reduce_kernel<<<(28 * C * C + 255) / 256, 256, 0, st>>>(part, nch, C * C, C,
-                                                                      grad + wo[l], grad + bo[l]);
-        return launch_status();
+        e = launch_wgrad<WG_HID>(d, am, gm, nullptr, nullptr, 1.f, part, status, nch, st);
+        nout = C * C;
     }
-    wgrad_reduce_kernel<<<(28 * nout + 255) / 256, 256, 0, st>>>(part, L.nchunk, nout, ni,
-                                                                 grad + wo[l], grad + bo[l]);
+    if (e != NR_OK) return e;
+    wgrad_reduce_kernel<<<(28 * nout + 31) / 32, 256, 0, st>>>(part, nch, nout, ni, grad + wo[l],
+                                                               grad + bo[l]);
     return launch_status();
 }
 

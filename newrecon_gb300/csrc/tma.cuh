@@ -8,7 +8,7 @@
 
 namespace nr {
 
-__device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, int x, int y,
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y,
                                             int z, uint64_t* bar) {
     asm volatile(
         "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
