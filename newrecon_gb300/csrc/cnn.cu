@@ -14,15 +14,14 @@
 // 130 input rows (x0-1 .. x0+128, zero outside the volume) into shared memory
 // in the K-major core-matrix layout with rows 16 bytes apart; the three dx
 // taps are the same strip read from row offsets 0, 1, 2 (descriptor start +
-// 16 B), so each input row is staged 9 times per tile instead of 27.  The
-// strips arrive by TMA (activations are stored in 8-channel planes so that a
-// strip's K chunk is one contiguous block); a producer warp, an MMA warp and
-// four epilogue warps overlap staging, MMAs and stores (conv32_tma_kernel).
-// Weights of all 27 taps stay in shared memory.  1-channel inputs gather the
-// 27 neighbours into one K = 32 row instead.  Weight gradients of the 32 -> 32
-// layers are a GEMM over voxels on the tensor cores (wgrad32_tc_kernel); those
-// of the 1-channel layers are per-tap outer products on the CUDA cores.  Both
-// end in the same fixed-order reduction of per-block partials.
+// 16 B).  The strips arrive by TMA (activations are stored in 8-channel planes
+// so that a strip's K chunk is one contiguous block); a CTA walks along y so
+// that each staged input row serves the three output rows that read it, and a
+// producer warp, an MMA warp and two groups of epilogue warps overlap staging,
+// MMAs and stores (conv32_walk_kernel).  Weights of all 27 taps stay in shared
+// memory.  1-channel inputs gather the 27 neighbours into one K = 32 row
+// instead.  Weight gradients are GEMMs over voxels on the tensor cores
+// (wgrad_tc_kernel), ending in a fixed-order reduction of per-CTA partials.
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
@@ -109,44 +108,13 @@ __device__ __forceinline__ void tile_pos(const Dims& d, int64_t t, int& b, int& 
     b = (int)(row / d.nz);
 }
 
-// ---- conv32 on a TMA + tcgen05 pipeline -------------------------------------
-// 32-channel input, NOUT = 32 (hidden / dgrad) or 16 (the last layer, output
-// channel 0 real) outputs; weights: 27 packed taps of NOUT x 32.  The work is
-// split between warps so that staging, MMAs and the epilogue overlap:
-//   warp 4 (one lane)  producer: loads each strip by TMA -- per 16-byte K
-//                      chunk one contiguous block of the plane layout, in two
-//                      boxes (load_strip) -- so the strip
-//                      lands in the K-major core-matrix layout with zeros
-//                      outside the volume in x, into a ring of TSTAGE stages
-//                      ("full": the bytes landed); strips outside the volume
-//                      in z or y are not loaded;
-//   warp 5 (one lane)  MMA issuer: 6 MMAs per loaded strip into one of two
-//                      TMEM accumulators (tiles alternate); tcgen05.commit
-//                      frees the stage ("empty") and, after the tile's last
-//                      strip, marks the accumulator full;
-//   warps 0-3          epilogue: read their 32 TMEM lanes of the finished
-//                      accumulator, hand it back ("acc empty"), then apply
-//                      bias / ReLU / mask and store -- while the MMAs of the
-//                      next tile run into the other accumulator.
-// Every wait is bounded and also gives up once another role has aborted; a
-// role that gives up flags NR_FLAG_TIMEOUT and aborts the block.  Before TMEM
-// is released the issuer's MMAs are drained, and the producer waits for
-// every copy it issued, so nothing is in flight when the block exits.
+// ---- strip staging shared by the convolution and the weight gradient ------
+// A strip is 130 input rows (x0 - 1 .. x0 + 128) of one (patch, z, y) row in
+// four planes of 8 channels, each plane a K-major core-matrix column block
+// (rows 16 bytes apart) for the MMAs.
 constexpr int PLANE = 2176;                           // one K-chunk plane: 130 rows x 16 B, 128-B aligned
 constexpr int TSTRIP = KCH * PLANE;                   // 8704 bytes per staged strip
-// Strips in flight per CTA.  Two CTAs per SM with 6 stages each measured
-// faster than one CTA per SM with 18 (25.9 against 40.7 ms for the network on
-// the clinical volume, activations then channels-last): two CTAs run two
-// chains of waits.
-constexpr int TSTAGE = 6;
-constexpr int T_THREADS = 192;
 constexpr uint32_t STRIP_TX = (uint32_t)KCH * SROWS * 16;  // bytes the four boxes deliver
-
-struct TmaCtl {
-    uint64_t full[TSTAGE], empty[TSTAGE], accf[2], acce[2], drain;
-    uint32_t tslot;
-    int abort;
-};
 
 // One strip (130 rows x 4 K-chunk planes, plane stride `pstride`) of row
 // `row` from x0 - 1 by TMA.  The activation tensor is mapped as (2 nx 8-byte
@@ -173,22 +141,111 @@ __device__ __forceinline__ bool wait_live(uint64_t* bar, uint32_t parity, volati
     return false;
 }
 
+// ---- conv32: TMA + tcgen05, walking along y -----------------------------------
+// 32-channel input, NOUT = 32 (hidden / input gradient) or 16 (the last layer,
+// output channel 0 real) outputs; weights: 27 packed taps of NOUT x 32; one
+// output tile (128 x of a row) per TMEM accumulator, staging shared between
+// neighbouring output rows.  A work item is a run of up to L output
+// rows y0 .. y0 + L - 1 of one column (patch b, plane z, x tile); its tiles
+// read the row-sets Y = y0 - 1 .. y0 + L, a row-set being the strips of input
+// row Y in planes z - 1, z, z + 1.  Each row-set is loaded once into a ring of
+// W_R slots and serves the up to three tiles that read it, so an input row is
+// staged about (L + 2) / L times per plane instead of nine.  A strip outside
+// the patch is loaded from row -1 (zero-filled), so that every tile issues the
+// same 54 MMAs, with descriptors formed as base + compile-time offset.
+//   warp 8 (one lane)  producer: row-sets in order into the ring ("full"),
+//                      after the slot's previous row-set was released;
+//   warp 9 (one lane)  MMA issuer: per tile the row-sets i, i + 1, i + 2 of
+//                      the item, 6 MMAs per valid strip, into accumulator
+//                      lt & 1; row-set i is released (tcgen05.commit to its
+//                      "empty") right after its MMAs -- its last use -- and
+//                      the item's last two after its last tile;
+//   warps 0-3, 4-7     two epilogue groups, group g for the tiles lt with
+//                      lt & 1 == g, so that two epilogues run at once.
+// One CTA per SM (the ring and all 27 taps' weights).  Every wait is bounded
+// and also gives up once another role has aborted; a role that gives up flags
+// NR_FLAG_TIMEOUT and aborts the block.  Before TMEM is released the issuer's
+// MMAs are drained, and the producer waits for every copy it issued.
+// Measured against the previous form (nine strips per tile, two CTAs per SM):
+// L2 traffic falls from 67 % to 8 % of its throughput and the network's
+// forward pass on the clinical volume from 22.6-23.0 to 22.5 ms -- the MMAs'
+// front end (sm__pipe_tc 57 % with the math at 14 %: an N = 32 MMA reads 5 KB
+// of operands for 65 K MACs) paces both.
+constexpr int W_R = 6;                                 // row-set slots
+constexpr int W_SET = 3 * TSTRIP;                      // 26112 bytes
+constexpr int W_THREADS = 320;
+
+struct WalkCtl {
+    uint64_t full[W_R], empty[W_R], accf[2], acce[2], drain;
+    uint32_t tslot;
+    int abort;
+};
+
+struct WalkPlan {
+    int L, nchunk;
+    int64_t nitems;
+};
+
+// Column (b, z, x0) and rows y0 .. y0 + ly - 1 of item it.
+__device__ __forceinline__ void item_pos(const Dims& d, const WalkPlan& w, int64_t it, int& b,
+                                         int& z, int& x0, int& y0, int& ly) {
+    const int xt = xtiles(d);
+    int64_t col = it / w.nchunk;
+    const int ch = (int)(it - col * w.nchunk);
+    x0 = (int)(col % xt) * TM;
+    col /= xt;
+    z = (int)(col % d.nz);
+    b = (int)(col / d.nz);
+    y0 = ch * w.L;
+    ly = min(w.L, d.ny - y0);
+}
+
+// Epilogue of output row `row` (one (patch, z, y) row), voxel x.
+template <int EPI>
+__device__ __forceinline__ void epilogue_rx(const uint32_t* acc, int64_t row, int x, int nx,
+                                            const float* __restrict__ bias, void* out,
+                                            const __nv_bfloat16* __restrict__ mask) {
+    if (EPI == EPI_RESID) {
+        ((float*)out)[row * nx + x] = __uint_as_float(acc[0]) + bias[0];
+        return;
+    }
+    const int64_t o0 = row * KCH * (int64_t)nx * 8 + (int64_t)x * 8;  // chunk q at o0 + q nx 8
+    __align__(16) __nv_bfloat16 o[C];
+    if (EPI == EPI_RELU) {
+#pragma unroll
+        for (int c = 0; c < C; c++)
+            o[c] = __float2bfloat16(fmaxf(__uint_as_float(acc[c]) + bias[c], 0.f));
+    } else {
+        __align__(16) __nv_bfloat16 m[C];
+#pragma unroll
+        for (int q = 0; q < KCH; q++)
+            ((uint4*)m)[q] = __ldg((const uint4*)(mask + o0 + (int64_t)q * nx * 8));
+#pragma unroll
+        for (int c = 0; c < C; c++)
+            o[c] = __bfloat162float(m[c]) > 0.f ? __float2bfloat16(__uint_as_float(acc[c]))
+                                                : __float2bfloat16(0.f);
+    }
+#pragma unroll
+    for (int q = 0; q < KCH; q++)
+        *(uint4*)((__nv_bfloat16*)out + o0 + (int64_t)q * nx * 8) = ((const uint4*)o)[q];
+}
+
 template <int NOUT, int EPI>
-__global__ void __launch_bounds__(T_THREADS) conv32_tma_kernel(
-    Dims d, const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap amap_hi,
-    const __nv_bfloat16* __restrict__ wpk,
+__global__ void __launch_bounds__(W_THREADS, 1) conv32_walk_kernel(
+    Dims d, WalkPlan wp, const __grid_constant__ CUtensorMap amap,
+    const __grid_constant__ CUtensorMap amap_hi, const __nv_bfloat16* __restrict__ wpk,
     const float* __restrict__ bias, void* out, const __nv_bfloat16* __restrict__ mask,
     int* status) {
     constexpr int WBYTES = 27 * NOUT * C * 2;
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t* sA = smem;
-    uint8_t* sW = smem + TSTAGE * TSTRIP;
-    TmaCtl* K = (TmaCtl*)(sW + WBYTES);
+    uint8_t* ring = smem;
+    uint8_t* sW = smem + W_R * W_SET;
+    WalkCtl* K = (WalkCtl*)(sW + WBYTES);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int k = tid; k < WBYTES / 16; k += T_THREADS)
+    for (int k = tid; k < WBYTES / 16; k += W_THREADS)
         ((uint4*)sW)[k] = __ldg((const uint4*)wpk + k);
     if (tid == 0) {
-        for (int s = 0; s < TSTAGE; s++) {
+        for (int s = 0; s < W_R; s++) {
             tc::mbar_init(&K->full[s], 1);
             tc::mbar_init(&K->empty[s], 1);
         }
@@ -206,133 +263,140 @@ __global__ void __launch_bounds__(T_THREADS) conv32_tma_kernel(
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = K->tslot;
-    const int64_t nt = ntiles(d);
     volatile int* abort = &K->abort;
     auto fail = [&]() {
         if (!*abort) atomicOr(status, NR_FLAG_TIMEOUT);
         *abort = 1;
         __threadfence_block();
     };
-    if (warp == 4) {
+    auto strip_ok = [&](int zz, int yy) { return zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny; };
+    if (warp == 8) {
         if (lane == 0) {
             // producer
-            int64_t qg = 0, issued = 0;
-            for (int64_t t = blockIdx.x; t < nt && !*abort; t += gridDim.x) {
-                int b, z, y, x0;
-                tile_pos(d, t, b, z, y, x0);
-                for (int q = 0; q < 9; q++, qg++) {
-                    const int s = (int)(qg % TSTAGE);
-                    if (qg >= TSTAGE &&
-                        !wait_live(&K->empty[s], (uint32_t)((qg / TSTAGE - 1) & 1), abort)) {
+            int64_t G = 0, issued = 0;
+            bool stop = false;
+            for (int64_t it = blockIdx.x; it < wp.nitems && !stop && !*abort; it += gridDim.x) {
+                int b, z, x0, y0, ly;
+                item_pos(d, wp, it, b, z, x0, y0, ly);
+                for (int j = 0; j < ly + 2; j++, G++) {
+                    const int s = (int)(G % W_R);
+                    if (G >= W_R &&
+                        !wait_live(&K->empty[s], (uint32_t)((G / W_R - 1) & 1), abort)) {
                         fail();
+                        stop = true;
                         break;
                     }
-                    const int zz = z + q / 3 - 1, yy = y + q % 3 - 1;
-                    if (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny) {
-                        const int row = (b * d.nz + zz) * d.ny + yy;
-                        uint8_t* st = sA + s * TSTRIP;
-                        tc::fence_async_smem();
-                        mbar_arrive_tx(&K->full[s], STRIP_TX);
-                        load_strip(st, PLANE, &amap, &amap_hi, x0, row, &K->full[s]);
-                    } else {
-                        mbar_arrive(&K->full[s]);
-                    }
-                    issued = qg + 1;
+                    const int Y = y0 - 1 + j;
+                    mbar_arrive_tx(&K->full[s], 3 * STRIP_TX);
+                    for (int dz = 0; dz < 3; dz++)
+                        load_strip(ring + s * W_SET + dz * TSTRIP, PLANE, &amap, &amap_hi, x0,
+                                   strip_ok(z + dz - 1, Y) ? (b * d.nz + z + dz - 1) * d.ny + Y : -1,
+                                   &K->full[s]);
+                    issued = G + 1;
                 }
             }
             // no copy may be in flight when the block exits
-            for (int64_t k = issued > TSTAGE ? issued - TSTAGE : 0; k < issued; k++) {
-                uint64_t* bar = &K->full[k % TSTAGE];
-                if (!tc::mbar_wait(bar, (uint32_t)((k / TSTAGE) & 1), WAIT_LIMIT))
-                    tc::mbar_wait(bar, (uint32_t)((k / TSTAGE) & 1), WAIT_LIMIT);
+            for (int64_t k = issued > W_R ? issued - W_R : 0; k < issued; k++) {
+                uint64_t* bar = &K->full[k % W_R];
+                if (!tc::mbar_wait(bar, (uint32_t)((k / W_R) & 1), WAIT_LIMIT))
+                    tc::mbar_wait(bar, (uint32_t)((k / W_R) & 1), WAIT_LIMIT);
             }
         }
-    } else if (warp == 5) {
+    } else if (warp == 9) {
         if (lane == 0) {
             // MMA issuer
             constexpr uint32_t idesc = tc::idesc_bf16(TM, NOUT);
-            const uint32_t sw = tc::smem_u32(sW);
-            int64_t qg = 0;
+            const uint64_t ad0 = tc::sdesc(tc::smem_u32(ring), PLANE, 128);
+            const uint64_t bd0 = tc::sdesc(tc::smem_u32(sW), 128, 512);
+            int64_t G = 0;
             int lt = 0;
-            for (int64_t t = blockIdx.x; t < nt && !*abort; t += gridDim.x, lt++) {
-                int b, z, y, x0;
-                tile_pos(d, t, b, z, y, x0);
-                const int a = lt & 1;
-                if (lt >= 2 && !wait_live(&K->acce[a], (uint32_t)(((lt >> 1) - 1) & 1), abort)) {
-                    fail();
-                    break;
-                }
-                tc::fence_after();
-                const uint32_t dacc = tmem + (uint32_t)(a * 32);
-                bool first = true, ok = true;
-                for (int q = 0; q < 9; q++, qg++) {
-                    const int s = (int)(qg % TSTAGE);
-                    if (!wait_live(&K->full[s], (uint32_t)((qg / TSTAGE) & 1), abort)) {
-                        ok = false;
+            bool stop = false;
+            for (int64_t it = blockIdx.x; it < wp.nitems && !stop && !*abort; it += gridDim.x) {
+                int b, z, x0, y0, ly;
+                item_pos(d, wp, it, b, z, x0, y0, ly);
+                for (int i = 0; i < ly && !stop; i++, lt++) {
+                    const int a = lt & 1;
+                    if (lt >= 2 &&
+                        !wait_live(&K->acce[a], (uint32_t)(((lt >> 1) - 1) & 1), abort)) {
+                        fail();
+                        stop = true;
                         break;
                     }
-                    const int zz = z + q / 3 - 1, yy = y + q % 3 - 1;
-                    if (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny) {
-                        tc::fence_after();
-                        const uint32_t sa = tc::smem_u32(sA + s * TSTRIP);
+                    tc::fence_after();
+                    const uint32_t dacc = tmem + (uint32_t)(a * 32);
 #pragma unroll
-                        for (int dx = 0; dx < 3; dx++) {
-                            const int tap = q * 3 + dx;
-#pragma unroll
-                            for (int j = 0; j < 2; j++) {
-                                const uint64_t ad =
-                                    tc::sdesc(sa + dx * 16 + j * 2 * PLANE, PLANE, 128);
-                                const uint64_t bd =
-                                    tc::sdesc(sw + tap * NOUT * C * 2 + j * 256, 128, 512);
-                                tc::mma_bf16(dacc, ad, bd, idesc, first ? 0u : 1u);
-                                first = false;
-                            }
+                    for (int dy = 0; dy < 3; dy++) {
+                        const int64_t gs = G + i + dy;
+                        const int s = (int)(gs % W_R);
+                        if ((i == 0 || dy == 2) &&
+                            !wait_live(&K->full[s], (uint32_t)((gs / W_R) & 1), abort)) {
+                            fail();
+                            stop = true;
+                            break;
                         }
-                        tc::commit(&K->empty[s]);
-                    } else {
-                        mbar_arrive(&K->empty[s]);
+                        tc::fence_after();
+                        // descriptors are linear in the address: base + offset / 16
+                        const uint64_t adr = ad0 + (uint64_t)((s * W_SET) >> 4);
+#pragma unroll
+                        for (int dz = 0; dz < 3; dz++)
+#pragma unroll
+                            for (int dx = 0; dx < 3; dx++)
+#pragma unroll
+                                for (int j = 0; j < 2; j++) {
+                                    const int tap = dz * 9 + dy * 3 + dx;
+                                    tc::mma_bf16(
+                                        dacc,
+                                        adr + (uint64_t)((dz * TSTRIP + dx * 16 + j * 2 * PLANE) >> 4),
+                                        bd0 + (uint64_t)((tap * NOUT * C * 2 + j * 256) >> 4), idesc,
+                                        (dy | dz | dx | j) ? 1u : 0u);
+                                }
+                        // row-set i is not read after this tile; the last tile
+                        // of the item also frees row-sets ly and ly + 1
+                        if (dy == 0 || i == ly - 1) tc::commit(&K->empty[s]);
                     }
+                    if (stop) break;
+                    tc::commit(&K->accf[a]);
                 }
-                if (!ok) {
-                    fail();
-                    break;
-                }
-                tc::commit(&K->accf[a]);
+                G += ly + 2;
             }
         }
     } else {
-        // epilogue warps 0-3: row tid of each tile.  Test hook: the
-        // workspace's second status word k + 1 > 0 makes the wait for this
-        // CTA's tile k report giving up once it has in fact succeeded (its
-        // MMAs are complete), so the failure path runs with nothing in flight.
+        // epilogue group g = warp / 4: TMEM lanes 32 (warp % 4) .. + 31 of the
+        // tiles lt with lt & 1 == g.  Test hook: the workspace's second status
+        // word k + 1 > 0 makes the wait for this CTA's tile k report giving up
+        // once it has in fact succeeded.
+        const int g = warp >> 2, wq = warp & 3;
         const int force_at = status[1] - 1;
         int lt = 0;
-        for (int64_t t = blockIdx.x; t < nt; t += gridDim.x, lt++) {
-            int b, z, y, x0;
-            tile_pos(d, t, b, z, y, x0);
-            const int a = lt & 1;
-            bool got = wait_live(&K->accf[a], (uint32_t)((lt >> 1) & 1), abort);
-            if (lt == force_at) got = false;
-            if (!got) {
-                if (lane == 0) fail();
-                break;
-            }
-            tc::fence_after();
-            uint32_t acc[32];
-            tc::ld32(tmem, (uint32_t)(warp * 32), (uint32_t)(a * 32), acc);
-            tc::fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&K->acce[a]);
-            const int x = x0 + tid;
-            if (x < d.nx) {
-                const int64_t v = (((int64_t)b * d.nz + z) * d.ny + y) * d.nx + x;
-                epilogue<EPI>(acc, v, d.nx, bias, out, mask);
+        bool stop = false;
+        for (int64_t it = blockIdx.x; it < wp.nitems && !stop; it += gridDim.x) {
+            int b, z, x0, y0, ly;
+            item_pos(d, wp, it, b, z, x0, y0, ly);
+            for (int i = 0; i < ly; i++, lt++) {
+                if ((lt & 1) != g) continue;
+                bool got = wait_live(&K->accf[g], (uint32_t)((lt >> 1) & 1), abort);
+                if (lt == force_at) got = false;
+                if (!got) {
+                    if (lane == 0) fail();
+                    stop = true;
+                    break;
+                }
+                tc::fence_after();
+                uint32_t acc[32];
+                tc::ld32(tmem, (uint32_t)(wq * 32), (uint32_t)(g * 32), acc);
+                tc::fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&K->acce[g]);
+                const int x = x0 + wq * 32 + lane;
+                if (x < d.nx)
+                    epilogue_rx<EPI>(acc, ((int64_t)b * d.nz + z) * d.ny + y0 + i, x, d.nx, bias,
+                                     out, mask);
             }
         }
     }
     // drain: every MMA issued has completed before TMEM is released
     __syncthreads();
-    if (warp == 5 && lane == 0) tc::commit(&K->drain);
+    if (warp == 9 && lane == 0) tc::commit(&K->drain);
     if (!tc::mbar_wait(&K->drain, 0, WAIT_LIMIT)) tc::mbar_wait(&K->drain, 0, WAIT_LIMIT);
     tc::fence_before();
     __syncthreads();
@@ -366,7 +430,7 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restr
     int ntile = 0;
     int ncommit = 0;
     bool ok = true;
-    const int force_at = status[1] - 1;  // test hook, as in conv32_kernel
+    const int force_at = status[1] - 1;  // test hook, as in conv32_walk_kernel
     for (int64_t t = blockIdx.x; t < nt; t += gridDim.x) {
         int b, z, y, x0;
         tile_pos(d, t, b, z, y, x0);
@@ -1048,15 +1112,27 @@ static nr_status launch_conv32(const Dims& d, const __nv_bfloat16* in, const __n
                                int* status, cudaStream_t s) {
     ActMaps map;
     if (!act_maps(d, in, &map)) return NR_ERR_CUDA;  // the input cannot be described for TMA
-    const size_t smem = (size_t)TSTAGE * TSTRIP + 27 * NOUT * C * 2 + sizeof(TmaCtl);
-    if (cudaFuncSetAttribute(conv32_tma_kernel<NOUT, EPI>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return NR_ERR_CUDA;
-    const int64_t nt = ntiles(d);
-    const int grid = (int)(nt < (int64_t)sm_count() * 2 ? nt : (int64_t)sm_count() * 2);
-    conv32_tma_kernel<NOUT, EPI><<<grid, T_THREADS, smem, s>>>(d, map.lo, map.hi, wpk, bias, out,
-                                                               mask, status);
-    return launch_status();
+    {
+        // runs of L rows: about eight items per SM, L in [4, 32]
+        const int nsm = sm_count();
+        const int64_t ncols = (int64_t)d.nb * d.nz * xtiles(d);
+        int64_t L = ((int64_t)d.ny * ncols + 8LL * nsm - 1) / (8LL * nsm);
+        L = L < 4 ? 4 : (L > 32 ? 32 : L);
+        if (L > d.ny) L = d.ny;
+        WalkPlan wp;
+        wp.L = (int)L;
+        wp.nchunk = (int)((d.ny + L - 1) / L);
+        wp.nitems = ncols * wp.nchunk;
+        const size_t smem = (size_t)W_R * W_SET + 27 * NOUT * C * 2 + sizeof(WalkCtl);
+        if (cudaFuncSetAttribute(conv32_walk_kernel<NOUT, EPI>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return NR_ERR_CUDA;
+        const int grid = (int)(wp.nitems < (int64_t)nsm ? wp.nitems : (int64_t)nsm);
+        conv32_walk_kernel<NOUT, EPI><<<grid, W_THREADS, smem, s>>>(d, wp, map.lo, map.hi, wpk,
+                                                                    bias, out, mask, status);
+        return launch_status();
+    }
 }
 
 template <int EPI>
