@@ -183,16 +183,17 @@ struct WalkCtl {
 
 struct WalkPlan {
     int L, nchunk;
+    int tw;  // outputs per tile along x
     int64_t nitems;
 };
 
 // Column (b, z, x0) and rows y0 .. y0 + ly - 1 of item it.
 __device__ __forceinline__ void item_pos(const Dims& d, const WalkPlan& w, int64_t it, int& b,
                                          int& z, int& x0, int& y0, int& ly) {
-    const int xt = xtiles(d);
+    const int xt = (d.nx + w.tw - 1) / w.tw;
     int64_t col = it / w.nchunk;
     const int ch = (int)(it - col * w.nchunk);
-    x0 = (int)(col % xt) * TM;
+    x0 = (int)(col % xt) * w.tw;
     col /= xt;
     z = (int)(col % d.nz);
     b = (int)(col / d.nz);
@@ -401,6 +402,235 @@ __global__ void __launch_bounds__(W_THREADS, 1) conv32_walk_kernel(
     tc::fence_before();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
+// ---- conv32 with the three dx taps in one MMA -------------------------------
+// The walk of conv32_walk_kernel with N = 3 NOUT: the weights of the three dx
+// taps of a strip are adjacent in the packed buffer (512-byte row groups), so
+// one MMA over the unshifted strip (A rows r = input x0 - 1 + r) computes
+// D[r][(dx, o)] = sum_i a[x0 - 1 + r][i] W[dz][dy][dx][o][i] for all three dx:
+// 18 MMAs per tile instead of 54, and each A row is fetched once per strip
+// instead of three times.  Output x0 - 1 + r (r = 1 .. 126: 126 outputs per
+// tile, tiles 126 apart) is D[r - 1][dx 0] + D[r][dx 1] + D[r + 1][dx 2]: the
+// dx = 0 and dx = 2 columns are moved one TMEM lane by warp shuffles, and
+// across the four warps' lane quarters through shared memory (each warp
+// publishes lane 31's dx-0 and lane 0's dx-2 columns; an mbarrier per
+// epilogue group, double-buffered by tile, orders the exchange with a bounded
+// wait).  TMEM: two accumulators of 3 NOUT columns (at 0 and 128).
+constexpr int W3_TW = TM - 2;  // 126 outputs per tile
+
+struct W3Ctl {
+    uint64_t full[W_R], empty[W_R], accf[2], acce[2], xchg[2], drain;
+    uint32_t tslot;
+    int abort;
+    float xb[2][2][4][2][C];  // [group][tile parity][warp][lane 31 dx 0 | lane 0 dx 2][o]
+};
+
+template <int NOUT, int EPI>
+__global__ void __launch_bounds__(W_THREADS, 1) conv32_w3_kernel(
+    Dims d, WalkPlan wp, const __grid_constant__ CUtensorMap amap,
+    const __grid_constant__ CUtensorMap amap_hi, const __nv_bfloat16* __restrict__ wpk,
+    const float* __restrict__ bias, void* out, const __nv_bfloat16* __restrict__ mask,
+    int* status) {
+    constexpr int WBYTES = 27 * NOUT * C * 2;
+    constexpr int NO = EPI == EPI_RESID ? 1 : NOUT;  // output channels the epilogue needs
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* ring = smem;
+    uint8_t* sW = smem + W_R * W_SET;
+    W3Ctl* K = (W3Ctl*)(sW + WBYTES);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int k = tid; k < WBYTES / 16; k += W_THREADS)
+        ((uint4*)sW)[k] = __ldg((const uint4*)wpk + k);
+    if (tid == 0) {
+        for (int s = 0; s < W_R; s++) {
+            tc::mbar_init(&K->full[s], 1);
+            tc::mbar_init(&K->empty[s], 1);
+        }
+        for (int a = 0; a < 2; a++) {
+            tc::mbar_init(&K->accf[a], 1);
+            tc::mbar_init(&K->acce[a], 4);
+            tc::mbar_init(&K->xchg[a], 4);
+        }
+        tc::mbar_init(&K->drain, 1);
+        K->abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tc::tmem_alloc(&K->tslot, 256);
+    tc::fence_async_smem();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = K->tslot;
+    volatile int* abort = &K->abort;
+    auto fail = [&]() {
+        if (!*abort) atomicOr(status, NR_FLAG_TIMEOUT);
+        *abort = 1;
+        __threadfence_block();
+    };
+    auto strip_ok = [&](int zz, int yy) { return zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny; };
+    if (warp == 8) {
+        if (lane == 0) {
+            // producer (as in conv32_walk_kernel)
+            int64_t G = 0, issued = 0;
+            bool stop = false;
+            for (int64_t it = blockIdx.x; it < wp.nitems && !stop && !*abort; it += gridDim.x) {
+                int b, z, x0, y0, ly;
+                item_pos(d, wp, it, b, z, x0, y0, ly);
+                for (int j = 0; j < ly + 2; j++, G++) {
+                    const int s = (int)(G % W_R);
+                    if (G >= W_R &&
+                        !wait_live(&K->empty[s], (uint32_t)((G / W_R - 1) & 1), abort)) {
+                        fail();
+                        stop = true;
+                        break;
+                    }
+                    const int Y = y0 - 1 + j;
+                    mbar_arrive_tx(&K->full[s], 3 * STRIP_TX);
+                    for (int dz = 0; dz < 3; dz++)
+                        load_strip(ring + s * W_SET + dz * TSTRIP, PLANE, &amap, &amap_hi, x0,
+                                   strip_ok(z + dz - 1, Y) ? (b * d.nz + z + dz - 1) * d.ny + Y : -1,
+                                   &K->full[s]);
+                    issued = G + 1;
+                }
+            }
+            for (int64_t k = issued > W_R ? issued - W_R : 0; k < issued; k++) {
+                uint64_t* bar = &K->full[k % W_R];
+                if (!tc::mbar_wait(bar, (uint32_t)((k / W_R) & 1), WAIT_LIMIT))
+                    tc::mbar_wait(bar, (uint32_t)((k / W_R) & 1), WAIT_LIMIT);
+            }
+        }
+    } else if (warp == 9) {
+        if (lane == 0) {
+            // MMA issuer: per strip (dz, dy) two MMAs of K = 16, N = 3 NOUT
+            constexpr uint32_t idesc = tc::idesc_bf16(TM, 3 * NOUT);
+            const uint64_t ad0 = tc::sdesc(tc::smem_u32(ring), PLANE, 128);
+            const uint64_t bd0 = tc::sdesc(tc::smem_u32(sW), 128, 512);
+            int64_t G = 0;
+            int lt = 0;
+            bool stop = false;
+            for (int64_t it = blockIdx.x; it < wp.nitems && !stop && !*abort; it += gridDim.x) {
+                int b, z, x0, y0, ly;
+                item_pos(d, wp, it, b, z, x0, y0, ly);
+                for (int i = 0; i < ly && !stop; i++, lt++) {
+                    const int a = lt & 1;
+                    if (lt >= 2 &&
+                        !wait_live(&K->acce[a], (uint32_t)(((lt >> 1) - 1) & 1), abort)) {
+                        fail();
+                        stop = true;
+                        break;
+                    }
+                    tc::fence_after();
+                    const uint32_t dacc = tmem + (uint32_t)(a * 128);
+#pragma unroll
+                    for (int dy = 0; dy < 3; dy++) {
+                        const int64_t gs = G + i + dy;
+                        const int s = (int)(gs % W_R);
+                        if ((i == 0 || dy == 2) &&
+                            !wait_live(&K->full[s], (uint32_t)((gs / W_R) & 1), abort)) {
+                            fail();
+                            stop = true;
+                            break;
+                        }
+                        tc::fence_after();
+                        const uint64_t adr = ad0 + (uint64_t)((s * W_SET) >> 4);
+#pragma unroll
+                        for (int dz = 0; dz < 3; dz++)
+#pragma unroll
+                            for (int j = 0; j < 2; j++)
+                                tc::mma_bf16(
+                                    dacc, adr + (uint64_t)((dz * TSTRIP + j * 2 * PLANE) >> 4),
+                                    bd0 + (uint64_t)(((dz * 9 + dy * 3) * NOUT * C * 2 + j * 256) >> 4),
+                                    idesc, (dy | dz | j) ? 1u : 0u);
+                        if (dy == 0 || i == ly - 1) tc::commit(&K->empty[s]);
+                    }
+                    if (stop) break;
+                    tc::commit(&K->accf[a]);
+                }
+                G += ly + 2;
+            }
+        }
+    } else {
+        // epilogue group g = warp / 4 (tiles lt with lt & 1 == g); TMEM lane
+        // 32 wq + lane = tile row r.  Test hook as in conv32_walk_kernel.
+        const int g = warp >> 2, wq = warp & 3;
+        const int force_at = status[1] - 1;
+        int lt = 0, kg = 0;
+        bool stop = false;
+        for (int64_t it = blockIdx.x; it < wp.nitems && !stop; it += gridDim.x) {
+            int b, z, x0, y0, ly;
+            item_pos(d, wp, it, b, z, x0, y0, ly);
+            for (int i = 0; i < ly; i++, lt++) {
+                if ((lt & 1) != g) continue;
+                bool got = wait_live(&K->accf[g], (uint32_t)((lt >> 1) & 1), abort);
+                if (lt == force_at) got = false;
+                if (!got) {
+                    if (lane == 0) fail();
+                    stop = true;
+                    break;
+                }
+                tc::fence_after();
+                // columns: dx 0 at 0, dx 1 at NOUT, dx 2 at 2 NOUT
+                uint32_t c0[32], c1[32];
+                float d0[NO], d1[NO], d2[NO];
+                const uint32_t col = (uint32_t)(g * 128);
+                tc::ld32(tmem, (uint32_t)(wq * 32), col, c0);
+                tc::ld32(tmem, (uint32_t)(wq * 32), col + 32, c1);
+                if (NOUT == C) {
+#pragma unroll
+                    for (int o = 0; o < NO; o++) {
+                        d0[o] = __uint_as_float(c0[o]);
+                        d1[o] = __uint_as_float(c1[o]);
+                    }
+                    tc::ld32(tmem, (uint32_t)(wq * 32), col + 64, c0);
+#pragma unroll
+                    for (int o = 0; o < NO; o++) d2[o] = __uint_as_float(c0[o]);
+                } else {
+#pragma unroll
+                    for (int o = 0; o < NO; o++) {
+                        d0[o] = __uint_as_float(c0[o]);
+                        d1[o] = __uint_as_float(c0[NOUT + o]);
+                        d2[o] = __uint_as_float(c1[o]);
+                    }
+                }
+                tc::fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&K->acce[g]);
+                // publish the lane-quarter edges, then read the neighbours'
+                float* xb = &K->xb[g][kg & 1][0][0][0];
+                if (lane == 31)
+                    for (int o = 0; o < NO; o++) xb[(wq * 2 + 0) * C + o] = d0[o];
+                if (lane == 0)
+                    for (int o = 0; o < NO; o++) xb[(wq * 2 + 1) * C + o] = d2[o];
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&K->xchg[g]);
+                if (!wait_live(&K->xchg[g], (uint32_t)(kg & 1), abort)) {
+                    if (lane == 0) fail();
+                    stop = true;
+                    break;
+                }
+                kg++;
+                uint32_t acc[32];
+#pragma unroll
+                for (int o = 0; o < NO; o++) {
+                    float up = __shfl_up_sync(0xffffffffu, d0[o], 1);
+                    float dn = __shfl_down_sync(0xffffffffu, d2[o], 1);
+                    if (lane == 0) up = wq > 0 ? xb[((wq - 1) * 2 + 0) * C + o] : 0.f;
+                    if (lane == 31) dn = wq < 3 ? xb[((wq + 1) * 2 + 1) * C + o] : 0.f;
+                    acc[o] = __float_as_uint((up + d1[o]) + dn);
+                }
+                const int r = wq * 32 + lane, x = x0 - 1 + r;
+                if (r >= 1 && r <= W3_TW && x < d.nx)
+                    epilogue_rx<EPI>(acc, ((int64_t)b * d.nz + z) * d.ny + y0 + i, x, d.nx, bias,
+                                     out, mask);
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == 9 && lane == 0) tc::commit(&K->drain);
+    if (!tc::mbar_wait(&K->drain, 0, WAIT_LIMIT)) tc::mbar_wait(&K->drain, 0, WAIT_LIMIT);
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 256);
 }
 
 // 1-channel input conv (the first layer, and the back projection of the last
@@ -1112,27 +1342,44 @@ static nr_status launch_conv32(const Dims& d, const __nv_bfloat16* in, const __n
                                int* status, cudaStream_t s) {
     ActMaps map;
     if (!act_maps(d, in, &map)) return NR_ERR_CUDA;  // the input cannot be described for TMA
-    {
-        // runs of L rows: about eight items per SM, L in [4, 32]
-        const int nsm = sm_count();
-        const int64_t ncols = (int64_t)d.nb * d.nz * xtiles(d);
-        int64_t L = ((int64_t)d.ny * ncols + 8LL * nsm - 1) / (8LL * nsm);
-        L = L < 4 ? 4 : (L > 32 ? 32 : L);
-        if (L > d.ny) L = d.ny;
-        WalkPlan wp;
-        wp.L = (int)L;
-        wp.nchunk = (int)((d.ny + L - 1) / L);
-        wp.nitems = ncols * wp.nchunk;
-        const size_t smem = (size_t)W_R * W_SET + 27 * NOUT * C * 2 + sizeof(WalkCtl);
-        if (cudaFuncSetAttribute(conv32_walk_kernel<NOUT, EPI>,
+    // runs of L rows: about eight items per SM, L in [4, 32]
+    const int nsm = sm_count();
+    const int64_t ncols = (int64_t)d.nb * d.nz * xtiles(d);
+    int64_t L = ((int64_t)d.ny * ncols + 8LL * nsm - 1) / (8LL * nsm);
+    L = L < 4 ? 4 : (L > 32 ? 32 : L);
+    if (L > d.ny) L = d.ny;
+    WalkPlan wp;
+    wp.L = (int)L;
+    wp.nchunk = (int)((d.ny + L - 1) / L);
+    const int grid_max = nsm;
+    // The dx-stacked kernel costs about 0.73 of the other per tile (clinical
+    // network forward 18.45 ms over 126-wide tiles against 22.48 ms over
+    // 128-wide ones) but needs ceil(nx / 126) tiles per row: it is used when
+    // that is cheaper (not for nx = 128 or 256).
+    const int t126 = (d.nx + W3_TW - 1) / W3_TW, t128 = (d.nx + TM - 1) / TM;
+    if (73 * t126 < 100 * t128) {
+        wp.tw = W3_TW;
+        wp.nitems = (int64_t)d.nb * d.nz * t126 * wp.nchunk;
+        const size_t smem = (size_t)W_R * W_SET + 27 * NOUT * C * 2 + sizeof(W3Ctl);
+        if (cudaFuncSetAttribute(conv32_w3_kernel<NOUT, EPI>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess)
             return NR_ERR_CUDA;
-        const int grid = (int)(wp.nitems < (int64_t)nsm ? wp.nitems : (int64_t)nsm);
-        conv32_walk_kernel<NOUT, EPI><<<grid, W_THREADS, smem, s>>>(d, wp, map.lo, map.hi, wpk,
-                                                                    bias, out, mask, status);
+        const int grid = (int)(wp.nitems < (int64_t)grid_max ? wp.nitems : (int64_t)grid_max);
+        conv32_w3_kernel<NOUT, EPI><<<grid, W_THREADS, smem, s>>>(d, wp, map.lo, map.hi, wpk,
+                                                                  bias, out, mask, status);
         return launch_status();
     }
+    wp.tw = TM;
+    wp.nitems = (int64_t)d.nb * d.nz * t128 * wp.nchunk;
+    const size_t smem = (size_t)W_R * W_SET + 27 * NOUT * C * 2 + sizeof(WalkCtl);
+    if (cudaFuncSetAttribute(conv32_walk_kernel<NOUT, EPI>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return NR_ERR_CUDA;
+    const int grid = (int)(wp.nitems < (int64_t)grid_max ? wp.nitems : (int64_t)grid_max);
+    conv32_walk_kernel<NOUT, EPI><<<grid, W_THREADS, smem, s>>>(d, wp, map.lo, map.hi, wpk, bias,
+                                                                out, mask, status);
+    return launch_status();
 }
 
 template <int EPI>

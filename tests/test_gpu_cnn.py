@@ -26,7 +26,9 @@ def ws():
     return warmstart
 
 
-# (nx, ny, nz, nb): a partial x-tile, two x-tiles (one partial), one full tile
+# (nx, ny, nz, nb): a partial x-tile, two x-tiles (one partial), one full tile.
+# The 32-channel layers run the dx-stacked kernel (126-wide tiles) for nx = 20
+# and 150 and the 128-wide walk for nx = 128.
 DIMS = [(20, 6, 5, 2), (150, 3, 4, 1), (128, 4, 3, 1)]
 
 
@@ -59,7 +61,8 @@ def test_forward_matches_reference(ws, dims):
 MANY = (160, 16, 8, 2)
 
 
-@pytest.mark.parametrize("dims", DIMS[:2] + [MANY], ids=["partial", "two_tiles", "many_blocks"])
+@pytest.mark.parametrize("dims", DIMS + [MANY],
+                         ids=["partial", "two_tiles", "full_tile", "many_blocks"])
 def test_gradients_match_reference(ws, dims):
     from oracle import cnn_oracle as co
 

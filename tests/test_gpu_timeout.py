@@ -111,15 +111,17 @@ def test_staged_projection_expiry_falls_back_to_global_reads(mod):
     assert staged.check() == 0
 
 
-def test_convolution_expiry_releases_tensor_memory(mod):
-    """The tensor-core convolutions: a tile wait that gives up flags the
+@pytest.mark.parametrize("dims", [(256, 40, 8, 1), (252, 40, 8, 1)], ids=["walk128", "dx3"])
+def test_convolution_expiry_releases_tensor_memory(mod, dims):
+    """The tensor-core convolutions (the 128-wide walk for nx = 256, the
+    dx-stacked kernel for nx = 252): a tile wait that gives up flags the
     timeout, drains and releases TMEM; with the hook off the next forward
-    pass on the same workspace is the reference's bit for bit."""
+    pass on the same workspace is the reference's bit for bit.  Every CTA
+    takes at least one run of 4 rows, so tiles 0 and 1 exist everywhere."""
     from newrecon_gb300 import native, warmstart
     from newrecon_gb300.native import NrError
     from oracle import cnn_oracle as co
 
-    dims = (256, 40, 8, 1)  # 640 tiles: every CTA of the convolutions runs 2 or 3
     rng = np.random.default_rng(5)
     x = torch.from_numpy(rng.uniform(0.0, 0.1, size=int(np.prod(dims))).astype(np.float32)).cuda()
     net = warmstart.WarmStartCNN(co.init_params(3, last_scale=0.5), scale=20.0)
