@@ -418,16 +418,18 @@ __global__ void __launch_bounds__(W_THREADS, 1) conv32_walk_kernel(
 // epilogue group, double-buffered by tile, orders the exchange with a bounded
 // wait).  TMEM: two accumulators of 3 NOUT columns (at 0 and 128).
 constexpr int W3_TW = TM - 2;  // 126 outputs per tile
+constexpr int W3_NG = 3;       // epilogue groups = TMEM accumulators
+constexpr int W3_THREADS = 32 * (4 * W3_NG + 2);
 
 struct W3Ctl {
-    uint64_t full[W_R], empty[W_R], accf[2], acce[2], xchg[2], drain;
+    uint64_t full[W_R], empty[W_R], accf[W3_NG], acce[W3_NG], xchg[W3_NG], drain;
     uint32_t tslot;
     int abort;
-    float xb[2][2][4][2][C];  // [group][tile parity][warp][lane 31 dx 0 | lane 0 dx 2][o]
+    float xb[W3_NG][2][4][2][C];  // [group][tile parity][warp][lane 31 dx 0 | lane 0 dx 2][o]
 };
 
 template <int NOUT, int EPI>
-__global__ void __launch_bounds__(W_THREADS, 1) conv32_w3_kernel(
+__global__ void __launch_bounds__(W3_THREADS, 1) conv32_w3_kernel(
     Dims d, WalkPlan wp, const __grid_constant__ CUtensorMap amap,
     const __grid_constant__ CUtensorMap amap_hi, const __nv_bfloat16* __restrict__ wpk,
     const float* __restrict__ bias, void* out, const __nv_bfloat16* __restrict__ mask,
@@ -439,14 +441,14 @@ __global__ void __launch_bounds__(W_THREADS, 1) conv32_w3_kernel(
     uint8_t* sW = smem + W_R * W_SET;
     W3Ctl* K = (W3Ctl*)(sW + WBYTES);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int k = tid; k < WBYTES / 16; k += W_THREADS)
+    for (int k = tid; k < WBYTES / 16; k += W3_THREADS)
         ((uint4*)sW)[k] = __ldg((const uint4*)wpk + k);
     if (tid == 0) {
         for (int s = 0; s < W_R; s++) {
             tc::mbar_init(&K->full[s], 1);
             tc::mbar_init(&K->empty[s], 1);
         }
-        for (int a = 0; a < 2; a++) {
+        for (int a = 0; a < W3_NG; a++) {
             tc::mbar_init(&K->accf[a], 1);
             tc::mbar_init(&K->acce[a], 4);
             tc::mbar_init(&K->xchg[a], 4);
@@ -455,7 +457,7 @@ __global__ void __launch_bounds__(W_THREADS, 1) conv32_w3_kernel(
         K->abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) tc::tmem_alloc(&K->tslot, 256);
+    if (warp == 0) tc::tmem_alloc(&K->tslot, 512);
     tc::fence_async_smem();
     tc::fence_before();
     __syncthreads();
@@ -468,7 +470,7 @@ __global__ void __launch_bounds__(W_THREADS, 1) conv32_w3_kernel(
         __threadfence_block();
     };
     auto strip_ok = [&](int zz, int yy) { return zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny; };
-    if (warp == 8) {
+    if (warp == 4 * W3_NG) {
         if (lane == 0) {
             // producer (as in conv32_walk_kernel)
             int64_t G = 0, issued = 0;
@@ -499,7 +501,7 @@ __global__ void __launch_bounds__(W_THREADS, 1) conv32_w3_kernel(
                     tc::mbar_wait(bar, (uint32_t)((k / W_R) & 1), WAIT_LIMIT);
             }
         }
-    } else if (warp == 9) {
+    } else if (warp == 4 * W3_NG + 1) {
         if (lane == 0) {
             // MMA issuer: per strip (dz, dy) two MMAs of K = 16, N = 3 NOUT
             constexpr uint32_t idesc = tc::idesc_bf16(TM, 3 * NOUT);
@@ -512,9 +514,9 @@ __global__ void __launch_bounds__(W_THREADS, 1) conv32_w3_kernel(
                 int b, z, x0, y0, ly;
                 item_pos(d, wp, it, b, z, x0, y0, ly);
                 for (int i = 0; i < ly && !stop; i++, lt++) {
-                    const int a = lt & 1;
-                    if (lt >= 2 &&
-                        !wait_live(&K->acce[a], (uint32_t)(((lt >> 1) - 1) & 1), abort)) {
+                    const int a = lt % W3_NG;
+                    if (lt >= W3_NG &&
+                        !wait_live(&K->acce[a], (uint32_t)((lt / W3_NG - 1) & 1), abort)) {
                         fail();
                         stop = true;
                         break;
@@ -550,7 +552,7 @@ __global__ void __launch_bounds__(W_THREADS, 1) conv32_w3_kernel(
             }
         }
     } else {
-        // epilogue group g = warp / 4 (tiles lt with lt & 1 == g); TMEM lane
+        // epilogue group g = warp / 4 (tiles lt with lt % W3_NG == g); TMEM lane
         // 32 wq + lane = tile row r.  Test hook as in conv32_walk_kernel.
         const int g = warp >> 2, wq = warp & 3;
         const int force_at = status[1] - 1;
@@ -560,8 +562,8 @@ __global__ void __launch_bounds__(W_THREADS, 1) conv32_w3_kernel(
             int b, z, x0, y0, ly;
             item_pos(d, wp, it, b, z, x0, y0, ly);
             for (int i = 0; i < ly; i++, lt++) {
-                if ((lt & 1) != g) continue;
-                bool got = wait_live(&K->accf[g], (uint32_t)((lt >> 1) & 1), abort);
+                if (lt % W3_NG != g) continue;
+                bool got = wait_live(&K->accf[g], (uint32_t)((lt / W3_NG) & 1), abort);
                 if (lt == force_at) got = false;
                 if (!got) {
                     if (lane == 0) fail();
@@ -626,11 +628,11 @@ __global__ void __launch_bounds__(W_THREADS, 1) conv32_w3_kernel(
         }
     }
     __syncthreads();
-    if (warp == 9 && lane == 0) tc::commit(&K->drain);
+    if (warp == 4 * W3_NG + 1 && lane == 0) tc::commit(&K->drain);
     if (!tc::mbar_wait(&K->drain, 0, WAIT_LIMIT)) tc::mbar_wait(&K->drain, 0, WAIT_LIMIT);
     tc::fence_before();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 256);
+    if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
 // 1-channel input conv (the first layer, and the back projection of the last
@@ -1366,8 +1368,8 @@ static nr_status launch_conv32(const Dims& d, const __nv_bfloat16* in, const __n
             cudaSuccess)
             return NR_ERR_CUDA;
         const int grid = (int)(wp.nitems < (int64_t)grid_max ? wp.nitems : (int64_t)grid_max);
-        conv32_w3_kernel<NOUT, EPI><<<grid, W_THREADS, smem, s>>>(d, wp, map.lo, map.hi, wpk,
-                                                                  bias, out, mask, status);
+        conv32_w3_kernel<NOUT, EPI><<<grid, W3_THREADS, smem, s>>>(d, wp, map.lo, map.hi, wpk,
+                                                                   bias, out, mask, status);
         return launch_status();
     }
     wp.tw = TM;
