@@ -96,20 +96,22 @@ __device__ __forceinline__ void commit(uint64_t* bar) {
 }
 
 // Warp w reads TMEM lanes 32(w%4) .. +31, 32 consecutive columns from col:
-// thread `lane` gets row 32(w%4)+lane, r[c] = column col + c.
+// thread `lane` gets row 32(w%4)+lane, r[c] = column col + c.  The wait is in
+// the same statement, so the outputs are defined only once it has completed.
 __device__ __forceinline__ void ld32(uint32_t tmem, uint32_t lane0, uint32_t col, uint32_t* r) {
     const uint32_t a = tmem + (lane0 << 16) + col;
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-        "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        "tcgen05.wait::ld.sync.aligned;"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
           "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
           "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
           "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
           "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
           "=r"(r[31])
-        : "r"(a));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        : "r"(a)
+        : "memory");
 }
 
 }  // namespace tc
