@@ -491,6 +491,7 @@ def batch_bench(args, rank):
             t_seq += timed(run, xx.zero_)
     vox = sum(cs["geom"].n_voxels for cs in cases)
     return {"cases": len(cases), "steps_timed": steps, "whole_run": full,
+            "mode": bt.mode if full else "shared",
             "timing": "CUDA graph replay of " + ("the whole batch (every step and the finish)"
                                                  if full else f"the first {steps} steps"),
             "voxels_total": vox, "seconds": t_batch,

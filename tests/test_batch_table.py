@@ -144,3 +144,19 @@ def test_launching_calls_refuse_foreign_tables(native):
         native.call("nr_batch_step", ctypes.c_void_p(ptr), 0, None)
     assert e.value.code == 2
     buf[:] = before
+
+
+def test_batch_mode_choice():
+    """"auto" runs cases that each fill the GPU (2^26 voxels or more) one after
+    another and smaller ones by shared launches; explicit modes are kept."""
+    from newrecon_gb300.ostr import Batch
+
+    big, small = Batch.SEQUENTIAL_VOXELS, Batch.SEQUENTIAL_VOXELS - 1
+    assert Batch.choose_mode([2048 * 1024 * 70] * 4) == "sequential"
+    assert Batch.choose_mode([big, big]) == "sequential"
+    assert Batch.choose_mode([big, small]) == "shared"
+    assert Batch.choose_mode([1024 * 512 * 60]) == "shared"
+    assert Batch.choose_mode([big], "shared") == "shared"
+    assert Batch.choose_mode([small], "sequential") == "sequential"
+    with pytest.raises(ValueError):
+        Batch.choose_mode([big], "persistent")

@@ -209,3 +209,25 @@ def test_autotune_variants_agree_and_cache(mod, tmp_path, monkeypatch):
     assert plan.params.fp_stage == rec["fp_stage"]
     assert plan.params.upd_tile == rec["upd_tile"] in autotune.UPD_TILES
     assert len(rec["update_ms"]) == len(autotune.UPD_PLANES) * len(autotune.UPD_TILES)
+
+
+def test_sequential_mode_matches_shared_launches(mod):
+    """mode="sequential" (each case through its own loop, and its whole-run
+    graph: each case's loop as its own graph) gives the shared launches'
+    volumes bit for bit."""
+    cases = batch_cases()
+    ref = [x.clone() for x in mod.Batch(cases, mode="shared").run()]
+    bs = mod.Batch(cases, mode="sequential")
+    assert bs.mode == "sequential"
+    out = bs.run()
+    for a, b in zip(ref, out):
+        assert torch.equal(a, b)
+    for x in bs.x:
+        x.zero_()
+    gr = bs.graph()
+    gr.launch()
+    torch.cuda.synchronize()
+    bs.check()
+    gr.close()
+    for a, b in zip(ref, bs.x):
+        assert torch.equal(a, b)

@@ -26,10 +26,11 @@ def ws():
     return warmstart
 
 
-# (nx, ny, nz, nb): a partial x-tile, two x-tiles (one partial), one full tile.
-# The 32-channel layers run the dx-stacked kernel (126-wide tiles) for nx = 20
-# and 150 and the 128-wide walk for nx = 128.
-DIMS = [(20, 6, 5, 2), (150, 3, 4, 1), (128, 4, 3, 1)]
+# (nx, ny, nz, nb): a partial x-tile, two x-tiles (one partial), one full tile,
+# four x-tiles.  The 32-channel layers run the dx-stacked kernel (126-wide
+# tiles) for nx = 20, 150 and 384 and the 128-wide walk for nx = 128.
+DIMS = [(20, 6, 5, 2), (150, 3, 4, 1), (128, 4, 3, 1), (384, 8, 5, 1)]
+DIM_IDS = ["partial", "two_tiles", "full_tile", "four_tiles"]
 
 
 def data(dims, seed):
@@ -40,7 +41,7 @@ def data(dims, seed):
     return x, t
 
 
-@pytest.mark.parametrize("dims", DIMS, ids=["partial", "two_tiles", "full_tile"])
+@pytest.mark.parametrize("dims", DIMS, ids=DIM_IDS)
 def test_forward_matches_reference(ws, dims):
     from oracle import cnn_oracle as co
 
@@ -61,8 +62,7 @@ def test_forward_matches_reference(ws, dims):
 MANY = (160, 16, 8, 2)
 
 
-@pytest.mark.parametrize("dims", DIMS + [MANY],
-                         ids=["partial", "two_tiles", "full_tile", "many_blocks"])
+@pytest.mark.parametrize("dims", DIMS + [MANY], ids=DIM_IDS + ["many_blocks"])
 def test_gradients_match_reference(ws, dims):
     from oracle import cnn_oracle as co
 
