@@ -66,37 +66,6 @@ __host__ __device__ inline int64_t act_off(int64_t v, int c, int nx) {
     return (row * KCH + (c >> 3)) * (int64_t)nx * 8 + (int64_t)x * 8 + (c & 7);
 }
 
-// Epilogue of one output row: 32 accumulator columns -> output voxel v (x of
-// a row of nx voxels).
-template <int EPI>
-__device__ __forceinline__ void epilogue(const uint32_t* acc, int64_t v, int nx,
-                                         const float* __restrict__ bias, void* out,
-                                         const __nv_bfloat16* __restrict__ mask) {
-    if (EPI == EPI_RESID) {
-        ((float*)out)[v] = __uint_as_float(acc[0]) + bias[0];
-        return;
-    }
-    const int64_t o0 = act_off(v, 0, nx);  // chunk q at o0 + q * nx * 8
-    __align__(16) __nv_bfloat16 o[C];
-    if (EPI == EPI_RELU) {
-#pragma unroll
-        for (int c = 0; c < C; c++)
-            o[c] = __float2bfloat16(fmaxf(__uint_as_float(acc[c]) + bias[c], 0.f));
-    } else {
-        __align__(16) __nv_bfloat16 m[C];
-#pragma unroll
-        for (int q = 0; q < KCH; q++)
-            ((uint4*)m)[q] = __ldg((const uint4*)(mask + o0 + (int64_t)q * nx * 8));
-#pragma unroll
-        for (int c = 0; c < C; c++)
-            o[c] = __bfloat162float(m[c]) > 0.f ? __float2bfloat16(__uint_as_float(acc[c]))
-                                                : __float2bfloat16(0.f);
-    }
-#pragma unroll
-    for (int q = 0; q < KCH; q++)
-        *(uint4*)((__nv_bfloat16*)out + o0 + (int64_t)q * nx * 8) = ((const uint4*)o)[q];
-}
-
 // Row (patch b, z, y) of tile t and its first x.
 __device__ __forceinline__ void tile_pos(const Dims& d, int64_t t, int& b, int& z, int& y, int& x0) {
     const int xt = xtiles(d);
@@ -663,22 +632,32 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restr
     int ncommit = 0;
     bool ok = true;
     const int force_at = status[1] - 1;  // test hook, as in conv32_walk_kernel
+    // the 27 neighbours of this thread's voxel in tile t (zero outside the
+    // patch), loaded one tile ahead so that their latency overlaps the
+    // previous tile's MMAs and epilogue
+    float nb[27];
+    auto gather = [&](int64_t t) {
+        int b, z, y, x0;
+        tile_pos(d, t, b, z, y, x0);
+        const int x = x0 + tid;
+#pragma unroll
+        for (int k = 0; k < 27; k++) {
+            const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
+            const int zz = z + dz, yy = y + dy, xx = x + dx;
+            nb[k] = (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny && xx >= 0 && xx < d.nx &&
+                     x < d.nx)
+                        ? __ldg(in + (((int64_t)b * d.nz + zz) * d.ny + yy) * d.nx + xx)
+                        : 0.f;
+        }
+    };
+    if (blockIdx.x < nt) gather(blockIdx.x);
     for (int64_t t = blockIdx.x; t < nt; t += gridDim.x) {
         int b, z, y, x0;
         tile_pos(d, t, b, z, y, x0);
         const int x = x0 + tid;
         __align__(16) __nv_bfloat16 row[32];
 #pragma unroll
-        for (int k = 0; k < 32; k++) {
-            float v = 0.f;
-            if (k < 27) {
-                const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
-                const int zz = z + dz, yy = y + dy, xx = x + dx;
-                if (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny && xx >= 0 && xx < d.nx && x < d.nx)
-                    v = __ldg(in + (((int64_t)b * d.nz + zz) * d.ny + yy) * d.nx + xx) * scale;
-            }
-            row[k] = __float2bfloat16(v);
-        }
+        for (int k = 0; k < 32; k++) row[k] = __float2bfloat16(k < 27 ? nb[k] * scale : 0.f);
         // previous tile's MMAs have completed (waited below), so sA is free
 #pragma unroll
         for (int kc = 0; kc < KCH; kc++) *(uint4*)(sA + kc * TM * 16 + tid * 16) = ((uint4*)row)[kc];
@@ -693,6 +672,7 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restr
                              tc::sdesc(sw + j * 256, 128, 512), idesc, j != 0);
             tc::commit(&bars[0]);
         }
+        if (t + gridDim.x < nt) gather(t + gridDim.x);
         if (ok) {
             ok = tc::mbar_wait(&bars[0], (uint32_t)(ncommit & 1), WAIT_LIMIT) && ntile != force_at;
             ncommit++;
@@ -705,10 +685,7 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restr
         }
         uint32_t acc[32];
         tc::ld32(tmem, (uint32_t)(warp * 32), 0, acc);
-        if (x < d.nx) {
-            const int64_t v = (((int64_t)b * d.nz + z) * d.ny + y) * d.nx + x;
-            epilogue<EPI>(acc, v, d.nx, bias, out, mask);
-        }
+        if (x < d.nx) epilogue_rx<EPI>(acc, ((int64_t)b * d.nz + z) * d.ny + y, x, d.nx, bias, out, mask);
         tc::fence_before();
         __syncthreads();
     }
@@ -1388,6 +1365,8 @@ template <int EPI>
 static nr_status launch_conv1(const Dims& d, const float* in, float scale,
                               const __nv_bfloat16* wpk, const float* bias, void* out,
                               const __nv_bfloat16* mask, int* status, cudaStream_t s) {
+    // four CTAs per SM: nine (as many as fit) measured 2.7x slower on the
+    // clinical volume (6.0 against 2.25 ms)
     const int64_t nt = ntiles(d);
     const int grid = (int)(nt < (int64_t)sm_count() * 4 ? nt : (int64_t)sm_count() * 4);
     conv1_kernel<EPI><<<grid, 128, 0, s>>>(d, in, scale, wpk, bias, out, mask, status);
