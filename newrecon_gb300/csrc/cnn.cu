@@ -604,6 +604,178 @@ __global__ void __launch_bounds__(W3_THREADS, 1) conv32_w3_kernel(
     if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
+// ---- the 32 -> 1 layer in two passes -----------------------------------------
+// f[v] = b + sum over taps of W[tap] . a[v + off(tap)], regrouped by the tap's
+// (dz, dy).  Pass 1 (last_rows_kernel), per input row u of the volume:
+//     q[(dz, dy)][u] = sum_dx W[dz][dy][dx] . a[u + (dx - 1, 0, 0)]
+// as three MMAs (one per dx: the row's strip at a 16-byte offset) of N = 16
+// (rows (dz, dy), 9 used) and K = 32 per 128 voxels -- one strip per tile
+// against the convolution's nine, and no walk.  Pass 2 (last_sum_kernel):
+//     f[v] = b + sum_{(dz, dy)} q[(dz, dy)][v + (0, dy - 1, dz - 1)]
+// (zero outside the patch), nine coalesced loads in a fixed order.  Pass 1:
+// a producer lane loads the strips into a ring of LR_STAGE stages, an issuer
+// lane runs the MMAs into one of two TMEM accumulators, four epilogue warps
+// store the nine planes of q; waits bounded as in conv32_walk_kernel.
+constexpr int LR_STAGE = 6;
+constexpr int LR_THREADS = 192;
+
+struct LastCtl {
+    uint64_t full[LR_STAGE], empty[LR_STAGE], accf[2], acce[2], drain;
+    uint32_t tslot;
+    int abort;
+};
+
+__global__ void __launch_bounds__(LR_THREADS) last_rows_kernel(
+    Dims d, const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap amap_hi,
+    const __nv_bfloat16* __restrict__ wpk, float* __restrict__ q, int* status) {
+    constexpr int WBYTES = 3 * 16 * C * 2;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* ring = smem;
+    uint8_t* sW = smem + LR_STAGE * TSTRIP;
+    LastCtl* K = (LastCtl*)(sW + WBYTES);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int k = tid; k < WBYTES / 16; k += LR_THREADS)
+        ((uint4*)sW)[k] = __ldg((const uint4*)wpk + k);
+    if (tid == 0) {
+        for (int s = 0; s < LR_STAGE; s++) {
+            tc::mbar_init(&K->full[s], 1);
+            tc::mbar_init(&K->empty[s], 1);
+        }
+        for (int a = 0; a < 2; a++) {
+            tc::mbar_init(&K->accf[a], 1);
+            tc::mbar_init(&K->acce[a], 4);
+        }
+        tc::mbar_init(&K->drain, 1);
+        K->abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tc::tmem_alloc(&K->tslot, 64);
+    tc::fence_async_smem();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = K->tslot;
+    const int64_t nt = ntiles(d);
+    const int64_t V = nvox(d);
+    volatile int* abort = &K->abort;
+    auto fail = [&]() {
+        if (!*abort) atomicOr(status, NR_FLAG_TIMEOUT);
+        *abort = 1;
+        __threadfence_block();
+    };
+    if (warp == 4) {
+        if (lane == 0) {
+            // producer
+            int64_t lt = 0, issued = 0;
+            for (int64_t t = blockIdx.x; t < nt && !*abort; t += gridDim.x, lt++) {
+                const int s = (int)(lt % LR_STAGE);
+                if (lt >= LR_STAGE &&
+                    !wait_live(&K->empty[s], (uint32_t)((lt / LR_STAGE - 1) & 1), abort)) {
+                    fail();
+                    break;
+                }
+                int b, z, y, x0;
+                tile_pos(d, t, b, z, y, x0);
+                mbar_arrive_tx(&K->full[s], STRIP_TX);
+                load_strip(ring + s * TSTRIP, PLANE, &amap, &amap_hi, x0, (b * d.nz + z) * d.ny + y,
+                           &K->full[s]);
+                issued = lt + 1;
+            }
+            for (int64_t k = issued > LR_STAGE ? issued - LR_STAGE : 0; k < issued; k++) {
+                uint64_t* bar = &K->full[k % LR_STAGE];
+                if (!tc::mbar_wait(bar, (uint32_t)((k / LR_STAGE) & 1), WAIT_LIMIT))
+                    tc::mbar_wait(bar, (uint32_t)((k / LR_STAGE) & 1), WAIT_LIMIT);
+            }
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {
+            // MMA issuer: per dx, the strip at offset dx rows against its 16 x 32 block
+            constexpr uint32_t idesc = tc::idesc_bf16(TM, 16);
+            const uint64_t ad0 = tc::sdesc(tc::smem_u32(ring), PLANE, 128);
+            const uint64_t bd0 = tc::sdesc(tc::smem_u32(sW), 128, 512);
+            int64_t lt = 0;
+            for (int64_t t = blockIdx.x; t < nt && !*abort; t += gridDim.x, lt++) {
+                const int a = (int)(lt & 1), s = (int)(lt % LR_STAGE);
+                if (lt >= 2 && !wait_live(&K->acce[a], (uint32_t)(((lt >> 1) - 1) & 1), abort)) {
+                    fail();
+                    break;
+                }
+                if (!wait_live(&K->full[s], (uint32_t)((lt / LR_STAGE) & 1), abort)) {
+                    fail();
+                    break;
+                }
+                tc::fence_after();
+                const uint64_t adr = ad0 + (uint64_t)((s * TSTRIP) >> 4);
+#pragma unroll
+                for (int dx = 0; dx < 3; dx++)
+#pragma unroll
+                    for (int j = 0; j < 2; j++)
+                        tc::mma_bf16(tmem + (uint32_t)(a * 32),
+                                     adr + (uint64_t)((dx * 16 + j * 2 * PLANE) >> 4),
+                                     bd0 + (uint64_t)((dx * 16 * C * 2 + j * 256) >> 4), idesc,
+                                     (dx | j) ? 1u : 0u);
+                tc::commit(&K->empty[s]);
+                tc::commit(&K->accf[a]);
+            }
+        }
+    } else {
+        // epilogue warps 0-3: row 32 warp + lane of each tile.  Test hook: the
+        // workspace's second status word k + 1 > 0 makes the wait for this
+        // CTA's tile k report giving up once it has in fact succeeded.
+        const int force_at = status[1] - 1;
+        int64_t lt = 0;
+        for (int64_t t = blockIdx.x; t < nt; t += gridDim.x, lt++) {
+            const int a = (int)(lt & 1);
+            bool got = wait_live(&K->accf[a], (uint32_t)((lt >> 1) & 1), abort);
+            if (lt == force_at) got = false;
+            if (!got) {
+                if (lane == 0) fail();
+                break;
+            }
+            tc::fence_after();
+            uint32_t acc[32];
+            tc::ld32(tmem, (uint32_t)(warp * 32), (uint32_t)(a * 32), acc);
+            tc::fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&K->acce[a]);
+            int b, z, y, x0;
+            tile_pos(d, t, b, z, y, x0);
+            const int x = x0 + warp * 32 + lane;
+            if (x < d.nx) {
+                const int64_t v = (((int64_t)b * d.nz + z) * d.ny + y) * d.nx + x;
+#pragma unroll
+                for (int n = 0; n < 9; n++) q[n * V + v] = __uint_as_float(acc[n]);
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == 5 && lane == 0) tc::commit(&K->drain);
+    if (!tc::mbar_wait(&K->drain, 0, WAIT_LIMIT)) tc::mbar_wait(&K->drain, 0, WAIT_LIMIT);
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
+// Pass 2: grid (row of the stacked volume, block of 256 x).
+__global__ void __launch_bounds__(256) last_sum_kernel(Dims d, const float* __restrict__ q,
+                                                       const float* __restrict__ bias,
+                                                       float* __restrict__ f) {
+    const int64_t row = blockIdx.x;
+    const int x = blockIdx.y * 256 + threadIdx.x;
+    if (x >= d.nx) return;
+    const int y = (int)(row % d.ny), z = (int)((row / d.ny) % d.nz);
+    const int64_t b = row / ((int64_t)d.ny * d.nz);
+    const int64_t V = nvox(d);
+    float sum = 0.f;
+#pragma unroll
+    for (int n = 0; n < 9; n++) {
+        const int zz = z + n / 3 - 1, yy = y + n % 3 - 1;
+        if (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny)
+            sum += __ldg(q + n * V + ((b * d.nz + zz) * d.ny + yy) * d.nx + x);
+    }
+    f[row * d.nx + x] = sum + bias[0];
+}
+
 // 1-channel input conv (the first layer, and the back projection of the last
 // layer's gradient): each output row gathers its 27 neighbours (zero outside
 // its patch) x scale into one K = 32 row.  Weights: one packed 32 x 32 tile.
@@ -1126,10 +1298,13 @@ __global__ void __launch_bounds__(256) wgrad_reduce_kernel(const float* __restri
 // mode 2: forward of the 1-input layer: one tile, row n = o, k = tap.
 // mode 3: dgrad of the 1-output layer as a 1-channel conv: row n = i, k = tap',
 //         from W[26 - tap'][0][i].
+// mode 4: forward of the 1-output layer in row passes: per dx one 16 x 32
+//         block, row n = (dz, dy) = 3 dz + dy (n < 9), k = i, from
+//         W[9 dz + 3 dy + dx][0][i].
 __global__ void pack_kernel(const float* __restrict__ w, int mode, int NI, int NO, int NOUT,
                             __nv_bfloat16* __restrict__ out) {
     const int per_tap = NOUT * C;
-    const int total = (mode == 2 || mode == 3) ? C * C : 27 * per_tap;
+    const int total = (mode == 2 || mode == 3) ? C * C : (mode == 4 ? 3 * 16 * C : 27 * per_tap);
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
         float v = 0.f;
         int dst;
@@ -1145,10 +1320,14 @@ __global__ void pack_kernel(const float* __restrict__ w, int mode, int NI, int N
             const int n = e / C, k = e % C;
             if (k < 27 && n < NO) v = w[((int64_t)k * NO + n) * NI + 0];
             dst = bpk_index(n, k);
-        } else {
+        } else if (mode == 3) {
             const int n = e / C, k = e % C;
             if (k < 27 && n < NI) v = w[((int64_t)(26 - k) * NO + 0) * NI + n];
             dst = bpk_index(n, k);
+        } else {
+            const int dx = e / (16 * C), r = e % (16 * C), n = r / C, k = r % C;
+            if (n < 9) v = w[((int64_t)((n / 3) * 9 + (n % 3) * 3 + dx) * NO + 0) * NI + k];
+            dst = dx * 16 * C + bpk_index(n, k);
         }
         out[dst] = __float2bfloat16(v);
     }
@@ -1373,6 +1552,23 @@ static nr_status launch_conv1(const Dims& d, const float* in, float scale,
     return launch_status();
 }
 
+// The 32 -> 1 layer (two passes); q: 9 V floats of scratch.
+static nr_status launch_last(const Dims& d, const __nv_bfloat16* in, const __nv_bfloat16* wpk,
+                             const float* bias, float* q, float* f, int* status, cudaStream_t s) {
+    ActMaps map;
+    if (!act_maps(d, in, &map)) return NR_ERR_CUDA;
+    const size_t smem = (size_t)LR_STAGE * TSTRIP + 3 * 16 * C * 2 + sizeof(LastCtl);
+    if (cudaFuncSetAttribute(last_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+        return NR_ERR_CUDA;
+    const int64_t nt = ntiles(d);
+    const int grid = (int)(nt < (int64_t)sm_count() * 2 ? nt : (int64_t)sm_count() * 2);
+    last_rows_kernel<<<grid, LR_THREADS, smem, s>>>(d, map.lo, map.hi, wpk, q, status);
+    const dim3 g2((unsigned)((int64_t)d.nb * d.nz * d.ny), (unsigned)((d.nx + 255) / 256));
+    last_sum_kernel<<<g2, 256, 0, s>>>(d, q, bias, f);
+    return launch_status();
+}
+
 static void pack(const float* w, int mode, int ni, int no, int nout, __nv_bfloat16* out,
                  cudaStream_t s) {
     pack_kernel<<<64, 256, 0, s>>>(w, mode, ni, no, nout, out);
@@ -1388,7 +1584,7 @@ static nr_status forward(const Dims& d, const float* params, const float* x, flo
     auto pkf = [&](int l) { return (__nv_bfloat16*)(ws + L.pk_fwd[l]); };
     pack(params + wo[0], 2, 1, C, C, pkf(0), st);
     for (int l = 1; l < 5; l++) pack(params + wo[l], 0, C, C, C, pkf(l), st);
-    pack(params + wo[5], 0, C, 1, 16, pkf(5), st);
+    pack(params + wo[5], 4, C, 1, 16, pkf(5), st);
     auto act = [&](int l) {  // output of layer l (0-based, l < 5)
         return (__nv_bfloat16*)(ws + L.act[keep ? l : (l & 1)]);
     };
@@ -1399,8 +1595,10 @@ static nr_status forward(const Dims& d, const float* params, const float* x, flo
         if ((e = launch_conv32<C, EPI_RELU>(d, act(l - 1), pkf(l), params + bo[l], act(l), nullptr,
                                             status, st)) != NR_OK)
             return e;
-    return launch_conv32<16, EPI_RESID>(d, act(4), pkf(5), params + bo[5], ws + L.f, nullptr,
-                                        status, st);
+    // q of the last layer: a buffer idle by now (the gradient buffer when the
+    // activations are kept for training, else layer 4's ping-pong buffer)
+    float* q = (float*)(ws + (keep ? L.dpre[0] : L.act[1]));
+    return launch_last(d, act(4), pkf(5), params + bo[5], q, (float*)(ws + L.f), status, st);
 }
 
 __global__ void target_kernel(const float* __restrict__ x, const float* __restrict__ t, float s,
