@@ -101,6 +101,25 @@ __device__ __forceinline__ void load_strip(uint8_t* dst, int pstride, const CUte
     }
 }
 
+// Named barriers over the n threads of a group of warps (id >= 1; id 0 is
+// __syncthreads).  group_all is also a vote: true when v is true in every
+// thread.  Every warp of the group must reach each of them the same number of
+// times; callers take their decisions to stop from group_all, so that no warp
+// leaves while the others wait.
+__device__ __forceinline__ bool group_all(bool v, int id, int n) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.and.pred p, %2, %3, q;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id), "r"(n)
+        : "memory");
+    return r != 0;
+}
+__device__ __forceinline__ void group_sync(int id, int n) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
 // A bounded wait that also gives up once the block has aborted.
 __device__ __forceinline__ bool wait_live(uint64_t* bar, uint32_t parity, volatile int* abort) {
     for (int round = 0; round < WAIT_LIMIT / 1024; round++) {
@@ -383,15 +402,16 @@ __global__ void __launch_bounds__(W_THREADS, 1) conv32_walk_kernel(
 // tile, tiles 126 apart) is D[r - 1][dx 0] + D[r][dx 1] + D[r + 1][dx 2]: the
 // dx = 0 and dx = 2 columns are moved one TMEM lane by warp shuffles, and
 // across the four warps' lane quarters through shared memory (each warp
-// publishes lane 31's dx-0 and lane 0's dx-2 columns; an mbarrier per
-// epilogue group, double-buffered by tile, orders the exchange with a bounded
-// wait).  TMEM: two accumulators of 3 NOUT columns (at 0 and 128).
+// publishes lane 31's dx-0 and lane 0's dx-2 columns, double-buffered by
+// tile; a named barrier per epilogue group orders the exchange, the group
+// having voted on the accumulator wait first, so that its warps stop
+// together or not at all).  TMEM: two accumulators of 3 NOUT columns (at 0 and 128).
 constexpr int W3_TW = TM - 2;  // 126 outputs per tile
 constexpr int W3_NG = 3;       // epilogue groups = TMEM accumulators
 constexpr int W3_THREADS = 32 * (4 * W3_NG + 2);
 
 struct W3Ctl {
-    uint64_t full[W_R], empty[W_R], accf[W3_NG], acce[W3_NG], xchg[W3_NG], drain;
+    uint64_t full[W_R], empty[W_R], accf[W3_NG], acce[W3_NG], drain;
     uint32_t tslot;
     int abort;
     float xb[W3_NG][2][4][2][C];  // [group][tile parity][warp][lane 31 dx 0 | lane 0 dx 2][o]
@@ -420,7 +440,6 @@ __global__ void __launch_bounds__(W3_THREADS, 1) conv32_w3_kernel(
         for (int a = 0; a < W3_NG; a++) {
             tc::mbar_init(&K->accf[a], 1);
             tc::mbar_init(&K->acce[a], 4);
-            tc::mbar_init(&K->xchg[a], 4);
         }
         tc::mbar_init(&K->drain, 1);
         K->abort = 0;
@@ -534,7 +553,7 @@ __global__ void __launch_bounds__(W3_THREADS, 1) conv32_w3_kernel(
                 if (lt % W3_NG != g) continue;
                 bool got = wait_live(&K->accf[g], (uint32_t)((lt / W3_NG) & 1), abort);
                 if (lt == force_at) got = false;
-                if (!got) {
+                if (!group_all(got, 1 + g, 128)) {  // the group stops together
                     if (lane == 0) fail();
                     stop = true;
                     break;
@@ -572,13 +591,7 @@ __global__ void __launch_bounds__(W3_THREADS, 1) conv32_w3_kernel(
                     for (int o = 0; o < NO; o++) xb[(wq * 2 + 0) * C + o] = d0[o];
                 if (lane == 0)
                     for (int o = 0; o < NO; o++) xb[(wq * 2 + 1) * C + o] = d2[o];
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&K->xchg[g]);
-                if (!wait_live(&K->xchg[g], (uint32_t)(kg & 1), abort)) {
-                    if (lane == 0) fail();
-                    stop = true;
-                    break;
-                }
+                group_sync(1 + g, 128);
                 kg++;
                 uint32_t acc[32];
 #pragma unroll
