@@ -140,7 +140,8 @@ class TrainConfig:
     early_iters: int = 2             # the network's input: OSTR after this many iterations
     full_iters: int = 50             # the target: OSTR after this many iterations
     after_iters: int = 3             # OSTR iterations after the warm start
-    patch: Tuple[int, int, int] = (128, 32, 16)  # training patch (nx, ny, nz)
+    patch: Tuple[int, int, int] = (126, 32, 16)  # training patch (nx, ny, nz): one 126-wide
+                                                 # tile of the dx-stacked convolution per row
     batch: int = 8                   # patches per Adam step
     steps: int = 2000
     lr: float = 2e-3
