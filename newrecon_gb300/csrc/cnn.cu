@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(W_THREADS, 1) conv32_walk_kernel(
 // having voted on the accumulator wait first, so that its warps stop
 // together or not at all).  TMEM: two accumulators of 3 NOUT columns (at 0 and 128).
 constexpr int W3_TW = TM - 2;  // 126 outputs per tile
-constexpr int W3_NG = 3;       // epilogue groups = TMEM accumulators
+constexpr int W3_NG = 4;       // epilogue groups = TMEM accumulators
 constexpr int W3_THREADS = 32 * (4 * W3_NG + 2);
 
 struct W3Ctl {
@@ -559,48 +559,42 @@ __global__ void __launch_bounds__(W3_THREADS, 1) conv32_w3_kernel(
                     break;
                 }
                 tc::fence_after();
-                // columns: dx 0 at 0, dx 1 at NOUT, dx 2 at 2 NOUT
-                uint32_t c0[32], c1[32];
-                float d0[NO], d1[NO], d2[NO];
-                const uint32_t col = (uint32_t)(g * 128);
-                tc::ld32(tmem, (uint32_t)(wq * 32), col, c0);
-                tc::ld32(tmem, (uint32_t)(wq * 32), col + 32, c1);
-                if (NOUT == C) {
+                // columns: dx 0 at col, dx 1 at col + NOUT, dx 2 at col + 2 NOUT.
+                // First publish the lane-quarter edges (lane 31's dx 0, lane 0's
+                // dx 2), then, after the group barrier, read the columns again
+                // into a running sum: at most 64 accumulator values live.
+                const uint32_t col = (uint32_t)(g * 128), l0 = (uint32_t)(wq * 32);
+                float* xb = &K->xb[g][kg & 1][0][0][0];
+                uint32_t c[32];
+                tc::ld32(tmem, l0, col, c);
+                if (lane == 31)
+                    for (int o = 0; o < NO; o++) xb[(wq * 2 + 0) * C + o] = __uint_as_float(c[o]);
+                tc::ld32(tmem, l0, col + 2 * NOUT, c);
+                if (lane == 0)
+                    for (int o = 0; o < NO; o++) xb[(wq * 2 + 1) * C + o] = __uint_as_float(c[o]);
+                group_sync(1 + g, 128);
+                kg++;
+                float sum[NO];
+                tc::ld32(tmem, l0, col, c);
 #pragma unroll
-                    for (int o = 0; o < NO; o++) {
-                        d0[o] = __uint_as_float(c0[o]);
-                        d1[o] = __uint_as_float(c1[o]);
-                    }
-                    tc::ld32(tmem, (uint32_t)(wq * 32), col + 64, c0);
-#pragma unroll
-                    for (int o = 0; o < NO; o++) d2[o] = __uint_as_float(c0[o]);
-                } else {
-#pragma unroll
-                    for (int o = 0; o < NO; o++) {
-                        d0[o] = __uint_as_float(c0[o]);
-                        d1[o] = __uint_as_float(c0[NOUT + o]);
-                        d2[o] = __uint_as_float(c1[o]);
-                    }
+                for (int o = 0; o < NO; o++) {
+                    float up = __shfl_up_sync(0xffffffffu, __uint_as_float(c[o]), 1);
+                    if (lane == 0) up = wq > 0 ? xb[((wq - 1) * 2 + 0) * C + o] : 0.f;
+                    sum[o] = up;
                 }
+                tc::ld32(tmem, l0, col + NOUT, c);
+#pragma unroll
+                for (int o = 0; o < NO; o++) sum[o] = sum[o] + __uint_as_float(c[o]);
+                tc::ld32(tmem, l0, col + 2 * NOUT, c);
                 tc::fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&K->acce[g]);
-                // publish the lane-quarter edges, then read the neighbours'
-                float* xb = &K->xb[g][kg & 1][0][0][0];
-                if (lane == 31)
-                    for (int o = 0; o < NO; o++) xb[(wq * 2 + 0) * C + o] = d0[o];
-                if (lane == 0)
-                    for (int o = 0; o < NO; o++) xb[(wq * 2 + 1) * C + o] = d2[o];
-                group_sync(1 + g, 128);
-                kg++;
                 uint32_t acc[32];
 #pragma unroll
                 for (int o = 0; o < NO; o++) {
-                    float up = __shfl_up_sync(0xffffffffu, d0[o], 1);
-                    float dn = __shfl_down_sync(0xffffffffu, d2[o], 1);
-                    if (lane == 0) up = wq > 0 ? xb[((wq - 1) * 2 + 0) * C + o] : 0.f;
+                    float dn = __shfl_down_sync(0xffffffffu, __uint_as_float(c[o]), 1);
                     if (lane == 31) dn = wq < 3 ? xb[((wq + 1) * 2 + 1) * C + o] : 0.f;
-                    acc[o] = __float_as_uint((up + d1[o]) + dn);
+                    acc[o] = __float_as_uint(sum[o] + dn);
                 }
                 const int r = wq * 32 + lane, x = x0 - 1 + r;
                 if (r >= 1 && r <= W3_TW && x < d.nx)
