@@ -763,24 +763,45 @@ __global__ void __launch_bounds__(LR_THREADS) last_rows_kernel(
     if (warp == 0) tc::tmem_dealloc(tmem, 64);
 }
 
-// Pass 2: grid (row of the stacked volume, block of 256 x).
+// Pass 2: grid (row of the stacked volume, block of 256 x VEC); VEC = 4 when
+// rows are 16-byte aligned (nx % 4 == 0): four x per thread in float4 loads.
+template <int VEC>
 __global__ void __launch_bounds__(256) last_sum_kernel(Dims d, const float* __restrict__ q,
                                                        const float* __restrict__ bias,
                                                        float* __restrict__ f) {
     const int64_t row = blockIdx.x;
-    const int x = blockIdx.y * 256 + threadIdx.x;
+    const int x = (blockIdx.y * 256 + threadIdx.x) * VEC;
     if (x >= d.nx) return;
     const int y = (int)(row % d.ny), z = (int)((row / d.ny) % d.nz);
     const int64_t b = row / ((int64_t)d.ny * d.nz);
     const int64_t V = nvox(d);
-    float sum = 0.f;
+    if (VEC == 4) {
+        float4 sum = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int n = 0; n < 9; n++) {
-        const int zz = z + n / 3 - 1, yy = y + n % 3 - 1;
-        if (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny)
-            sum += __ldg(q + n * V + ((b * d.nz + zz) * d.ny + yy) * d.nx + x);
+        for (int n = 0; n < 9; n++) {
+            const int zz = z + n / 3 - 1, yy = y + n % 3 - 1;
+            if (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny) {
+                const float4 v =
+                    __ldg((const float4*)(q + n * V + ((b * d.nz + zz) * d.ny + yy) * d.nx + x));
+                sum.x += v.x;
+                sum.y += v.y;
+                sum.z += v.z;
+                sum.w += v.w;
+            }
+        }
+        const float b0 = bias[0];
+        *(float4*)(f + row * d.nx + x) =
+            make_float4(sum.x + b0, sum.y + b0, sum.z + b0, sum.w + b0);
+    } else {
+        float sum = 0.f;
+#pragma unroll
+        for (int n = 0; n < 9; n++) {
+            const int zz = z + n / 3 - 1, yy = y + n % 3 - 1;
+            if (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny)
+                sum += __ldg(q + n * V + ((b * d.nz + zz) * d.ny + yy) * d.nx + x);
+        }
+        f[row * d.nx + x] = sum + bias[0];
     }
-    f[row * d.nx + x] = sum + bias[0];
 }
 
 // 1-channel input conv (the first layer, and the back projection of the last
@@ -1571,8 +1592,15 @@ static nr_status launch_last(const Dims& d, const __nv_bfloat16* in, const __nv_
     const int64_t nt = ntiles(d);
     const int grid = (int)(nt < (int64_t)sm_count() * 2 ? nt : (int64_t)sm_count() * 2);
     last_rows_kernel<<<grid, LR_THREADS, smem, s>>>(d, map.lo, map.hi, wpk, q, status);
-    const dim3 g2((unsigned)((int64_t)d.nb * d.nz * d.ny), (unsigned)((d.nx + 255) / 256));
-    last_sum_kernel<<<g2, 256, 0, s>>>(d, q, bias, f);
+    // q planes start at multiples of V floats: with nx % 4 == 0 every row is 16-byte
+    // aligned (the workspace is 256-byte aligned)
+    if (d.nx % 4 == 0) {
+        const dim3 g2((unsigned)((int64_t)d.nb * d.nz * d.ny), (unsigned)((d.nx / 4 + 255) / 256));
+        last_sum_kernel<4><<<g2, 256, 0, s>>>(d, q, bias, f);
+    } else {
+        const dim3 g2((unsigned)((int64_t)d.nb * d.nz * d.ny), (unsigned)((d.nx + 255) / 256));
+        last_sum_kernel<1><<<g2, 256, 0, s>>>(d, q, bias, f);
+    }
     return launch_status();
 }
 
