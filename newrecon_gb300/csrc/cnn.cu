@@ -1590,7 +1590,7 @@ static nr_status launch_last(const Dims& d, const __nv_bfloat16* in, const __nv_
                              (int)smem) != cudaSuccess)
         return NR_ERR_CUDA;
     const int64_t nt = ntiles(d);
-    const int grid = (int)(nt < (int64_t)sm_count() * 2 ? nt : (int64_t)sm_count() * 2);
+    const int grid = (int)(nt < (int64_t)sm_count() * 4 ? nt : (int64_t)sm_count() * 4);
     last_rows_kernel<<<grid, LR_THREADS, smem, s>>>(d, map.lo, map.hi, wpk, q, status);
     // q planes start at multiples of V floats: with nx % 4 == 0 every row is 16-byte
     // aligned (the workspace is 256-byte aligned)
