@@ -808,7 +808,8 @@ __global__ void __launch_bounds__(256) last_sum_kernel(Dims d, const float* __re
 // layer's gradient): each output row gathers its 27 neighbours (zero outside
 // its patch) x scale into one K = 32 row.  Weights: one packed 32 x 32 tile.
 template <int EPI>
-__global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restrict__ in, float scale,
+__global__ void __launch_bounds__(128) conv1_kernel(Dims d, WalkPlan wp, const float* __restrict__ in,
+                                                    float scale,
                                                     const __nv_bfloat16* __restrict__ wpk,
                                                     const float* __restrict__ bias, void* out,
                                                     const __nv_bfloat16* __restrict__ mask,
@@ -827,19 +828,31 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restr
     tc::fence_after();
     const uint32_t tmem = tslot;
     constexpr uint32_t idesc = tc::idesc_bf16(TM, C);
-    const int64_t nt = ntiles(d);
     int ntile = 0;
     int ncommit = 0;
     bool ok = true;
     const int force_at = status[1] - 1;  // test hook, as in conv32_walk_kernel
-    // the 27 neighbours of this thread's voxel in tile t (zero outside the
+    // Tiles in runs of rows along y (the items of conv32_walk_kernel), so
+    // that consecutive tiles of a CTA share six of their nine input rows.
+    struct Pos {
+        int64_t it;
+        int i, b, z, y0, ly, x0;
+    };
+    auto first = [&](int64_t it, Pos& p) {
+        p.it = it;
+        p.i = 0;
+        if (it < wp.nitems) item_pos(d, wp, it, p.b, p.z, p.x0, p.y0, p.ly);
+    };
+    auto advance = [&](Pos& p) {
+        if (++p.i >= p.ly) first(p.it + gridDim.x, p);
+    };
+    // the 27 neighbours of this thread's voxel in a tile (zero outside the
     // patch), loaded one tile ahead so that their latency overlaps the
     // previous tile's MMAs and epilogue
     float nb[27];
-    auto gather = [&](int64_t t) {
-        int b, z, y, x0;
-        tile_pos(d, t, b, z, y, x0);
-        const int x = x0 + tid;
+    auto gather = [&](const Pos& p) {
+        const int b = p.b, z = p.z, y = p.y0 + p.i;
+        const int x = p.x0 + tid;
 #pragma unroll
         for (int k = 0; k < 27; k++) {
             const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
@@ -850,10 +863,13 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restr
                         : 0.f;
         }
     };
-    if (blockIdx.x < nt) gather(blockIdx.x);
-    for (int64_t t = blockIdx.x; t < nt; t += gridDim.x) {
-        int b, z, y, x0;
-        tile_pos(d, t, b, z, y, x0);
+    Pos cur, nxt;
+    first(blockIdx.x, cur);
+    if (cur.it < wp.nitems) gather(cur);
+    for (; cur.it < wp.nitems; cur = nxt) {
+        nxt = cur;
+        advance(nxt);
+        const int b = cur.b, z = cur.z, y = cur.y0 + cur.i, x0 = cur.x0;
         const int x = x0 + tid;
         __align__(16) __nv_bfloat16 row[32];
 #pragma unroll
@@ -872,7 +888,7 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, const float* __restr
                              tc::sdesc(sw + j * 256, 128, 512), idesc, j != 0);
             tc::commit(&bars[0]);
         }
-        if (t + gridDim.x < nt) gather(t + gridDim.x);
+        if (nxt.it < wp.nitems) gather(nxt);
         if (ok) {
             ok = tc::mbar_wait(&bars[0], (uint32_t)(ncommit & 1), WAIT_LIMIT) && ntile != force_at;
             ncommit++;
@@ -1572,11 +1588,20 @@ template <int EPI>
 static nr_status launch_conv1(const Dims& d, const float* in, float scale,
                               const __nv_bfloat16* wpk, const float* bias, void* out,
                               const __nv_bfloat16* mask, int* status, cudaStream_t s) {
-    // four CTAs per SM: nine (as many as fit) measured 2.7x slower on the
-    // clinical volume (6.0 against 2.25 ms)
-    const int64_t nt = ntiles(d);
-    const int grid = (int)(nt < (int64_t)sm_count() * 4 ? nt : (int64_t)sm_count() * 4);
-    conv1_kernel<EPI><<<grid, 128, 0, s>>>(d, in, scale, wpk, bias, out, mask, status);
+    // four CTAs per SM (nine, as many as fit, measured 2.7x slower on the
+    // clinical volume), each walking runs of L rows: about eight runs per CTA
+    const int nsm = sm_count();
+    const int64_t ncols = (int64_t)d.nb * d.nz * xtiles(d);
+    int64_t L = ((int64_t)d.ny * ncols + 32LL * nsm - 1) / (32LL * nsm);
+    L = L < 1 ? 1 : (L > 32 ? 32 : L);
+    if (L > d.ny) L = d.ny;
+    WalkPlan wp;
+    wp.L = (int)L;
+    wp.nchunk = (int)((d.ny + L - 1) / L);
+    wp.tw = TM;
+    wp.nitems = ncols * wp.nchunk;
+    const int grid = (int)(wp.nitems < (int64_t)nsm * 4 ? wp.nitems : (int64_t)nsm * 4);
+    conv1_kernel<EPI><<<grid, 128, 0, s>>>(d, wp, in, scale, wpk, bias, out, mask, status);
     return launch_status();
 }
 
