@@ -905,7 +905,7 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, WalkPlan wp, const f
         tc::fence_before();
         __syncthreads();
     }
-    if (tid == 0) tc::commit(&bars[0]);  // drain, as in conv32_kernel
+    if (tid == 0) tc::commit(&bars[0]);  // drain: every MMA issued completes before TMEM goes
     if (!tc::mbar_wait(&bars[0], (uint32_t)(ncommit & 1), WAIT_LIMIT))
         tc::mbar_wait(&bars[0], (uint32_t)(ncommit & 1), WAIT_LIMIT);
     tc::fence_before();
