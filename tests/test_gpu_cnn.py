@@ -27,10 +27,12 @@ def ws():
 
 
 # (nx, ny, nz, nb): a partial x-tile, two x-tiles (one partial), one full tile,
-# four x-tiles.  The 32-channel layers run the dx-stacked kernel (126-wide
-# tiles) for nx = 20, 150 and 384 and the 128-wide walk for nx = 128.
-DIMS = [(20, 6, 5, 2), (150, 3, 4, 1), (128, 4, 3, 1), (384, 8, 5, 1)]
-DIM_IDS = ["partial", "two_tiles", "full_tile", "four_tiles"]
+# four x-tiles, and one row per plane (ny = 1: every row-set but the centre
+# lies outside the patch) in three stacked patches of two planes.  The
+# 32-channel layers run the dx-stacked kernel (126-wide tiles) for nx = 20,
+# 150, 384 and 200 and the 128-wide walk for nx = 128.
+DIMS = [(20, 6, 5, 2), (150, 3, 4, 1), (128, 4, 3, 1), (384, 8, 5, 1), (200, 1, 2, 3)]
+DIM_IDS = ["partial", "two_tiles", "full_tile", "four_tiles", "one_row"]
 
 
 def data(dims, seed):
