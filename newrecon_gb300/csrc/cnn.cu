@@ -1296,6 +1296,246 @@ __global__ void __launch_bounds__(WG_THREADS, 1) wgrad_tc_kernel(
     if (warp == 0) tc::tmem_dealloc(tmem, Cfg::NCOL);
 }
 
+// ---- 32 -> 32 weight gradient walking along y --------------------------------
+// The WG_HID GEMM of wgrad_tc_kernel with its staging shared between
+// neighbouring rows, as in conv32_walk_kernel: a CTA takes runs of L rows y of
+// one (patch, z, x tile) column; the input strips come as row-sets (the strips
+// of one input row in planes z - 1, z, z + 1) through a ring of GW_R slots, each
+// row-set loaded once for the three K blocks (output rows) that read it.  Per
+// K step three MMAs of N = 96, one per row-set (its three strips; the ring's
+// slots are not contiguous), into TMEM columns 96 dy + 32 dz + i.  The
+// gradient strip is loaded once per K block (from x0 - 1) and the builder
+// warps derive the copies staged from x0 + 1 and x0 (rows shifted by 2 and 1)
+// in shared memory; copy 3 stays zero.  About 5.5 strips are staged per K
+// block instead of 12.  Roles as in wgrad_tc_kernel; every wait is bounded.
+constexpr int GW_R = 5;
+constexpr int GW_G = 4 * WG_STRIP;  // one gradient stage: copies 0..3
+constexpr int GW_THREADS = 192;
+
+struct GwCtl {
+    uint64_t rfull[GW_R], rempty[GW_R], gfull[2], gbuilt[2], gempty[2], drain;
+    uint32_t tslot;
+    int abort;
+    float bsum[4][C];
+};
+
+__global__ void __launch_bounds__(GW_THREADS, 1) wgrad_walk_kernel(
+    Dims d, WalkPlan wp, const __grid_constant__ CUtensorMap amap,
+    const __grid_constant__ CUtensorMap amap_hi, const __grid_constant__ CUtensorMap gmap,
+    const __grid_constant__ CUtensorMap gmap_hi, float* __restrict__ partial, int* status) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t* ring = smem;
+    uint8_t* gst = smem + GW_R * W_SET;
+    GwCtl* K = (GwCtl*)(gst + 2 * GW_G);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int k = tid; k < WG_STRIP / 16; k += GW_THREADS) {  // copy 3 of both stages: zeros
+        ((uint4*)(gst + 3 * WG_STRIP))[k] = make_uint4(0, 0, 0, 0);
+        ((uint4*)(gst + GW_G + 3 * WG_STRIP))[k] = make_uint4(0, 0, 0, 0);
+    }
+    tc::fence_async_smem();
+    if (tid == 0) {
+        for (int s = 0; s < GW_R; s++) {
+            tc::mbar_init(&K->rfull[s], 1);
+            tc::mbar_init(&K->rempty[s], 1);
+        }
+        for (int s = 0; s < 2; s++) {
+            tc::mbar_init(&K->gfull[s], 1);
+            tc::mbar_init(&K->gbuilt[s], 4);
+            tc::mbar_init(&K->gempty[s], 1);
+        }
+        tc::mbar_init(&K->drain, 1);
+        K->abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tc::tmem_alloc(&K->tslot, 512);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = K->tslot;
+    volatile int* abort = &K->abort;
+    auto fail = [&]() {
+        if (!*abort) atomicOr(status, NR_FLAG_TIMEOUT);
+        *abort = 1;
+        __threadfence_block();
+    };
+    auto strip_ok = [&](int zz, int yy) { return zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny; };
+    if (warp == 0) {
+        if (lane == 0) {
+            // producer: per item row-sets 0 and 1, then per K block i row-set
+            // i + 2 and the gradient strip
+            int64_t G = 0, kb = 0, rissued = 0, kissued = 0;
+            bool stop = false;
+            auto load_set = [&](int b, int z, int x0, int Y) {
+                const int s = (int)(G % GW_R);
+                if (G >= GW_R &&
+                    !wait_live(&K->rempty[s], (uint32_t)((G / GW_R - 1) & 1), abort))
+                    return false;
+                mbar_arrive_tx(&K->rfull[s], 3 * STRIP_TX);
+                for (int dz = 0; dz < 3; dz++)
+                    load_strip(ring + s * W_SET + dz * TSTRIP, PLANE, &amap, &amap_hi, x0,
+                               strip_ok(z + dz - 1, Y) ? (b * d.nz + z + dz - 1) * d.ny + Y : -1,
+                               &K->rfull[s]);
+                rissued = ++G;
+                return true;
+            };
+            for (int64_t it = blockIdx.x; it < wp.nitems && !stop && !*abort; it += gridDim.x) {
+                int b, z, x0, y0, ly;
+                item_pos(d, wp, it, b, z, x0, y0, ly);
+                if (!load_set(b, z, x0, y0 - 1) || !load_set(b, z, x0, y0)) {
+                    fail();
+                    break;
+                }
+                for (int i = 0; i < ly; i++, kb++) {
+                    if (!load_set(b, z, x0, y0 + i + 1)) {
+                        fail();
+                        stop = true;
+                        break;
+                    }
+                    const int gs = (int)(kb & 1);
+                    if (kb >= 2 && !wait_live(&K->gempty[gs], (uint32_t)(((kb >> 1) - 1) & 1), abort)) {
+                        fail();
+                        stop = true;
+                        break;
+                    }
+                    mbar_arrive_tx(&K->gfull[gs], STRIP_TX);
+                    load_strip(gst + gs * GW_G + 2 * WG_STRIP, PLANE, &gmap, &gmap_hi, x0,
+                               (b * d.nz + z) * d.ny + y0 + i, &K->gfull[gs]);
+                    kissued = kb + 1;
+                }
+            }
+            // no copy may be in flight when the block exits
+            for (int64_t k = rissued > GW_R ? rissued - GW_R : 0; k < rissued; k++) {
+                uint64_t* bar = &K->rfull[k % GW_R];
+                if (!tc::mbar_wait(bar, (uint32_t)((k / GW_R) & 1), WAIT_LIMIT))
+                    tc::mbar_wait(bar, (uint32_t)((k / GW_R) & 1), WAIT_LIMIT);
+            }
+            for (int64_t k = kissued > 2 ? kissued - 2 : 0; k < kissued; k++) {
+                uint64_t* bar = &K->gfull[k & 1];
+                if (!tc::mbar_wait(bar, (uint32_t)((k >> 1) & 1), WAIT_LIMIT))
+                    tc::mbar_wait(bar, (uint32_t)((k >> 1) & 1), WAIT_LIMIT);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // MMA issuer.  Test hook: the workspace's second status word k + 1
+            // > 0 makes the wait for this CTA's K block k report giving up
+            // once it has in fact succeeded.
+            const int force_at = status[1] - 1;
+            constexpr uint32_t idesc = tc::idesc_bf16(TM, 96) | (1u << 15) | (1u << 16);
+            const uint64_t ad0 = tc::sdesc(tc::smem_u32(gst), 128, WG_PLANE);
+            const uint64_t bd0 = tc::sdesc(tc::smem_u32(ring), 128, WG_PLANE);
+            int64_t G = 0, kb = 0;
+            bool stop = false;
+            for (int64_t it = blockIdx.x; it < wp.nitems && !stop && !*abort; it += gridDim.x) {
+                int b, z, x0, y0, ly;
+                item_pos(d, wp, it, b, z, x0, y0, ly);
+                for (int i = 0; i < ly; i++, kb++) {
+                    const int gs = (int)(kb & 1);
+                    bool got = wait_live(&K->gbuilt[gs], (uint32_t)((kb >> 1) & 1), abort);
+                    int slot[3];
+                    for (int dy = 0; dy < 3 && got; dy++) {
+                        const int64_t g2 = G + i + dy;
+                        slot[dy] = (int)(g2 % GW_R);
+                        if (i == 0 || dy == 2)
+                            got = wait_live(&K->rfull[slot[dy]], (uint32_t)((g2 / GW_R) & 1), abort);
+                    }
+                    if (kb == force_at) got = false;
+                    if (!got) {
+                        fail();
+                        stop = true;
+                        break;
+                    }
+                    tc::fence_after();
+                    const uint64_t adg = ad0 + (uint64_t)((gs * GW_G) >> 4);
+#pragma unroll
+                    for (int ks = 0; ks < TM / 16; ks++)
+#pragma unroll
+                        for (int dy = 0; dy < 3; dy++)
+                            tc::mma_bf16(tmem + (uint32_t)(dy * 96),
+                                         adg + (uint64_t)((ks * 256) >> 4),
+                                         bd0 + (uint64_t)((slot[dy] * W_SET + 16 + ks * 256) >> 4),
+                                         idesc, (kb > 0 || ks > 0) ? 1u : 0u);
+                    tc::commit(&K->gempty[gs]);
+                    // row-set i is not read after this K block; the last one of
+                    // the item also frees row-sets ly and ly + 1
+                    tc::commit(&K->rempty[slot[0]]);
+                    if (i == ly - 1) {
+                        tc::commit(&K->rempty[slot[1]]);
+                        tc::commit(&K->rempty[slot[2]]);
+                    }
+                }
+                G += ly + 2;
+            }
+        }
+    } else {
+        // warps 2-5: the shifted gradient copies and the bias sum
+        const int h = warp - 2;
+        float bacc = 0.f;
+        int64_t kb = 0;
+        bool stop = false;
+        for (int64_t it = blockIdx.x; it < wp.nitems && !stop && !*abort; it += gridDim.x) {
+            int b, z, x0, y0, ly;
+            item_pos(d, wp, it, b, z, x0, y0, ly);
+            for (int i = 0; i < ly; i++, kb++) {
+                const int gs = (int)(kb & 1);
+                if (!__all_sync(0xffffffffu,
+                                wait_live(&K->gfull[gs], (uint32_t)((kb >> 1) & 1), abort))) {
+                    if (lane == 0) fail();
+                    stop = true;
+                    break;
+                }
+                uint8_t* st = gst + gs * GW_G;
+                // copy c (c = 0, 1) row r = copy 2 row r + 2 - c, r < 128: 8 planes
+                // x 128 rows of 16 bytes over the 128 builder threads
+                const int t = h * 32 + lane;
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const int u = k * 128 + t;  // 0 .. 1023
+                    const int c = u >> 9, p = (u >> 7) & 3, r = u & 127;
+                    const uint4 v = *(const uint4*)(st + 2 * WG_STRIP + p * WG_PLANE + (r + 2 - c) * 16);
+                    *(uint4*)(st + c * WG_STRIP + p * WG_PLANE + r * 16) = v;
+                }
+                // channel o = lane of x = 32 h .. 32 h + 31 (copy 2, row x + 1)
+                const uint8_t* gp = st + 2 * WG_STRIP + (lane >> 3) * WG_PLANE + (lane & 7) * 2;
+#pragma unroll 8
+                for (int x = 32 * h; x < 32 * h + 32; x++)
+                    bacc += __bfloat162float(*(const __nv_bfloat16*)(gp + (x + 1) * 16));
+                tc::fence_async_smem();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&K->gbuilt[gs]);
+            }
+        }
+        K->bsum[h][lane] = bacc;
+    }
+    // drain: every MMA issued has completed before TMEM is read or released
+    __syncthreads();
+    if (warp == 1 && lane == 0) tc::commit(&K->drain);
+    if (!tc::mbar_wait(&K->drain, 0, WAIT_LIMIT)) tc::mbar_wait(&K->drain, 0, WAIT_LIMIT);
+    tc::fence_after();
+    const bool ok = *abort == 0;
+    float* prow = partial + (int64_t)blockIdx.x * 28 * C * C;
+    // TMEM lane 32 dx + o, column 96 dy + 32 dz + i: dW[9 dz + 3 dy + dx][o][i]
+    if (ok && warp < 3) {
+        for (int dy = 0; dy < 3; dy++)
+            for (int dz = 0; dz < 3; dz++) {
+                uint32_t acc[32];
+                tc::ld32(tmem, (uint32_t)(warp * 32), (uint32_t)(dy * 96 + dz * 32), acc);
+                float4* dst = (float4*)(prow + ((dz * 9 + dy * 3 + warp) * C + lane) * C);
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    dst[j] = make_float4(__uint_as_float(acc[4 * j]), __uint_as_float(acc[4 * j + 1]),
+                                         __uint_as_float(acc[4 * j + 2]),
+                                         __uint_as_float(acc[4 * j + 3]));
+            }
+    }
+    if (ok && warp == 3)
+        prow[(27 * C + lane) * C] =
+            ((K->bsum[0][lane] + K->bsum[1][lane]) + K->bsum[2][lane]) + K->bsum[3][lane];
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 512);
+}
+
 // grad[tap][o][i] (and grad_b[o] from tap 27, i = 0) = the sum of the CTAs'
 // partials (partial[cta][e], e = tap nout + o ni + i).  A block of 8 warps
 // takes 32 consecutive e: warp w adds, in CTA order, the CTAs of its eighth of
@@ -1702,7 +1942,23 @@ static nr_status wgrad(const Dims& d, int l, const void* g, const void* in, floa
     } else if (l == 5) {
         e = launch_wgrad<WG_LAST>(d, am, gm, (const float*)g, nullptr, 1.f, part, status, nch, st);
     } else {
-        e = launch_wgrad<WG_HID>(d, am, gm, nullptr, nullptr, 1.f, part, status, nch, st);
+        // runs of L rows along y: about eight per CTA
+        int64_t L = ((int64_t)d.ny * d.nb * d.nz * xtiles(d) + 8 * nch - 1) / (8 * nch);
+        L = L < 4 ? 4 : (L > 32 ? 32 : L);
+        if (L > d.ny) L = d.ny;
+        WalkPlan wp;
+        wp.L = (int)L;
+        wp.nchunk = (int)((d.ny + L - 1) / L);
+        wp.tw = TM;
+        wp.nitems = (int64_t)d.nb * d.nz * xtiles(d) * wp.nchunk;
+        if (wp.nitems < nch) nch = wp.nitems;
+        const size_t smem = (size_t)GW_R * W_SET + 2 * GW_G + sizeof(GwCtl);
+        if (cudaFuncSetAttribute(wgrad_walk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return NR_ERR_CUDA;
+        wgrad_walk_kernel<<<(unsigned)nch, GW_THREADS, smem, st>>>(d, wp, am.lo, am.hi, gm.lo,
+                                                                   gm.hi, part, status);
+        e = launch_status();
         nout = C * C;
     }
     if (e != NR_OK) return e;
