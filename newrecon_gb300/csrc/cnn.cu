@@ -924,14 +924,8 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, WalkPlan wp, const f
 // consecutive x in 16-byte rows), and strips staged one after another sit at
 // one uniform plane stride, so several strips form one operand whose rows are
 // (strip, channel), and a shift along x is a 16-byte start offset.
-//   WG_HID   (32 -> 32)  The shift moves to the gradient: per row of the
-//                        volume, sum_x g[x] a[x + dx - 1] = sum_x' g[x' + 1 - dx]
-//                        a[x'] (both zero outside the row), so with K = x' the
-//                        nine input strips are B unshifted (N = 9 x 32 = 288,
-//                        two MMAs of N = 144) and A (M = 128) is the gradient
-//                        strip staged three times, copy c from x0 + 1 - c (rows
-//                        (c, o); copy 3 is zeros).  D[(dx, o)][(strip, i)]: 16
-//                        MMAs per K block, each reading 8.6 KB of operands.
+// This kernel serves the 1-channel layers (the 32 -> 32 ones walk along y in
+// wgrad_walk_kernel, below):
 //   WG_LAST  (32 -> 1)   A = four input strips (rows (strip, i)) at the tap's
 //                        x shift: blocks {0-3}, {4-7}, {5-8} (of the last only
 //                        strip 8's rows are kept) x dx = 9 MMA blocks; B = the
@@ -957,7 +951,7 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, WalkPlan wp, const f
 // copy it issued.  Each CTA writes one partial per weight (row blockIdx.x of
 // partial[CTA][28 x weights per tap]); wgrad_reduce_kernel adds the rows in
 // order.
-enum { WG_HID = 0, WG_LAST = 1, WG_FIRST = 2 };
+enum { WG_LAST = 1, WG_FIRST = 2 };
 constexpr int WG_MAXCTA = 256;  // partial slots per weight
 constexpr int WG_GROUP = 2048;  // K-major built operand: bytes per 8-row group (16 K chunks)
 constexpr int WG_PLANE = 2176;  // staged plane: 130 rows x 16 B, 128-B aligned
@@ -974,17 +968,17 @@ struct WgCtl {
 
 template <int MODE>
 struct WgCfg {
-    // one stage: [input strips 0..8 | gradient strip copies | built operand]
+    // one stage: [input strips 0..8 | gradient strip | built operand]
     static constexpr int NSTRIP = MODE == WG_FIRST ? 0 : 9;
-    static constexpr int NCOPY = MODE == WG_HID ? 4 : (MODE == WG_FIRST ? 1 : 0);
-    static constexpr int NLOAD = MODE == WG_HID ? 3 : NCOPY;  // copies loaded (HID copy 3: zeros)
+    static constexpr int NCOPY = MODE == WG_FIRST ? 1 : 0;
+    static constexpr int NLOAD = NCOPY;
     static constexpr int OFF_G = NSTRIP * WG_STRIP;
     static constexpr int OFF_X = OFF_G + NCOPY * WG_STRIP;
     static constexpr int XBYTES =
         MODE == WG_LAST ? 2 * WG_GROUP : (MODE == WG_FIRST ? 16 * WG_GROUP : 0);
     static constexpr int STAGE = OFF_X + XBYTES;
     static constexpr uint32_t TX = (uint32_t)(NSTRIP + NLOAD) * KCH * SROWS * 16;
-    static constexpr int N = MODE == WG_HID ? 144 : (MODE == WG_LAST ? 16 : C);
+    static constexpr int N = MODE == WG_LAST ? 16 : C;
     static constexpr uint32_t NCOL = MODE == WG_FIRST ? 32 : 512;
     // WG_FIRST: each builder warp's window of the input, 9 rows x WG_WIN x
     static constexpr int XS = MODE == WG_FIRST ? 4 * 9 * WG_WIN * 4 : 0;
@@ -1046,8 +1040,8 @@ __global__ void __launch_bounds__(WG_THREADS, 1) wgrad_tc_kernel(
     WgCtl* K = (WgCtl*)(smem + 2 * Cfg::STAGE + Cfg::XS);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     // regions the copies and the builders never write stay zero
-    constexpr int ZOFF = MODE == WG_HID ? Cfg::OFF_G + 3 * WG_STRIP : Cfg::OFF_X;
-    constexpr int ZBYTES = MODE == WG_HID ? WG_STRIP : Cfg::XBYTES;
+    constexpr int ZOFF = Cfg::OFF_X;
+    constexpr int ZBYTES = Cfg::XBYTES;
     for (int k = tid; k < ZBYTES / 16; k += WG_THREADS) {
         ((uint4*)(smem + ZOFF))[k] = make_uint4(0, 0, 0, 0);
         ((uint4*)(smem + Cfg::STAGE + ZOFF))[k] = make_uint4(0, 0, 0, 0);
@@ -1094,7 +1088,7 @@ __global__ void __launch_bounds__(WG_THREADS, 1) wgrad_tc_kernel(
                 // gradient copy c starts at x0 + 1 - c (HID) / x0 - 1 (FIRST)
                 for (int c = 0; c < Cfg::NLOAD; c++)
                     load_strip(st + Cfg::OFF_G + c * WG_STRIP, WG_PLANE, &gmap, &gmap_hi,
-                               MODE == WG_HID ? x0 + 2 - c : x0, grow, &K->tfull[sg]);
+                               x0, grow, &K->tfull[sg]);
                 for (int q = 0; q < Cfg::NSTRIP; q++) {
                     const int zz = z + q / 3 - 1, yy = y + q % 3 - 1;
                     const int row = (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny)
@@ -1123,7 +1117,7 @@ __global__ void __launch_bounds__(WG_THREADS, 1) wgrad_tc_kernel(
                 const int sg = (int)(kb & 1);
                 const uint32_t par = (uint32_t)((kb >> 1) & 1);
                 bool got = wait_live(&K->tfull[sg], par, abort);
-                if (MODE != WG_HID && got) got = wait_live(&K->bfull[sg], par, abort);
+                if (got) got = wait_live(&K->bfull[sg], par, abort);
                 if (kb == force_at) got = false;
                 if (!got) {
                     fail();
@@ -1131,21 +1125,7 @@ __global__ void __launch_bounds__(WG_THREADS, 1) wgrad_tc_kernel(
                 }
                 tc::fence_after();
                 const uint32_t sb = tc::smem_u32(smem + sg * Cfg::STAGE);
-                if (MODE == WG_HID) {
-                    // columns 0-143: strips 0-3 and channels 0-15 of strip 4;
-                    // columns 144-287: the rest (from plane 2 of strip 4)
-#pragma unroll
-                    for (int k = 0; k < TM / 16; k++) {
-                        const uint64_t ad = tc::sdesc(sb + Cfg::OFF_G + k * 256, 128, WG_PLANE);
-                        const uint32_t acc = (kb > 0 || k > 0) ? 1u : 0u;
-                        tc::mma_bf16(tmem, ad, tc::sdesc(sb + 16 + k * 256, 128, WG_PLANE),
-                                     Cfg::IDESC, acc);
-                        tc::mma_bf16(tmem + 144, ad,
-                                     tc::sdesc(sb + 4 * WG_STRIP + 2 * WG_PLANE + 16 + k * 256,
-                                               128, WG_PLANE),
-                                     Cfg::IDESC, acc);
-                    }
-                } else if (MODE == WG_FIRST) {
+                if (MODE == WG_FIRST) {
 #pragma unroll
                     for (int k = 0; k < TM / 16; k++)
                         tc::mma_bf16(tmem, tc::sdesc(sb + Cfg::OFF_X + k * 256, 128, WG_GROUP),
@@ -1178,11 +1158,11 @@ __global__ void __launch_bounds__(WG_THREADS, 1) wgrad_tc_kernel(
         float r[NR];  // the next block's global data, in flight
         float bacc = 0.f;
         int64_t t = blockIdx.x;
-        if (MODE != WG_HID && t < nt) wg_fetch<MODE>(d, t, h, lane, gvec, xin, s, r);
+        if (t < nt) wg_fetch<MODE>(d, t, h, lane, gvec, xin, s, r);
         for (int64_t kb = 0; t < nt && !*abort; t += gridDim.x, kb++) {
             const int sg = (int)(kb & 1);
             uint8_t* st = smem + sg * Cfg::STAGE;
-            if (MODE != WG_HID) {
+            {
                 if (!__all_sync(0xffffffffu,
                                 kb < 2 || wait_live(&K->empty[sg],
                                                     (uint32_t)(((kb >> 1) - 1) & 1), abort))) {
@@ -1222,7 +1202,7 @@ __global__ void __launch_bounds__(WG_THREADS, 1) wgrad_tc_kernel(
                 }
                 // channel o = lane of x = 32 h .. 32 h + 31, in the gradient
                 // copy staged from x0 - 1 (row x + 1)
-                const uint8_t* gp = st + Cfg::OFF_G + (MODE == WG_HID ? 2 * WG_STRIP : 0) +
+                const uint8_t* gp = st + Cfg::OFF_G +
                                     (lane >> 3) * WG_PLANE + (lane & 7) * 2;
 #pragma unroll 8
                 for (int x = 32 * h; x < 32 * h + 32; x++)
@@ -1239,26 +1219,11 @@ __global__ void __launch_bounds__(WG_THREADS, 1) wgrad_tc_kernel(
     if (!tc::mbar_wait(&K->drain, 0, WAIT_LIMIT)) tc::mbar_wait(&K->drain, 0, WAIT_LIMIT);
     tc::fence_after();
     const bool ok = *abort == 0;
-    float* prow = partial + (int64_t)blockIdx.x * 28 * (MODE == WG_HID ? C * C : C);
+    float* prow = partial + (int64_t)blockIdx.x * 28 * C;
     auto bias_of = [&](int o) {
         return ((K->bsum[0][o] + K->bsum[1][o]) + K->bsum[2][o]) + K->bsum[3][o];
     };
-    if (MODE == WG_HID) {
-        // TMEM lane 32 dx + o, column 32 q + i: dW[3 q + dx][o][i]
-        if (ok && warp < 3) {
-            for (int q = 0; q < 9; q++) {
-                uint32_t acc[32];
-                tc::ld32(tmem, (uint32_t)(warp * 32), (uint32_t)(q * 32), acc);
-                float4* dst = (float4*)(prow + ((3 * q + warp) * C + lane) * C);
-#pragma unroll
-                for (int j = 0; j < 8; j++)
-                    dst[j] = make_float4(__uint_as_float(acc[4 * j]), __uint_as_float(acc[4 * j + 1]),
-                                         __uint_as_float(acc[4 * j + 2]),
-                                         __uint_as_float(acc[4 * j + 3]));
-            }
-        }
-        if (ok && warp == 3) prow[(27 * C + lane) * C] = bias_of(lane);
-    } else if (MODE == WG_FIRST) {
+    if (MODE == WG_FIRST) {
         // rows 32 + tap (lo) of warp 1 meet rows tap (hi) of warp 0
         float* lo = (float*)smem;  // the stages are idle now
         uint32_t acc[32];
@@ -1297,8 +1262,12 @@ __global__ void __launch_bounds__(WG_THREADS, 1) wgrad_tc_kernel(
 }
 
 // ---- 32 -> 32 weight gradient walking along y --------------------------------
-// The WG_HID GEMM of wgrad_tc_kernel with its staging shared between
-// neighbouring rows, as in conv32_walk_kernel: a CTA takes runs of L rows y of
+// dW of a 32 -> 32 layer: the tap's x shift moves onto the gradient (per row of
+// the volume, sum_x g[x] a[x + dx - 1] = sum_x' g[x' + 1 - dx] a[x'], both zero
+// outside the row), so that with K = x' the input strips are B unshifted (rows
+// (strip, i)) and A (M = 128) is the gradient strip in three copies, copy c
+// staged from x0 + 1 - c (rows (c, o); copy 3 is zeros): D[(dx, o)][(strip, i)].
+// The staging is shared between neighbouring rows, as in conv32_walk_kernel: a CTA takes runs of L rows y of
 // one (patch, z, x tile) column; the input strips come as row-sets (the strips
 // of one input row in planes z - 1, z, z + 1) through a ring of GW_R slots, each
 // row-set loaded once for the three K blocks (output rows) that read it.  Per
