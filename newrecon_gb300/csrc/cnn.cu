@@ -201,9 +201,15 @@ __device__ __forceinline__ void epilogue_rx(const uint32_t* acc, int64_t row, in
     const int64_t o0 = row * KCH * (int64_t)nx * 8 + (int64_t)x * 8;  // chunk q at o0 + q nx 8
     __align__(16) __nv_bfloat16 o[C];
     if (EPI == EPI_RELU) {
+        // the bias in FP32, then BF16 pairs and the ReLU on the pairs (rounding
+        // is monotone, so max(round(v), 0) = round(max(v, 0)) up to a zero's sign)
+        const __nv_bfloat162 zero2 = __float2bfloat162_rn(0.f);
 #pragma unroll
-        for (int c = 0; c < C; c++)
-            o[c] = __float2bfloat16(fmaxf(__uint_as_float(acc[c]) + bias[c], 0.f));
+        for (int c = 0; c < C; c += 2)
+            ((__nv_bfloat162*)o)[c / 2] =
+                __hmax2(__floats2bfloat162_rn(__uint_as_float(acc[c]) + bias[c],
+                                              __uint_as_float(acc[c + 1]) + bias[c + 1]),
+                        zero2);
     } else {
         __align__(16) __nv_bfloat16 m[C];
 #pragma unroll
@@ -849,18 +855,21 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, WalkPlan wp, const f
     // the 27 neighbours of this thread's voxel in a tile (zero outside the
     // patch), loaded one tile ahead so that their latency overlaps the
     // previous tile's MMAs and epilogue
+    // The nine rows' bases and validity and the three x offsets' validity
+    // are formed once per tile; each tap is then one predicated load.
     float nb[27];
     auto gather = [&](const Pos& p) {
         const int b = p.b, z = p.z, y = p.y0 + p.i;
         const int x = p.x0 + tid;
+        const bool xv[3] = {x >= 1 && x - 1 < d.nx, x < d.nx, x + 1 < d.nx};
 #pragma unroll
-        for (int k = 0; k < 27; k++) {
-            const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
-            const int zz = z + dz, yy = y + dy, xx = x + dx;
-            nb[k] = (zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny && xx >= 0 && xx < d.nx &&
-                     x < d.nx)
-                        ? __ldg(in + (((int64_t)b * d.nz + zz) * d.ny + yy) * d.nx + xx)
-                        : 0.f;
+        for (int q = 0; q < 9; q++) {
+            const int zz = z + q / 3 - 1, yy = y + q % 3 - 1;
+            const bool rv = zz >= 0 && zz < d.nz && yy >= 0 && yy < d.ny;
+            const float* row = in + (((int64_t)b * d.nz + (rv ? zz : z)) * d.ny + (rv ? yy : y)) * d.nx;
+#pragma unroll
+            for (int dx = 0; dx < 3; dx++)
+                nb[3 * q + dx] = (rv && xv[dx]) ? __ldg(row + x + dx - 1) : 0.f;
         }
     };
     Pos cur, nxt;
@@ -871,9 +880,11 @@ __global__ void __launch_bounds__(128) conv1_kernel(Dims d, WalkPlan wp, const f
         advance(nxt);
         const int b = cur.b, z = cur.z, y = cur.y0 + cur.i, x0 = cur.x0;
         const int x = x0 + tid;
-        __align__(16) __nv_bfloat16 row[32];
+        __align__(16) __nv_bfloat162 row[16];
 #pragma unroll
-        for (int k = 0; k < 32; k++) row[k] = __float2bfloat16(k < 27 ? nb[k] * scale : 0.f);
+        for (int k = 0; k < 16; k++)
+            row[k] = __floats2bfloat162_rn(2 * k < 27 ? nb[2 * k] * scale : 0.f,
+                                           2 * k + 1 < 27 ? nb[2 * k + 1] * scale : 0.f);
         // previous tile's MMAs have completed (waited below), so sA is free
 #pragma unroll
         for (int kc = 0; kc < KCH; kc++) *(uint4*)(sA + kc * TM * 16 + tid * 16) = ((uint4*)row)[kc];
