@@ -2,7 +2,7 @@
 
 An early OSTR iterate (after 2 iterations) goes in; the network predicts the
 converged volume (50 iterations) as x_warm = max(0, x + f(s x)/s); OSTR then
-continues from x_warm.  Plain OSTR is both the fallback and the judge: the
+continues from x_warm.  Plain OSTR is both the fallback and the arbiter: the
 warm start is kept only if, at equal total subset-iterations, its FP64
 penalized-likelihood objective is no worse than plain OSTR's.
 
