@@ -1774,12 +1774,13 @@ static nr_status launch_conv32(const Dims& d, const __nv_bfloat16* in, const __n
     wp.L = (int)L;
     wp.nchunk = (int)((d.ny + L - 1) / L);
     const int grid_max = nsm;
-    // The dx-stacked kernel costs about 0.73 of the other per tile (clinical
-    // network forward 18.45 ms over 126-wide tiles against 22.48 ms over
-    // 128-wide ones) but needs ceil(nx / 126) tiles per row: it is used when
-    // that is cheaper (not for nx = 128 or 256).
+    // The dx-stacked kernel costs about 0.6 of the other per row of tiles
+    // (whole network on 512 x 60 planes: 1.46 against 2.36 ms at one tile per
+    // row, nx = 126 / 128; 2.73 against 4.60 ms at two, nx = 252 / 256) but
+    // needs ceil(nx / 126) tiles per row: it is used when that is cheaper
+    // (not for nx = 128, where two of its tiles cost 2.73 ms against 2.36).
     const int t126 = (d.nx + W3_TW - 1) / W3_TW, t128 = (d.nx + TM - 1) / TM;
-    if (73 * t126 < 100 * t128) {
+    if (60 * t126 < 100 * t128) {
         wp.tw = W3_TW;
         wp.nitems = (int64_t)d.nb * d.nz * t126 * wp.nchunk;
         const size_t smem = (size_t)W_R * W_SET + 27 * NOUT * C * 2 + sizeof(W3Ctl);

@@ -111,9 +111,9 @@ def test_staged_projection_expiry_falls_back_to_global_reads(mod):
     assert staged.check() == 0
 
 
-@pytest.mark.parametrize("dims", [(256, 40, 8, 1), (252, 40, 8, 1)], ids=["walk128", "dx3"])
+@pytest.mark.parametrize("dims", [(128, 40, 8, 1), (252, 40, 8, 1)], ids=["walk128", "dx3"])
 def test_convolution_expiry_releases_tensor_memory(mod, dims):
-    """The tensor-core convolutions (the 128-wide walk for nx = 256, the
+    """The tensor-core convolutions (the 128-wide walk for nx = 128, the
     dx-stacked kernel for nx = 252): a tile wait that gives up flags the
     timeout, drains and releases TMEM; with the hook off the next forward
     pass on the same workspace is the reference's bit for bit.  Every CTA
