@@ -15,7 +15,11 @@ tests can only observe through their results:
   the weights of the three dx taps read as one N = 96 operand from the packed
   buffer (``bpk_index`` and the 512-byte row-group stride), and the output as
   D[r - 1][dx 0] + D[r][dx 1] + D[r + 1][dx 2] with the lane-quarter exchange,
-  against a direct 3x3x3 convolution.
+  against a direct 3x3x3 convolution;
+* the 32 -> 32 weight gradient of ``wgrad_walk_kernel`` (the tap's shift moved
+  onto three gradient copies, two of them built by row shifts) against a direct
+  weight gradient, and the BF16 hi/lo split of the 1-channel layers' FP32
+  operands.
 """
 import random
 
@@ -140,3 +144,63 @@ def test_dx_stacked_tile_arithmetic(dims, nout):
                                 out[b, z, y, x] = (up + D[r, nout:2 * nout]) + dn
     ref = sum(_shift(a, t // 9 - 1, (t // 3) % 3 - 1, t % 3 - 1) @ W[t].T for t in range(27))
     assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_weight_gradient_shifted_copies():
+    """``wgrad_walk_kernel``: per K block (128 voxels x0 .. x0 + 127 of a row)
+    A = three copies of the gradient strip, copy c staged from x0 + 1 - c and
+    built from the one strip loaded from x0 - 1 by shifting rows by 2 - c; B =
+    the row-sets' strips (staged from x0 - 1, read from row 1); D[(c, o)][(dy,
+    dz, i)] summed over K blocks is dW[9 dz + 3 dy + c][o][i]."""
+    rng = np.random.default_rng(4)
+    nb, nz, ny, nx = 2, 3, 4, 200
+    a = rng.standard_normal((nb, nz, ny, nx, C))
+    g = rng.standard_normal((nb, nz, ny, nx, C))
+
+    def strip(t, b, z, y, x0):  # rows x0 - 1 .. x0 + 128, zero outside the patch
+        s = np.zeros((130, C))
+        if 0 <= z < nz and 0 <= y < ny:
+            lo, hi = max(x0 - 1, 0), min(x0 + 129, nx)
+            s[lo - (x0 - 1):hi - (x0 - 1)] = t[b, z, y, lo:hi]
+        return s
+
+    D = np.zeros((3, C, 3, 3, C))  # [c][o][dy][dz][i]
+    for b in range(nb):
+        for z in range(nz):
+            for y in range(ny):
+                for x0 in range(0, nx, 128):
+                    g2 = strip(g, b, z, y, x0)                       # copy 2
+                    copies = [g2[2 - c:2 - c + 128] for c in range(3)]  # rows r + 2 - c
+                    for dy in range(3):
+                        for dz in range(3):
+                            s = strip(a, b, z + dz - 1, y + dy - 1, x0)[1:129]
+                            for c in range(3):
+                                D[c, :, dy, dz, :] += copies[c].T @ s
+    ref = np.stack([np.einsum("bzyxo,bzyxi->oi", g, _shift(a, t // 9 - 1, (t // 3) % 3 - 1,
+                                                            t % 3 - 1)) for t in range(27)])
+    got = np.zeros_like(ref)
+    for c in range(3):
+        for dy in range(3):
+            for dz in range(3):
+                got[dz * 9 + dy * 3 + c] = D[c, :, dy, dz, :]
+    assert np.abs(got - ref).max() <= 1e-11 * np.abs(ref).max()
+
+
+def test_bf16_hi_lo_split():
+    """The split operands of the 1-channel layers' weight gradients: hi =
+    bf16(u), lo = bf16(u - hi) reproduces u to 2^-17 relative (round to nearest
+    even, as __float2bfloat16_rn), and u - hi is exact in FP32."""
+    def bf16(v):
+        v = np.asarray(v, np.float32)
+        u = v.view(np.uint32).astype(np.uint64)
+        r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+        return r.astype(np.uint32).view(np.float32)
+
+    rng = np.random.default_rng(5)
+    u = (rng.standard_normal(1 << 16) * np.exp(rng.uniform(-20, 20, 1 << 16))).astype(np.float32)
+    hi = bf16(u)
+    d = (u - hi).astype(np.float32)
+    assert np.array_equal(d.astype(np.float64), u.astype(np.float64) - hi.astype(np.float64))
+    lo = bf16(d)
+    err = np.abs((hi.astype(np.float64) + lo) - u) / np.abs(u)
+    assert err.max() <= 2.0 ** -17
